@@ -1,0 +1,318 @@
+#!/usr/bin/env python
+"""Benchmark of the matrix-free Hamiltonian apply (and its Krylov drivers).
+
+Headline (`value`): plain FP64 single-vector H-apply throughput, basis
+states per second, on the 96-spin pyrochlore 1x2x3 cubic supercell restricted
+to the equal-polarisation (12.12.12.12, zero-winding) sector, H = ring exchange
++ Zeeman with seeded parameters.  One step = one y = H x over the whole sector.
+Beside it: the batched mixed-precision apply (R FP32 vectors, FP64 row
+accumulation) in state-vectors/s, FTLM vector-steps/s, the end-to-end rate
+through the C-ABI with host buffers, the kernel's HBM roofline and the CPU
+push loop of the reference (oracle restatement) on the host cores.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Under torchrun (N>1) each rank runs an independent replica on its own GPU
+(the apply does not shard across GPUs in this build); `value` sums the ranks'
+states over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "H-apply states/s, FTLM vec-steps/s: batched mixed vs plain FP64 GPU, |dE|<=1e-9"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--lattice", default="pyro_1x2x3", help="pyro_1x2x1 | pyro_1x2x2 | pyro_1x2x3")
+    p.add_argument("--full-basis", action="store_true", help="all Q=0 states instead of the equal sector")
+    p.add_argument("--R", type=int, default=32, help="vectors of the batched mixed apply")
+    p.add_argument("--seed", type=int, default=3)
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
+    p.add_argument("--no-extras", action="store_true", help="skip batched / FTLM / e2e legs")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(args):
+    from qsi_subspace_ed_gb300 import workloads
+
+    t0 = time.time()
+    lat = workloads.lattice(args.lattice)
+    if args.full_basis:
+        import qsi_subspace_ed_gb300 as q
+
+        g, B = workloads.ring_zeeman_params(args.seed, (0.2, 1.0), 0.5)
+        w = workloads.Workload(f"{args.lattice}.Q0", lat, q.enumerate_basis(lat), g, B)
+    else:
+        w = workloads.sector_workload(args.lattice, seed=args.seed)
+    return w, time.time() - t0
+
+
+def cpu_baseline(w, H, seconds: float):
+    """The reference's push loop (oracle restatement) on all host cores, over a bounded row sample."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    threads = O.cpu_threads()
+    terms = O.terms_array(H.specs())
+    n = len(w.basis_lohi)
+    x = np.random.default_rng(0).standard_normal(n)
+    y = np.zeros(n)
+    rows = min(n, 20000)
+    t0 = time.time()
+    O.apply_rows_port(w.basis_lohi, terms, x, y, 0, rows, threads)
+    dt = time.time() - t0
+    if dt < seconds / 4 and rows < n:
+        rows = int(min(n, rows * max(1.0, seconds / max(dt, 1e-3))))
+        y[:] = 0
+        t0 = time.time()
+        O.apply_rows_port(w.basis_lohi, terms, x, y, 0, rows, threads)
+        dt = time.time() - t0
+    return {"value": rows / dt, "unit": "states/s", "cores": threads, "kind": "port",
+            "sample": f"push-form apply (per-term OpenMP pass, atomic scatter, binary search) over source rows "
+                      f"[0,{rows}) of {n} of {w.name}; {dt:.1f}s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    w, setup_s = make_workload(args)
+    H = w.hamiltonian()
+    steps = []
+    base = None
+    for _ in range(max(1, args.warmup)):
+        cpu_baseline(w, H, min(args.cpu_seconds, 5.0))
+    for _ in range(args.steps):
+        base = cpu_baseline(w, H, args.cpu_seconds / max(1, args.steps) * 3)
+        steps.append(base["value"])
+    v = statistics.median(steps)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "states/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * len(w.basis_lohi) / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ring/Zeeman parameters)",
+            "config": {"workload": w.name, "n_states": int(len(w.basis_lohi)), "n_terms": len(H),
+                       "parallelism": "host OpenMP"},
+            "cpu_baseline": {**base, "value": v},
+            "e2e": {"value": v, "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import qsi_subspace_ed_gb300 as q
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w, setup_s = make_workload(args)
+    H = w.hamiltonian()
+    n = len(w.basis_lohi)
+    basis = q.ZBasis(w.basis_lohi)
+    op = q.LazyOpSum(basis, H)
+    hits, misses = op.connectivity()
+    h = hits / n
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    x = torch.randn(n, dtype=torch.float64, device=dev)
+    y = torch.zeros_like(x)
+    l2_flush = torch.empty(256 * 2**20, dtype=torch.uint8, device=dev)
+    inputs_exceed_l2 = (n * 16 + n * 8) > 2 * 129 * 2**20
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        op.evaluate(x, y)
+    torch.cuda.synchronize()
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t_wall = time.time()
+        for s in range(args.steps):
+            if not inputs_exceed_l2:
+                l2_flush.fill_(s & 0xff)
+            ev[s][0].record(stream)
+            op.evaluate(x, y)
+            ev[s][1].record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.time() - t_wall
+    barrier()
+    per = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(per) / len(per)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * n / (ms * 1e-3)
+    peak, peak_kind = measured_peaks()
+    bytes_per_row = 16 + 8 + 8 * h + 8
+    achieved = n * bytes_per_row / (ms * 1e-3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "apply_traffic.json"
+    if tp.exists():
+        tj = json.load(open(tp))
+        if tj.get("kernel") == "k_apply_rowthread" and tj.get("bytes_per_row"):
+            traffic = tj["bytes_per_row"] * n
+    line = {"metric": METRIC, "value": value, "unit": "states/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ring/Zeeman parameters, N(0,1) vectors)",
+            "config": {"workload": w.name, "n_states": n, "n_terms": len(H), "offdiag_hits_per_row": round(h, 4),
+                       "misses": misses, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs larger than L2" if inputs_exceed_l2 else "L2 flushed between steps",
+                       "setup_s": round(setup_s, 2)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "bytes_per_row": bytes_per_row, "kernel": "k_apply_rowthread"},
+            "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": t_wall}
+    if not args.no_extras and rank == 0:
+        # batched mixed precision: R FP32 vectors [row][R], FP64 row accumulation
+        R = args.R
+        X = torch.randn(n, R, dtype=torch.float32, device=dev)
+        Y = torch.zeros_like(X)
+        for _ in range(2):
+            op.apply_batched(X, Y)
+        torch.cuda.synchronize()
+        kb = max(3, args.steps // 2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(kb):
+            op.apply_batched(X, Y)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        bms = e0.elapsed_time(e1) / kb
+        bval = n * R / (bms * 1e-3)
+        bbytes = n * (16 + R * 4 * (h + 2))
+        line["batched_mixed"] = {"value": bval, "unit": "state-vectors/s", "R": R, "ms_per_apply": bms,
+                                 "vs_plain_fp64": bval / value * ws,
+                                 "roofline_frac": bbytes / (bms * 1e-3) / 1e9 / peak}
+        line["gpu_launches"] += kb
+        del X, Y
+        # FTLM vector-steps/s on the same operator (R vectors, M plain Lanczos steps)
+        Mf = 20
+        t0 = time.time()
+        q.ftlm([op], [R], M=Mf, seed=1, precision="mixed")
+        tf = time.time() - t0
+        line["ftlm"] = {"value": R * Mf / tf, "unit": "vec-steps/s", "R": R, "M": Mf, "precision": "mixed",
+                        "note": "includes graph capture and host readout"}
+        # end to end through the C-ABI with pinned host buffers (copies inside the timed region)
+        xh = torch.randn(n, dtype=torch.float64).pin_memory()
+        yh = torch.zeros(n, dtype=torch.float64).pin_memory()
+        lib = q.load()
+        lib.qsi_op_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), 0, 0, None)
+        ke = max(3, args.steps // 2)
+        t0 = time.time()
+        for _ in range(ke):
+            st = lib.qsi_op_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), 0, 0, None)
+            assert st == 0, q._lib.last_error()
+        te = (time.time() - t0) / ke
+        line["e2e"] = {"value": n / te, "unit": "states/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
+                       "api": "qsi_op_apply(host pointers)"}
+        line["cpu_baseline"] = cpu_baseline(w, H, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,224 @@
+/*
+ * qsi_ed.h — C-ABI of the GB300 matrix-free Hamiltonian engine for
+ * projected exact diagonalisation of quantum-spin-ice ring-exchange models.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns a qsi_status.  No C++ exception crosses this boundary; the text of
+ * the last error on the calling thread is available from qsi_last_error().
+ *
+ * Conventions (shared with qsi_subspace_ED):
+ *   - spin i is bit i of a 128-bit state; 1 = up, 0 = down
+ *     (components/common/include/bittools.hpp:69-81, README.md:146);
+ *   - a 128-bit state is stored as two uint64 words, LOW word first
+ *     (Uint128::uint64[0] is the low word; the HDF5 basis row is [lo, hi],
+ *     components/common/include/basis_io_h5.hpp:34,55);
+ *   - a basis is a strictly increasing array of such states.
+ *
+ * Pointer kinds: entry points that take vectors accept either host or device
+ * memory, selected by QSI_PTR_HOST / QSI_PTR_DEVICE in `flags`.  With host
+ * pointers the call copies in, computes on the GPU and copies out, and is
+ * synchronous.  With device pointers the work is enqueued on `stream`
+ * (a cudaStream_t, or NULL for the handle's own stream).
+ */
+#ifndef QSI_ED_H
+#define QSI_ED_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum qsi_status {
+    QSI_OK = 0,
+    QSI_INVALID_ARG = 1,   /* bad spec / size / pointer (bad_operator_spec, std::logic_error) */
+    QSI_OOM = 2,           /* device or host allocation failed */
+    QSI_CUDA_ERROR = 3,    /* a CUDA runtime call failed */
+    QSI_NOT_CONVERGED = 4, /* solver hit its iteration limit (Spectra CompInfo != Successful) */
+    QSI_TIMEOUT = 5,       /* a bounded wait ran out */
+    QSI_IO_ERROR = 6,      /* file missing / malformed (std::runtime_error in basis IO) */
+    QSI_NOT_FOUND = 7      /* dataset or state not present */
+} qsi_status;
+
+enum { QSI_PTR_HOST = 0, QSI_PTR_DEVICE = 1 };
+enum { QSI_F64 = 0, QSI_F32 = 1 };
+
+/* One compiled operator term: coefficient times SymbolicPMROperator.
+ * The mask fields are exactly SymbolicPMROperator's protected members
+ * (components/operator/include/operator.hpp:343-347), each as [lo, hi]. */
+typedef struct qsi_term {
+    double c;
+    uint64_t x[2];     /* X_mask: bits flipped */
+    uint64_t z[2];     /* Z_mask: sign (-1)^popcount(~state' & Z) */
+    uint64_t up[2];    /* state & up must equal up */
+    uint64_t down[2];  /* state & down must be 0 */
+    int32_t sign;      /* overall sign, 0 when the operator vanished at construction */
+    int32_t reserved;
+} qsi_term;
+
+typedef struct qsi_basis qsi_basis; /* device-resident sorted basis + bucket table */
+typedef struct qsi_op qsi_op;       /* operator bound to a basis */
+
+/* ---------------------------------------------------------------- errors */
+const char* qsi_version(void);
+/* Copies the calling thread's last error message into buf (NUL-terminated). */
+qsi_status qsi_last_error(char* buf, size_t len);
+
+/* ---------------------------------------------------------------- terms */
+/* SymbolicPMROperator(opstring, spin_ids) (operator.hpp:223-227, _construct
+ * :383-466).  ops is a string of n characters from "xXzZ+-pPqQ". */
+qsi_status qsi_term_compile(const char* ops, const int32_t* spin_ids, int32_t n,
+                            double c, qsi_term* out);
+/* SymbolicPMROperator(const std::string& spec), e.g. "0+ 1- 12z"
+ * (operator.hpp:229-232, parseSpec :349-381). */
+qsi_status qsi_term_parse(const char* spec, double c, qsi_term* out);
+/* a *= b (SymbolicPMROperator::operator*=, operator.hpp:312-330); coefficients multiply. */
+qsi_status qsi_term_mul(qsi_term* a, const qsi_term* b);
+/* Applies one term to one state, as SymbolicPMROperator::applyState
+ * (operator.hpp:232-254): state is updated in place, the sign is returned in *sign. */
+qsi_status qsi_term_apply_state(const qsi_term* t, uint64_t state[2], int32_t* sign);
+
+/* ---------------------------------------------------------------- basis files */
+/* Reads dataset `dataset` (uint64[N][2]) of an HDF5 basis file
+ * (basis_io::read_basis_hdf5, basis_io_h5.hpp:90-141).  Call with out=NULL to
+ * learn n; then call again with cap >= n. */
+qsi_status qsi_h5_read_basis(const char* path, const char* dataset,
+                             uint64_t* out_lohi, int64_t cap, int64_t* n_out);
+/* Reads a float64 dataset of any rank; dims_out receives up to 4 dims. */
+qsi_status qsi_h5_read_f64(const char* path, const char* dataset, double* out,
+                           int64_t cap, int64_t* n_out, int64_t* dims_out, int32_t* rank_out);
+/* Writes a basis file with one uint64[N][2] dataset per call (creates or
+ * truncates the file when `append` is 0) (basis_io_h5.hpp:30-70). */
+qsi_status qsi_h5_write_basis(const char* path, const char* dataset,
+                              const uint64_t* lohi, int64_t n, int32_t append);
+/* Writes the .eigs.h5 layout of diag_DOQSI_ham (src/diag_DOQSI_ham.cpp:143-173):
+ * eigenvalues (nev), eigenvectors (dim x nvec, the Eigen column-major bytes
+ * under a row-major (dim, nvec) shape), latfile_json and dset_name strings. */
+qsi_status qsi_h5_write_eigs(const char* path, const double* evals, int64_t nev,
+                             const double* evecs, int64_t dim, int64_t nvec,
+                             const char* latfile_json, const char* dset_name);
+/* CSV basis "0x%016hi%016lo" per line (basis_io.hpp:16-53). */
+qsi_status qsi_csv_read_basis(const char* path, uint64_t* out_lohi, int64_t cap, int64_t* n_out);
+
+/* ---------------------------------------------------------------- enumeration */
+/* Enumerates the spin-ice basis: every state whose tetrahedra satisfy the
+ * ice rule (member count up in [n/2, (n+1)/2]), with up to n_spinon_pairs
+ * rule violations admitted by the gen_spinon_basis rule
+ * (components/build_basis/src/pyro_tree.cpp:20-189), optionally restricted to
+ * a sublattice polarisation sector.  tetra_spins holds n_tetra rows of
+ * tetra_size spin ids.  ordering: 0 = spins in index order, 1 = the greedy
+ * tetrahedron-overlap order of lattice::greedy_spin_ordering
+ * (components/common/src/tetra_graph_io.cpp:105-150).  sector may be NULL.
+ * The result is sorted and written to *out_lohi (release with qsi_free_host). */
+qsi_status qsi_enumerate_basis(int32_t n_spins, const int32_t* tetra_spins,
+                               int32_t n_tetra, int32_t tetra_size,
+                               const int32_t* sublattice, int32_t n_sublattices,
+                               int32_t n_spinon_pairs, const int32_t* sector,
+                               int32_t ordering, int32_t n_threads,
+                               uint64_t** out_lohi, int64_t* n_out);
+void qsi_free_host(void* p);
+
+/* ---------------------------------------------------------------- device basis */
+/* Copies a sorted basis to the device and builds its top-bits bucket table.
+ * bucket_bits <= 0 picks a size automatically.  The caller keeps its buffer
+ * (LazyOpSum holds a non-owning basis reference, operator_matrix.hpp:116). */
+qsi_status qsi_basis_create(const uint64_t* lohi, int64_t n, int32_t bucket_bits,
+                            qsi_basis** out);
+qsi_status qsi_basis_destroy(qsi_basis* b);
+qsi_status qsi_basis_dim(const qsi_basis* b, int64_t* dim);
+/* Exact index lookup of n states (ZBasisBST::search, operator.cpp:4-34):
+ * idx[k] = position of states[k] in the basis, or -1 on a miss. */
+qsi_status qsi_basis_search(qsi_basis* b, const uint64_t* states_lohi, int64_t n,
+                            int64_t* idx, int32_t flags, void* stream);
+
+/* ---------------------------------------------------------------- operator */
+/* LazyOpSum(basis, ops) (operator_matrix.hpp:13-17): copies the term list. */
+qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t n_terms,
+                         qsi_op** out);
+qsi_status qsi_op_destroy(qsi_op* op);
+/* accumulate = 0: y = H x   (LazyOpSumProd::perform_op / LazyOpSum::evaluate,
+ *                            operator_matrix.hpp:32-36,129-131)
+ * accumulate = 1: y += H x  (LazyOpSum::evaluate_add, operator_matrix.cpp:108-112;
+ *                            the RealApplyFn contract, common_bits.hpp:18-23) */
+qsi_status qsi_op_apply(qsi_op* op, const double* x, double* y, int32_t accumulate,
+                        int32_t flags, void* stream);
+/* Batched apply over R vectors stored row-major [dim][R] (element type dtype:
+ * QSI_F64, or QSI_F32 storage with FP64 per-row accumulation). */
+qsi_status qsi_op_apply_batched(qsi_op* op, const void* X, void* Y, int32_t R,
+                                int32_t dtype, int32_t accumulate, int32_t flags,
+                                void* stream);
+/* Connectivity export in the order of LazyOpSum::toSparseMatrix
+ * (operator_matrix.hpp:79-105): for each basis index j, each off-diagonal
+ * term with |c*sign| > tol gives (J, j, c*sign); then (j, j, sum of diagonal
+ * terms).  Call with rows=NULL to get the count. */
+qsi_status qsi_op_triplets(qsi_op* op, double tol, int64_t* rows, int64_t* cols,
+                           double* vals, int64_t cap, int64_t* n_out);
+/* Number of off-diagonal terms whose flipped state is not in the basis,
+ * summed over all rows (projected-ED drops them). */
+qsi_status qsi_op_count_misses(qsi_op* op, int64_t* misses);
+/* Off-diagonal terms over all rows that land in the basis (hits: the
+ * off-diagonal non-zeros of H) and that leave it (misses). */
+qsi_status qsi_op_connectivity(qsi_op* op, int64_t* hits, int64_t* misses);
+
+/* ---------------------------------------------------------------- solvers */
+typedef struct qsi_lanczos_cfg {
+    int32_t nev;          /* eigenpairs wanted (smallest algebraic) */
+    int32_t ncv;          /* Krylov subspace dimension (-k/--ncv) */
+    int32_t max_iter;     /* restart limit (--max_iters) */
+    int32_t precision;    /* QSI_F64, or QSI_F32 = FP32 vectors + FP64 recurrences */
+    double tol;           /* relative residual tolerance (10^--atol) */
+    uint64_t seed;        /* start vector seed (N(0,1)) */
+    int32_t polish_steps; /* FP64 Rayleigh-Ritz polish rounds after convergence */
+    int32_t want_vectors; /* write eigenvectors */
+} qsi_lanczos_cfg;
+
+typedef struct qsi_report {
+    int32_t converged;      /* eigenpairs converged */
+    int32_t restarts;
+    int64_t applies;        /* operator applications */
+    double residual[64];    /* ||H v - lambda v|| per eigenpair (FP64) */
+    double seconds;
+} qsi_report;
+
+/* Thick-restart Lanczos for the nev smallest eigenpairs with full
+ * reorthogonalisation (the mfsparse path: compute_spectrum_iterative,
+ * include/matrix_diag_bits.hpp:51-95).  evecs is dim x nev, vector-major. */
+qsi_status qsi_lanczos_solve(qsi_op* op, const qsi_lanczos_cfg* cfg, double* evals,
+                             double* evecs, qsi_report* report);
+
+/* Plain 3-term Lanczos ground state without reorthogonalisation and the
+ * two-pass eigenvector of projED::lanczos::eigval0 (mfeig0 path,
+ * components/linalg_routines/src/lanczos.cpp:67-227). */
+typedef struct qsi_eigval0_cfg {
+    int32_t max_iterations;
+    int32_t min_iterations;
+    double abs_tol;
+    double rel_tol;
+    uint64_t seed;
+    int32_t calc_eigenvector;
+    int32_t reserved;
+} qsi_eigval0_cfg;
+qsi_status qsi_eigval0(qsi_op* op, const qsi_eigval0_cfg* cfg, double* e0,
+                       double* eigvec, int32_t* iterations);
+
+/* Finite-temperature Lanczos over several sectors at once.  Each sector s has
+ * an operator ops[s] and R[s] random vectors; all run M Lanczos steps in one
+ * batched apply per step.  Outputs per sector: alphas/betas of every vector
+ * (R[s] x M each, concatenated over sectors). */
+qsi_status qsi_ftlm_run(qsi_op** ops, int32_t n_sectors, const int32_t* R,
+                        int32_t M, uint64_t seed, int32_t precision,
+                        double* alphas, double* betas);
+
+/* Batched eigen-decomposition of n_mat symmetric tridiagonal m x m matrices
+ * (diagonals a[k*m..], off-diagonals b[k*m..], the first m-1 used), m <= 128:
+ * ascending eigenvalues and the first component of each eigenvector — the
+ * Ritz values and weights of FTLM (the dense tridiagonal solve of
+ * components/linalg_routines/include/lapack_adapter.hpp:37-91, batched). */
+qsi_status qsi_tridiag_ritz(const double* a, const double* b, int32_t m, int32_t n_mat,
+                            double* evals, double* first);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QSI_ED_H */

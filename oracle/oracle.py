@@ -1,0 +1,261 @@
+"""ORACLE — test infrastructure, never product code.
+
+Python access to the two CPU checkers of the hot path:
+  * the plain-C restatement oracle/qsi_oracle.c  -> oracle/libqsi_oracle.so ("port")
+  * the reference's own operator.cpp + oracle/ref_harness.cpp -> oracle/_ref/libqsi_ref.so
+    (built only where the reference checkout exists)
+plus the FP64 eigen-oracle (scipy ARPACK eigsh / numpy eigh on the oracle's
+triplets, the same implicitly-restarted-Lanczos family as the Spectra solver
+behind mfsparse, include/matrix_diag_bits.hpp:51-95) and an exact
+thermodynamics oracle from the full spectrum (the dense branch of the
+reference's FTLM study, jl/calc_Cv_ftlm.jl:114-139: Boltzmann weights with
+the ground state subtracted, C = beta^2 (<E^2> - <E>^2)).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_SO = HERE / "libqsi_oracle.so"
+REF_SO = HERE / "_ref" / "libqsi_ref.so"
+
+
+def build_port() -> Path:
+    src = HERE / "qsi_oracle.c"
+    if not PORT_SO.exists() or PORT_SO.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", str(src), "-o", str(PORT_SO)], check=True)
+    return PORT_SO
+
+
+def build_ref(reference_root: str = "/root/reference") -> Path | None:
+    if not Path(reference_root).exists():
+        return None
+    deps = [HERE / "ref_harness.cpp", HERE / "build_ref.sh", HERE / "ref_shim" / "hdf5.h"]
+    if not REF_SO.exists() or REF_SO.stat().st_mtime < max(d.stat().st_mtime for d in deps):
+        subprocess.run(["sh", str(HERE / "build_ref.sh"), reference_root], check=True, capture_output=True)
+    return REF_SO
+
+
+_port = None
+_ref = None
+
+
+def port():
+    global _port
+    if _port is None:
+        lib = C.CDLL(str(build_port()))
+        lib.oracle_apply_state.restype = C.c_int
+        lib.oracle_search.restype = C.c_int
+        lib.oracle_evaluate_add.restype = C.c_int
+        lib.oracle_triplets.restype = C.c_int64
+        lib.oracle_term_compile.restype = C.c_int
+        lib.oracle_dot.restype = C.c_double
+        lib.oracle_dot.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+        lib.oracle_axpby.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64]
+        lib.oracle_triplets.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_double, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]
+        lib.oracle_evaluate_add.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                            C.c_int]
+        lib.oracle_term_compile.argtypes = [C.c_char_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]
+        lib.oracle_apply_state.argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_evaluate_add_rows.restype = C.c_int
+        lib.oracle_evaluate_add_rows.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_int,
+                                                 C.c_void_p, C.c_void_p, C.c_int]
+        _port = lib
+    return _port
+
+
+def ref():
+    """The reference-built checker, or None where the reference is absent."""
+    global _ref
+    if _ref is None:
+        p = build_ref()
+        if p is None or not p.exists():
+            return None
+        lib = C.CDLL(str(p))
+        lib.ref_term_masks.restype = C.c_int
+        lib.ref_apply_state.restype = C.c_int
+        lib.ref_triplets.restype = C.c_int64
+        _ref = lib
+    return _ref
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+# ------------------------------------------------------------------ port wrappers
+def terms_array(specs):
+    """specs: list of (c, ops, ids) -> numpy structured bytes in qsi_term layout, compiled by the port."""
+    lib = port()
+    buf = np.zeros((max(1, len(specs)), 80), dtype=np.uint8)
+    for k, (c, ops, ids) in enumerate(specs):
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        rc = lib.oracle_term_compile(ops.encode(), _p(ids), len(ops), float(c), buf[k].ctypes.data_as(C.c_void_p))
+        if rc != 0:
+            raise ValueError(f"bad operator spec {ops!r}")
+    return buf[: len(specs)].copy()
+
+
+def apply_port(basis: np.ndarray, specs, x: np.ndarray, y: np.ndarray | None = None, threads: int = 0):
+    """y += H x by the restated push loop (y = H x when y is None)."""
+    t = terms_array(specs)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x) if y is None else y
+    port().oracle_evaluate_add(_p(basis), len(basis), _p(t), len(specs), _p(x), _p(y), threads)
+    return y
+
+
+def apply_rows_port(basis: np.ndarray, terms: np.ndarray, x: np.ndarray, y: np.ndarray, row_begin: int,
+                    row_end: int, threads: int = 0) -> None:
+    """Push loop over source rows [row_begin, row_end) only (CPU-baseline sample)."""
+    port().oracle_evaluate_add_rows(_p(basis), len(basis), row_begin, row_end, _p(terms), len(terms), _p(x), _p(y),
+                                    threads)
+
+
+def triplets_port(basis: np.ndarray, specs, tol: float = 1e-14):
+    t = terms_array(specs)
+    n = port().oracle_triplets(_p(basis), len(basis), _p(t), len(specs), tol, None, None, None)
+    r = np.zeros(n, np.int64)
+    c = np.zeros(n, np.int64)
+    v = np.zeros(n, np.float64)
+    port().oracle_triplets(_p(basis), len(basis), _p(t), len(specs), tol, _p(r), _p(c), _p(v))
+    return r, c, v
+
+
+# ------------------------------------------------------------------ reference-built wrappers
+def _spec_args(specs):
+    ops = (C.c_char_p * len(specs))(*[s[1].encode() for s in specs])
+    idarrs = [np.ascontiguousarray(s[2], dtype=np.int32) for s in specs]
+    ids = (C.c_void_p * len(specs))(*[a.ctypes.data for a in idarrs])
+    lens = np.array([len(s[1]) for s in specs], dtype=np.int32)
+    coef = np.array([s[0] for s in specs], dtype=np.float64)
+    return ops, ids, lens, coef, idarrs
+
+
+def term_masks_ref(ops: str, ids):
+    lib = ref()
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    m = np.zeros(8, np.uint64)
+    sg = C.c_int()
+    rc = lib.ref_term_masks(ops.encode(), _p(ids), len(ops), _p(m), C.byref(sg))
+    if rc != 0:
+        raise ValueError("bad operator spec")
+    return m, sg.value
+
+
+def triplets_ref(basis: np.ndarray, specs, tol: float = 1e-14):
+    lib = ref()
+    ops, ids, lens, coef, keep = _spec_args(specs)
+    args = (_p(basis), C.c_int64(len(basis)), ops, ids, _p(lens), _p(coef), C.c_int(len(specs)), C.c_double(tol))
+    n = lib.ref_triplets(*args, None, None, None)
+    r = np.zeros(n, np.int64)
+    c = np.zeros(n, np.int64)
+    v = np.zeros(n, np.float64)
+    lib.ref_triplets(*args, _p(r), _p(c), _p(v))
+    return r, c, v
+
+
+def apply_ref(basis: np.ndarray, specs, x: np.ndarray, threads: int = 0):
+    lib = ref()
+    ops, ids, lens, coef, keep = _spec_args(specs)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x)
+    lib.ref_evaluate_add(_p(basis), C.c_int64(len(basis)), ops, ids, _p(lens), _p(coef), C.c_int(len(specs)), _p(x),
+                         _p(y), C.c_int(threads))
+    return y
+
+
+def search_ref(basis: np.ndarray, queries: np.ndarray):
+    lib = ref()
+    q = np.ascontiguousarray(queries, dtype=np.uint64)
+    idx = np.zeros(len(q), np.int64)
+    lib.ref_search(_p(basis), C.c_int64(len(basis)), _p(q), C.c_int64(len(q)), _p(idx))
+    return idx
+
+
+# ------------------------------------------------------------------ checksums and eigen-oracles
+def triplet_digest(r, c, v) -> str:
+    h = hashlib.sha256()
+    for a in (r, c, v):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def csr_from_triplets(r, c, v, n):
+    import scipy.sparse as sp
+
+    return sp.csr_matrix((v, (r, c)), shape=(n, n))
+
+
+def lowest_eigs(r, c, v, n, k=1, tol=1e-13, v0_seed=0):
+    """FP64 eigen-oracle: numpy eigh (n <= 4000) or scipy eigsh(which='SA')."""
+    H = csr_from_triplets(r, c, v, n)
+    if n <= 4000:
+        w, V = np.linalg.eigh(H.toarray())
+        return w[:k], V[:, :k]
+    from scipy.sparse.linalg import eigsh
+
+    rng = np.random.default_rng(v0_seed)
+    w, V = eigsh(H, k=k, which="SA", tol=tol, v0=rng.standard_normal(n), ncv=max(2 * k + 1, 30))
+    o = np.argsort(w)
+    return w[o], V[:, o]
+
+
+def exact_thermo(evals: np.ndarray, temps: np.ndarray):
+    """E(T), C(T) from a full spectrum with the ground state subtracted."""
+    e = np.asarray(evals, np.float64)
+    e0 = e.min()
+    x = e - e0
+    bf = np.exp(-np.outer(1.0 / np.asarray(temps), x))
+    Z = bf.sum(1)
+    E1 = (bf @ x) / Z
+    E2 = (bf @ (x * x)) / Z
+    return {"T": np.asarray(temps), "E": E1 + e0, "C": (E2 - E1 * E1) / np.asarray(temps) ** 2}
+
+
+def ftlm_oracle(r, c, v, n, R, M, seed, temps):
+    """Per-vector FP64 FTLM (plain Lanczos, M steps) over R Rademacher vectors, numpy on the CPU."""
+    H = csr_from_triplets(r, c, v, n)
+    rng = np.random.default_rng(seed)
+    ev_all, w_all = [], []
+    for _ in range(R):
+        q = rng.choice([-1.0, 1.0], size=n) / np.sqrt(n)
+        qp = np.zeros(n)
+        a, b = [], []
+        beta = 0.0
+        for j in range(M):
+            w = H @ q
+            al = q @ w
+            w = w - al * q - beta * qp
+            beta = np.linalg.norm(w)
+            a.append(al)
+            b.append(beta)
+            qp, q = q, w / beta
+        T = np.diag(a) + np.diag(b[:-1], 1) + np.diag(b[:-1], -1)
+        ew, Y = np.linalg.eigh(T)
+        ev_all.append(ew)
+        w_all.append(Y[0] ** 2)
+    ev = np.array(ev_all)
+    w = np.array(w_all)
+    e0 = ev.min()
+    x = (ev - e0).reshape(-1)
+    ww = w.reshape(-1) * (n / R)
+    bf = np.exp(-np.outer(1.0 / np.asarray(temps), x))
+    Z = bf @ ww
+    E1 = (bf @ (ww * x)) / Z
+    E2 = (bf @ (ww * x * x)) / Z
+    return {"T": np.asarray(temps), "E": E1 + e0, "C": (E2 - E1 * E1) / np.asarray(temps) ** 2, "ritz": ev,
+            "weights": w}
+
+
+def cpu_threads() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)

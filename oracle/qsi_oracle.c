@@ -1,0 +1,286 @@
+/*
+ * ORACLE — test infrastructure, not product code.
+ *
+ * Plain-C restatement of qsi_subspace_ED's CPU hot path, used only by
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+ * checker.  It follows the reference's loops one to one:
+ *
+ *   oracle_term_compile   SymbolicPMROperator::_construct
+ *                         (components/operator/include/operator.hpp:383-466)
+ *   oracle_apply_state    SymbolicPMROperator::applyState (operator.hpp:232-254)
+ *   oracle_search         ZBasisBST::search (components/operator/src/operator.cpp:4-34)
+ *   oracle_evaluate_add   LazyOpSum::evaluate_add_off_diag_omp + evaluate_add_diagonal
+ *                         (components/operator/src/operator_matrix.cpp:28-82,108-112):
+ *                         per term, an OpenMP loop over rows, push y[J] += c x[i] sign
+ *                         with an atomic update, |x[i]| <= 1e-15 skipped
+ *   oracle_triplets       LazyOpSum::toSparseMatrix (operator_matrix.hpp:79-105)
+ *
+ * Terms use the qsi_term layout of include/qsi_ed.h; they are split into
+ * off-diagonal (X != 0) and diagonal lists in the given order, as
+ * SymbolicOpSum::add_term does (operator.hpp:489-495).
+ *
+ * Its pin: tests/golden holds checksums of the same quantities computed by
+ * the reference's own operator.cpp (oracle/build_ref.sh -> oracle/_ref).
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef unsigned __int128 u128;
+
+typedef struct {
+    double c;
+    uint64_t x[2], z[2], up[2], down[2];
+    int32_t sign, reserved;
+} oterm;
+
+static inline u128 mk(const uint64_t w[2]) { return ((u128)w[1] << 64) | w[0]; }
+static inline int popc128(u128 v) { return __builtin_popcountll((uint64_t)v) + __builtin_popcountll((uint64_t)(v >> 64)); }
+
+/* applyState: ok = (s & down)==0 && (s & up)==up ; s ^= X if ok ;
+ * returns sign * (-1)^popcount(~s & Z) * ok */
+int oracle_apply_state(const oterm* t, uint64_t st[2]) {
+    u128 s = mk(st), d = mk(t->down), u = mk(t->up), X = mk(t->x), Z = mk(t->z);
+    int ok = ((s & d) == 0) && ((s & u) == u);
+    u128 m = (u128)0 - (u128)ok;
+    s = s ^ (X & m);
+    st[0] = (uint64_t)s;
+    st[1] = (uint64_t)(s >> 64);
+    return t->sign * (1 - 2 * (popc128(~s & Z) % 2)) * ok;
+}
+
+/* ZBasisBST::search: lower-bound bisection while the window exceeds 32
+ * entries, then a linear scan of [left, right]. */
+int oracle_search(const uint64_t* basis, int64_t n, const uint64_t st[2], int64_t* J) {
+    const u128 s = mk(st);
+    int64_t left = 0, right = n - 1;
+    while (right - left > 32) {
+        int64_t mid = (left + right) / 2;
+        if (mk(basis + 2 * mid) < s) left = mid + 1;
+        else right = mid;
+    }
+    for (int64_t j = left; j <= right; ++j) {
+        if (j >= 0 && mk(basis + 2 * j) == s) {
+            *J = j;
+            return 1;
+        }
+    }
+    *J = right + 1;
+    return 0;
+}
+
+static void split_terms(const oterm* terms, int n, const oterm** off, int* n_off, const oterm** dg, int* n_dg) {
+    int a = 0, b = 0;
+    for (int k = 0; k < n; ++k) {
+        if ((terms[k].x[0] | terms[k].x[1]) != 0) off[a++] = &terms[k];
+        else dg[b++] = &terms[k];
+    }
+    *n_off = a;
+    *n_dg = b;
+}
+
+/* y += H x, push form with atomics, one parallel pass per term. */
+int oracle_evaluate_add(const uint64_t* basis, int64_t n, const oterm* terms, int n_terms, const double* x, double* y,
+                        int n_threads) {
+    const oterm** off = (const oterm**)malloc(sizeof(oterm*) * (size_t)(n_terms + 1));
+    const oterm** dg = (const oterm**)malloc(sizeof(oterm*) * (size_t)(n_terms + 1));
+    if (!off || !dg) return -1;
+    int n_off, n_dg;
+    split_terms(terms, n_terms, off, &n_off, dg, &n_dg);
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+    (void)n_threads;
+#endif
+    for (int t = 0; t < n_off; ++t) {
+        const oterm* T = off[t];
+        const double c = T->c;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            uint64_t st[2] = {basis[2 * i], basis[2 * i + 1]};
+            int sign = oracle_apply_state(T, st);
+            if (sign != 0 && fabs(x[i]) > 1e-15) {
+                int64_t J;
+                sign *= oracle_search(basis, n, st, &J);
+                /* the reference writes y[J] += 0 on a miss, with J possibly == n;
+                 * the restatement skips that write */
+                if (sign != 0) {
+                    double dy = c * x[i] * sign;
+#pragma omp atomic
+                    y[J] += dy;
+                }
+            }
+        }
+    }
+    for (int t = 0; t < n_dg; ++t) {
+        const oterm* T = dg[t];
+        const double c = T->c;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            uint64_t st[2] = {basis[2 * i], basis[2 * i + 1]};
+            double dy = c * x[i] * (double)oracle_apply_state(T, st);
+            y[i] += dy;
+        }
+    }
+    free(off);
+    free(dg);
+    return 0;
+}
+
+/* The same push loop restricted to source rows [row_begin, row_end): a
+ * bounded sample of one apply for timing the CPU path on large bases. */
+int oracle_evaluate_add_rows(const uint64_t* basis, int64_t n, int64_t row_begin, int64_t row_end, const oterm* terms,
+                             int n_terms, const double* x, double* y, int n_threads) {
+    const oterm** off = (const oterm**)malloc(sizeof(oterm*) * (size_t)(n_terms + 1));
+    const oterm** dg = (const oterm**)malloc(sizeof(oterm*) * (size_t)(n_terms + 1));
+    if (!off || !dg) return -1;
+    int n_off, n_dg;
+    split_terms(terms, n_terms, off, &n_off, dg, &n_dg);
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+    (void)n_threads;
+#endif
+    for (int t = 0; t < n_off; ++t) {
+        const oterm* T = off[t];
+        const double c = T->c;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = row_begin; i < row_end; ++i) {
+            uint64_t st[2] = {basis[2 * i], basis[2 * i + 1]};
+            int sign = oracle_apply_state(T, st);
+            if (sign != 0 && fabs(x[i]) > 1e-15) {
+                int64_t J;
+                sign *= oracle_search(basis, n, st, &J);
+                if (sign != 0) {
+                    double dy = c * x[i] * sign;
+#pragma omp atomic
+                    y[J] += dy;
+                }
+            }
+        }
+    }
+    for (int t = 0; t < n_dg; ++t) {
+        const oterm* T = dg[t];
+        const double c = T->c;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = row_begin; i < row_end; ++i) {
+            uint64_t st[2] = {basis[2 * i], basis[2 * i + 1]};
+            y[i] += c * x[i] * (double)oracle_apply_state(T, st);
+        }
+    }
+    free(off);
+    free(dg);
+    return 0;
+}
+
+/* toSparseMatrix triplets in the reference's order; rows==NULL counts only. */
+int64_t oracle_triplets(const uint64_t* basis, int64_t n, const oterm* terms, int n_terms, double tol, int64_t* rows,
+                        int64_t* cols, double* vals) {
+    const oterm** off = (const oterm**)malloc(sizeof(oterm*) * (size_t)(n_terms + 1));
+    const oterm** dg = (const oterm**)malloc(sizeof(oterm*) * (size_t)(n_terms + 1));
+    if (!off || !dg) return -1;
+    int n_off, n_dg;
+    split_terms(terms, n_terms, off, &n_off, dg, &n_dg);
+    int64_t w = 0;
+    for (int64_t j = 0; j < n; ++j) {
+        for (int t = 0; t < n_off; ++t) {
+            uint64_t st[2] = {basis[2 * j], basis[2 * j + 1]};
+            int sign = oracle_apply_state(off[t], st);
+            int64_t J = j;
+            if (sign != 0) sign *= oracle_search(basis, n, st, &J);
+            double res = off[t]->c * sign;
+            if (fabs(res) > tol) {
+                if (rows) {
+                    rows[w] = J;
+                    cols[w] = j;
+                    vals[w] = res;
+                }
+                ++w;
+            }
+        }
+        double acc = 0;
+        for (int t = 0; t < n_dg; ++t) {
+            uint64_t st[2] = {basis[2 * j], basis[2 * j + 1]};
+            int sign = oracle_apply_state(dg[t], st);
+            int64_t J = j;
+            if (sign != 0) sign *= oracle_search(basis, n, st, &J);
+            acc += dg[t]->c * sign;
+        }
+        if (rows) {
+            rows[w] = j;
+            cols[w] = j;
+            vals[w] = acc;
+        }
+        ++w;
+    }
+    free(off);
+    free(dg);
+    return w;
+}
+
+/* _construct: right-to-left walk over (op, spin) pairs.  Returns 0, or -1 on
+ * an unknown op character (bad_operator_spec). */
+int oracle_term_compile(const char* ops, const int32_t* ids, int n, double c, oterm* out) {
+    u128 X = 0, Z = 0, up = 0, down = 0;
+    int sign = 1;
+    for (int i = n - 1; i >= 0; --i) {
+        const int J = ids[i];
+        const u128 b = (u128)1 << J;
+        switch (ops[i]) {
+            case 'x': case 'X':
+                X ^= b;
+                if (Z & b) sign = -sign;
+                break;
+            case 'z': case 'Z':
+                Z ^= b;
+                break;
+            case '+': case 'q': case 'Q':
+                if (down & X & b) { sign = 0; break; }
+                if (Z & b) sign = -sign;
+                X ^= b;
+                if (!(X & b)) up |= b;
+                else down |= b;
+                break;
+            case '-':
+                if (up & X & b) { sign = 0; break; }
+                if (Z & b) sign = -sign;
+                X ^= b;
+                if (!(X & b)) down |= b;
+                else up |= b;
+                break;
+            case 'p': case 'P':
+                if (up & X & b) { sign = 0; break; }
+                if (!(X & b)) down |= b;
+                else up |= b;
+                break;
+            default:
+                return -1;
+        }
+    }
+    out->c = c;
+    out->x[0] = (uint64_t)X, out->x[1] = (uint64_t)(X >> 64);
+    out->z[0] = (uint64_t)Z, out->z[1] = (uint64_t)(Z >> 64);
+    out->up[0] = (uint64_t)up, out->up[1] = (uint64_t)(up >> 64);
+    out->down[0] = (uint64_t)down, out->down[1] = (uint64_t)(down >> 64);
+    out->sign = sign;
+    out->reserved = 0;
+    return 0;
+}
+
+/* Plain three-term Lanczos step helpers for the CPU baseline of the Krylov
+ * loop (lanczos.cpp:117-146 with OpenMP dot/axpy in place of BLAS). */
+double oracle_dot(const double* a, const double* b, int64_t n) {
+    double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+void oracle_axpby(double* y, const double* x, double a, double b, int64_t n) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) y[i] = b * y[i] + a * x[i];
+}

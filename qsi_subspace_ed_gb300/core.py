@@ -1,0 +1,382 @@
+"""Host-side mirror of the reference's operator and basis API on top of the C-ABI.
+
+Names follow qsi_subspace_ED:
+  SymbolicPMROperator  components/operator/include/operator.hpp:215-467
+  SymbolicOpSum        operator.hpp:476-503
+  ZBasis               ZBasisBase/ZBasisBST/ZBasisInterp, operator.hpp:153-204
+  LazyOpSum            components/operator/include/operator_matrix.hpp:10-118
+  LazyOpSumProd        operator_matrix.hpp:120-139
+All arithmetic runs in libqsi_ed.so on the GPU (term compilation and basis
+enumeration are host C++ in the same library).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import Term, call, ptr
+
+
+# ---------------------------------------------------------------- operators
+def _parse_spec(spec: str):
+    """Token rule of parseSpec (operator.hpp:349-381): leading digits, then the op character."""
+    ops, ids = [], []
+    for tok in spec.split():
+        i = 0
+        while i < len(tok) - 1 and tok[i].isdigit():
+            i += 1
+        ops.append(tok[i])
+        ids.append(int(tok[:i]) if i else 0)
+    return "".join(ops), ids
+
+
+class SymbolicPMROperator:
+    """One permutation-matrix-representation operator: sign * Z X P."""
+
+    __slots__ = ("t", "spec")
+
+    def __init__(self, ops=None, spin_ids=None):
+        self.t = Term()
+        self.t.sign = 1
+        self.spec = ("", [])  # (op characters, spin ids) it was built from; None after products
+        if ops is None:
+            return
+        if spin_ids is None:  # spec string "0+ 1- 12z"
+            call("qsi_term_parse", str(ops).encode(), 1.0, C.byref(self.t))
+            self.spec = _parse_spec(str(ops))
+        else:
+            ops = "".join(ops)
+            ids = np.ascontiguousarray(spin_ids, dtype=np.int32)
+            call("qsi_term_compile", ops.encode(), ptr(ids), len(ops), 1.0, C.byref(self.t))
+            self.spec = (ops, [int(i) for i in ids])
+
+    @staticmethod
+    def _mask(pair) -> int:
+        return int(pair[0]) | (int(pair[1]) << 64)
+
+    @property
+    def X_mask(self) -> int:
+        return self._mask(self.t.x)
+
+    @property
+    def Z_mask(self) -> int:
+        return self._mask(self.t.z)
+
+    @property
+    def up_mask(self) -> int:
+        return self._mask(self.t.up)
+
+    @property
+    def down_mask(self) -> int:
+        return self._mask(self.t.down)
+
+    @property
+    def sign(self) -> int:
+        return int(self.t.sign)
+
+    def is_diagonal(self) -> bool:
+        return self.X_mask == 0
+
+    def applyState(self, state: int):
+        """Returns (new_state, sign) as SymbolicPMROperator::applyState."""
+        s = (C.c_uint64 * 2)(state & (2**64 - 1), state >> 64)
+        sg = C.c_int32()
+        call("qsi_term_apply_state", C.byref(self.t), C.cast(s, C.c_void_p), C.byref(sg))
+        return int(s[0]) | (int(s[1]) << 64), int(sg.value)
+
+    def __imul__(self, other):
+        if isinstance(other, int):
+            self.t.sign *= other
+            return self
+        call("qsi_term_mul", C.byref(self.t), C.byref(other.t))
+        self.spec = None
+        return self
+
+    def __mul__(self, other):
+        r = self.copy()
+        r *= other
+        return r
+
+    def __rmul__(self, m: int):
+        r = self.copy()
+        r.t.sign *= m
+        return r
+
+    def copy(self):
+        r = SymbolicPMROperator()
+        C.memmove(C.byref(r.t), C.byref(self.t), C.sizeof(Term))
+        r.spec = self.spec
+        return r
+
+    def __eq__(self, o):
+        return (self.X_mask, self.Z_mask, self.up_mask, self.down_mask, self.sign) == (
+            o.X_mask, o.Z_mask, o.up_mask, o.down_mask, o.sign)
+
+    def __repr__(self):
+        return (f"SymbolicPMROperator(X={self.X_mask:#x}, Z={self.Z_mask:#x}, up={self.up_mask:#x}, "
+                f"down={self.down_mask:#x}, sign={self.sign})")
+
+
+class SymbolicOpSum:
+    """Sum of c * operator; add_term splits diagonal and off-diagonal terms."""
+
+    def __init__(self, op: SymbolicPMROperator | None = None):
+        self.diagonal_terms: list[tuple[float, SymbolicPMROperator]] = []
+        self.off_diag_terms: list[tuple[float, SymbolicPMROperator]] = []
+        if op is not None:
+            self.add_term(1.0, op)
+
+    def add_term(self, c: float, op: SymbolicPMROperator) -> None:
+        (self.diagonal_terms if op.is_diagonal() else self.off_diag_terms).append((float(c), op.copy()))
+
+    def __iadd__(self, op):
+        self.add_term(1.0, op)
+        return self
+
+    def to_terms(self) -> C.Array:
+        """Packed qsi_term array: off-diagonal terms then diagonal terms (each in insertion order)."""
+        items = self.off_diag_terms + self.diagonal_terms
+        arr = (Term * max(1, len(items)))()
+        for k, (c, op) in enumerate(items):
+            C.memmove(C.byref(arr[k]), C.byref(op.t), C.sizeof(Term))
+            arr[k].c = c
+        return arr, len(items)
+
+    def __len__(self):
+        return len(self.off_diag_terms) + len(self.diagonal_terms)
+
+    def specs(self):
+        """[(c, op characters, spin ids)] in to_terms() order (for the checkers)."""
+        return [(c, op.spec[0], op.spec[1]) for c, op in self.off_diag_terms + self.diagonal_terms]
+
+
+# ---------------------------------------------------------------- basis
+def states_to_lohi(states: Iterable[int]) -> np.ndarray:
+    s = list(states)
+    a = np.zeros((len(s), 2), dtype=np.uint64)
+    for k, v in enumerate(s):
+        a[k, 0] = v & (2**64 - 1)
+        a[k, 1] = v >> 64
+    return a
+
+
+def read_basis_h5(path, dataset: str = "basis") -> np.ndarray:
+    n = C.c_int64()
+    call("qsi_h5_read_basis", str(path).encode(), dataset.encode(), None, 0, C.byref(n))
+    a = np.zeros((n.value, 2), dtype=np.uint64)
+    call("qsi_h5_read_basis", str(path).encode(), dataset.encode(), ptr(a), n.value, C.byref(n))
+    return a
+
+
+def read_f64_h5(path, dataset: str) -> np.ndarray:
+    n = C.c_int64()
+    dims = np.zeros(4, dtype=np.int64)
+    rank = C.c_int32()
+    call("qsi_h5_read_f64", str(path).encode(), dataset.encode(), None, 0, C.byref(n), ptr(dims), C.byref(rank))
+    a = np.zeros(n.value, dtype=np.float64)
+    call("qsi_h5_read_f64", str(path).encode(), dataset.encode(), ptr(a), n.value, C.byref(n), ptr(dims),
+         C.byref(rank))
+    return a.reshape(tuple(int(d) for d in dims[: rank.value])) if rank.value else a
+
+
+def read_basis_csv(path) -> np.ndarray:
+    n = C.c_int64()
+    call("qsi_csv_read_basis", str(path).encode(), None, 0, C.byref(n))
+    a = np.zeros((n.value, 2), dtype=np.uint64)
+    call("qsi_csv_read_basis", str(path).encode(), ptr(a), n.value, C.byref(n))
+    return a
+
+
+def write_basis_h5(path, lohi: np.ndarray, dataset: str = "basis", append: bool = False) -> None:
+    a = np.ascontiguousarray(lohi, dtype=np.uint64)
+    call("qsi_h5_write_basis", str(path).encode(), dataset.encode(), ptr(a), len(a), int(append))
+
+
+def write_eigs_h5(path, evals, evecs, latfile_json: str, dset_name: str) -> None:
+    """The .eigs.h5 layout of diag_DOQSI_ham: evecs is (dim, nvec) in Eigen column-major bytes."""
+    e = np.ascontiguousarray(evals, dtype=np.float64)
+    v = np.asarray(evecs, dtype=np.float64)
+    dim, nvec = v.shape
+    colmajor = np.ascontiguousarray(v.T)  # Eigen stores columns contiguously
+    call("qsi_h5_write_eigs", str(path).encode(), ptr(e), len(e), ptr(colmajor), dim, nvec,
+         latfile_json.encode(), dset_name.encode())
+
+
+def enumerate_basis(lattice, n_spinon_pairs: int = 0, sector=None, ordering: str = "greedy",
+                    n_threads: int = 0) -> np.ndarray:
+    """Sorted spin-ice basis of a lattice (see qsi_enumerate_basis)."""
+    from .lattice import Lattice
+
+    L = lattice if isinstance(lattice, Lattice) else Lattice.load(lattice)
+    tets = np.ascontiguousarray(L.tetrahedra, dtype=np.int32)
+    sl = np.ascontiguousarray(L.sublattice, dtype=np.int32)
+    sec = None if sector is None else np.ascontiguousarray(sector, dtype=np.int32)
+    out = C.POINTER(C.c_uint64)()
+    n = C.c_int64()
+    call("qsi_enumerate_basis", L.n_spins, ptr(tets), tets.shape[0], tets.shape[1], ptr(sl), int(sl.max()) + 1,
+         int(n_spinon_pairs), ptr(sec) if sec is not None else None, 1 if ordering == "greedy" else 0,
+         int(n_threads), C.byref(out), C.byref(n))
+    try:
+        a = np.ctypeslib.as_array(out, shape=(max(1, n.value) * 2,))[: n.value * 2].reshape(-1, 2).copy()
+    finally:
+        _lib.load().qsi_free_host(C.cast(out, C.c_void_p))
+    return a
+
+
+class ZBasis:
+    """Sorted 128-bit basis resident on the GPU with its bucket table."""
+
+    def __init__(self, lohi: np.ndarray, bucket_bits: int = 0):
+        self.states = np.ascontiguousarray(lohi, dtype=np.uint64).reshape(-1, 2)
+        self._h = C.c_void_p()
+        call("qsi_basis_create", ptr(self.states), len(self.states), int(bucket_bits), C.byref(self._h))
+
+    @classmethod
+    def load_from_file(cls, path, dataset: str = "basis", bucket_bits: int = 0):
+        """ZBasisBase::load_from_file (operator.cpp:138-159): .h5 (dataset) or .csv."""
+        p = Path(path)
+        if p.suffix == ".h5":
+            return cls(read_basis_h5(p, dataset), bucket_bits)
+        if p.suffix == ".csv":
+            return cls(read_basis_csv(p), bucket_bits)
+        raise ValueError("Bad basis format: file must end with .csv or .h5")
+
+    def dim(self) -> int:
+        return len(self.states)
+
+    size = dim
+
+    def __len__(self):
+        return len(self.states)
+
+    def __getitem__(self, i) -> int:
+        return int(self.states[i, 0]) | (int(self.states[i, 1]) << 64)
+
+    def search(self, lohi: np.ndarray) -> np.ndarray:
+        """Exact indices (or -1) of many states."""
+        q = np.ascontiguousarray(lohi, dtype=np.uint64).reshape(-1, 2)
+        idx = np.zeros(len(q), dtype=np.int64)
+        call("qsi_basis_search", self._h, ptr(q), len(q), ptr(idx), _lib.QSI_PTR_HOST, None)
+        return idx
+
+    def close(self):
+        if self._h:
+            _lib.load().qsi_basis_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LazyOpSum:
+    """Matrix-free H on a ZBasis (non-owning basis reference, copied term list)."""
+
+    def __init__(self, basis: ZBasis, ops: SymbolicOpSum):
+        self.basis = basis
+        self.ops = ops
+        self._terms, n = ops.to_terms()
+        self._h = C.c_void_p()
+        call("qsi_op_create", basis._h, C.cast(self._terms, C.c_void_p), n, C.byref(self._h))
+
+    def rows(self):
+        return self.basis.dim()
+
+    cols = rows
+
+    @staticmethod
+    def _kind(a):
+        return _lib.QSI_PTR_DEVICE if hasattr(a, "is_cuda") and a.is_cuda else _lib.QSI_PTR_HOST
+
+    def _stream(self, a):
+        if self._kind(a) == _lib.QSI_PTR_DEVICE:
+            import torch
+
+            return C.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+        return None
+
+    def evaluate_add(self, x, y) -> None:
+        """y += H x (FP64; numpy arrays or CUDA tensors)."""
+        call("qsi_op_apply", self._h, ptr(x), ptr(y), 1, self._kind(x), self._stream(x))
+
+    def evaluate(self, x, y) -> None:
+        """y = H x."""
+        call("qsi_op_apply", self._h, ptr(x), ptr(y), 0, self._kind(x), self._stream(x))
+
+    def __matmul__(self, x):
+        y = np.zeros_like(x) if not hasattr(x, "is_cuda") else x.new_zeros(x.shape)
+        self.evaluate(x, y)
+        return y
+
+    def apply_batched(self, X, Y, accumulate: bool = False) -> None:
+        """Y (+)= H X for X of shape (dim, R), float64 or float32 (FP64 row accumulation)."""
+        R = X.shape[1]
+        dt = str(X.dtype)
+        dtype = _lib.QSI_F32 if "float32" in dt else _lib.QSI_F64
+        call("qsi_op_apply_batched", self._h, ptr(X), ptr(Y), R, dtype, int(accumulate), self._kind(X),
+             self._stream(X))
+
+    def triplets(self, tol: float = 1e-14):
+        """(rows, cols, vals) in LazyOpSum::toSparseMatrix order."""
+        n = C.c_int64()
+        call("qsi_op_triplets", self._h, tol, None, None, None, 0, C.byref(n))
+        r = np.zeros(n.value, dtype=np.int64)
+        c = np.zeros(n.value, dtype=np.int64)
+        v = np.zeros(n.value, dtype=np.float64)
+        call("qsi_op_triplets", self._h, tol, ptr(r), ptr(c), ptr(v), n.value, C.byref(n))
+        return r, c, v
+
+    def toSparseMatrix(self, tol: float = 1e-14):
+        import scipy.sparse as sp
+
+        r, c, v = self.triplets(tol)
+        N = self.basis.dim()
+        return sp.csr_matrix((v, (r, c)), shape=(N, N))
+
+    def connectivity(self):
+        """(hits, misses): off-diagonal terms over all rows landing in / leaving the basis."""
+        h, m = C.c_int64(), C.c_int64()
+        call("qsi_op_connectivity", self._h, C.byref(h), C.byref(m))
+        return h.value, m.value
+
+    def count_misses(self) -> int:
+        n = C.c_int64()
+        call("qsi_op_count_misses", self._h, C.byref(n))
+        return n.value
+
+    def close(self):
+        if self._h:
+            _lib.load().qsi_op_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LazyOpSumProd:
+    """Spectra adaptor: perform_op(x, y) computes y = H x."""
+
+    def __init__(self, op: LazyOpSum):
+        self.op = op
+
+    def perform_op(self, x_in, y_out) -> None:
+        self.op.evaluate(x_in, y_out)
+
+    def rows(self):
+        return self.op.rows()
+
+    cols = rows
+
+
+def real_apply_fn(op: LazyOpSum):
+    """projED::RealApplyFn adaptor: f(in, out) performs out += H in."""
+    return lambda x, y: op.evaluate_add(x, y)

@@ -1,0 +1,1093 @@
+// Krylov solvers on the device: thick-restart Lanczos with full
+// reorthogonalisation (the mfsparse path), the plain three-term Lanczos of
+// projED::lanczos::eigval0 (the mfeig0 path) and batched FTLM recurrences.
+//
+// All dot products, norms and reorthogonalisation coefficients are FP64 and
+// reduced in a fixed order (per-block partial sums, then one block), so a solve
+// is deterministic for a given seed.  With precision QSI_F32 the stored Krylov
+// vectors are FP32 and the operator gathers FP32, while the working vector w,
+// every coefficient and the projected eigenproblem stay FP64; the Ritz pairs
+// are then polished by FP64 Rayleigh-Ritz steps with FP64 applies.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "qsi_device.cuh"
+#include "qsi_handles.h"
+
+namespace qsi {
+
+constexpr int kRedBlock = 256;
+constexpr int kRedGrid = 1024;  // fixed partial-sum grid: reduction order independent of the device
+
+template <typename T>
+__device__ __forceinline__ double ld(const T* p, int64_t i) {
+    return (double)p[i];
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) r += sh[k];
+    return r;  // valid in thread 0
+}
+
+// partial[b*(k+1) + i] = sum over this block's rows of V_i . w  (i < k), and
+// partial[b*(k+1) + k] = sum of w^2.
+template <typename VT>
+__global__ void __launch_bounds__(kRedBlock) k_multidot(const VT* __restrict__ V, int64_t ld_v, int k,
+                                                        const double* __restrict__ w, int64_t n,
+                                                        double* __restrict__ partial) {
+    __shared__ double sh[32];
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+    for (int i = 0; i <= k; ++i) {
+        double acc = 0.0;
+        if (i < k) {
+            const VT* vi = V + (int64_t)i * ld_v;
+            for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) acc += ld(vi, r) * w[r];
+        } else {
+            for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) acc += w[r] * w[r];
+        }
+        double s = block_sum(acc, sh);
+        if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * (k + 1) + i] = s;
+    }
+}
+
+__global__ void k_reduce_partials(const double* __restrict__ partial, int nblocks, int k1, double* __restrict__ out) {
+    __shared__ double sh[32];
+    for (int i = 0; i < k1; ++i) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partial[(int64_t)b * k1 + i];
+        double s = block_sum(acc, sh);
+        if (threadIdx.x == 0) out[i] = s;
+    }
+}
+
+// w -= sum_i h_i V_i ; partial[b] = this block's sum of the new w^2.
+template <typename VT>
+__global__ void __launch_bounds__(kRedBlock) k_multi_axpy(const VT* __restrict__ V, int64_t ld_v, int k,
+                                                          const double* __restrict__ h, double* __restrict__ w,
+                                                          int64_t n, double* __restrict__ partial) {
+    __shared__ double sh[32];
+    __shared__ double hs[256];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) hs[i] = h[i];
+    __syncthreads();
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+    double acc = 0.0;
+    for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+        double v = w[r];
+        for (int i = 0; i < k; ++i) v -= hs[i] * ld(V + (int64_t)i * ld_v, r);
+        w[r] = v;
+        acc += v * v;
+    }
+    double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// out = w * (1/beta), converted to the storage type.
+template <typename VT>
+__global__ void k_scale_store(const double* __restrict__ w, const double* __restrict__ beta, VT* __restrict__ out,
+                              int64_t n) {
+    const double inv = 1.0 / sqrt(*beta);  // beta holds the squared norm
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        out[r] = (VT)(w[r] * inv);
+}
+
+// Deterministic N(0,1) start vector: counter-based SplitMix64 bits, Box-Muller.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_randn(double* __restrict__ w, int64_t n, uint64_t seed, int rademacher) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t a = splitmix64(seed * 0x632be59bd9b4e019ULL + 2 * (uint64_t)r);
+        if (rademacher) {
+            w[r] = (a >> 63) ? 1.0 : -1.0;
+            continue;
+        }
+        uint64_t b = splitmix64(seed * 0x632be59bd9b4e019ULL + 2 * (uint64_t)r + 1);
+        double u1 = ((a >> 11) + 1) * (1.0 / 9007199254740993.0);  // (0,1]
+        double u2 = (b >> 11) * (1.0 / 9007199254740992.0);        // [0,1)
+        double rad = sqrt(-2.0 * log(u1));
+        w[r] = rad * cospi(2.0 * u2);
+    }
+}
+
+template <typename VT>
+__global__ void k_to_f64(const VT* __restrict__ v, double* __restrict__ w, int64_t n) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        w[r] = (double)v[r];
+}
+
+// V[:, 0..k) <- V[:, 0..m) * Y[0..m, 0..k) in place, row chunk by row chunk.
+template <typename VT>
+__global__ void __launch_bounds__(128) k_rotate(VT* __restrict__ V, int64_t ld_v, int m, int k,
+                                                const double* __restrict__ Y, int64_t n) {
+    extern __shared__ double ys[];  // m*k
+    for (int i = threadIdx.x; i < m * k; i += blockDim.x) ys[i] = Y[i];
+    __syncthreads();
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        double row[160];
+        for (int j = 0; j < m; ++j) row[j] = (double)V[(int64_t)j * ld_v + r];
+        for (int i = 0; i < k; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < m; ++j) acc += row[j] * ys[j * k + i];
+            V[(int64_t)i * ld_v + r] = (VT)acc;
+        }
+    }
+}
+
+// X[:, i] = sum_j V[:, j] Y[j, i]  (i < k) into a separate FP64 output.
+template <typename VT>
+__global__ void __launch_bounds__(128) k_ritz_vectors(const VT* __restrict__ V, int64_t ld_v, int m, int k,
+                                                      const double* __restrict__ Y, double* __restrict__ X,
+                                                      int64_t n) {
+    extern __shared__ double ys[];
+    for (int i = threadIdx.x; i < m * k; i += blockDim.x) ys[i] = Y[i];
+    __syncthreads();
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        for (int i = 0; i < k; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < m; ++j) acc += (double)V[(int64_t)j * ld_v + r] * ys[j * k + i];
+            X[(int64_t)i * n + r] = acc;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ small dense symmetric eigensolver
+// Cyclic Jacobi with round-robin pair ordering, one thread block per matrix.
+// A (M x M, row-major, M even, M <= 128) is read from global, diagonalised in
+// shared memory; eigenvalues ascending to evals, eigenvectors as columns of
+// evecs (row-major M x M).  Padding rows/columns of zeros stay decoupled.
+__global__ void __launch_bounds__(256) k_jacobi(const double* __restrict__ Ain, int M, double* __restrict__ evals,
+                                                double* __restrict__ evecs, int max_sweeps) {
+    extern __shared__ double sm[];
+    double* A = sm;                 // M*M
+    double* cs = A + M * M;         // M/2 cosines
+    double* sn = cs + M / 2;        // M/2 sines
+    int* pp = (int*)(sn + M / 2);   // M/2 p indices
+    int* qq = pp + M / 2;           // M/2 q indices
+    int* perm = qq + M / 2;         // M positions
+    __shared__ double red[32];
+    __shared__ int stop;
+    const double* Ab = Ain + (int64_t)blockIdx.x * M * M;
+    double* Vb = evecs + (int64_t)blockIdx.x * M * M;
+    double* eb = evals + (int64_t)blockIdx.x * M;
+    for (int i = threadIdx.x; i < M * M; i += blockDim.x) {
+        A[i] = Ab[i];
+        Vb[i] = (i / M == i % M) ? 1.0 : 0.0;
+    }
+    for (int i = threadIdx.x; i < M; i += blockDim.x) perm[i] = i;
+    __syncthreads();
+    const int H = M / 2;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        // convergence: off-diagonal mass relative to total
+        double off = 0.0, tot = 0.0;
+        for (int i = threadIdx.x; i < M * M; i += blockDim.x) {
+            double a = A[i] * A[i];
+            tot += a;
+            if (i / M != i % M) off += a;
+        }
+        double offs = block_sum(off, red);
+        double tots = block_sum(tot, red);
+        if (threadIdx.x == 0) stop = !(offs > 1e-32 * tots) || tots == 0.0;
+        __syncthreads();
+        if (stop) break;
+        for (int round = 0; round < M - 1; ++round) {
+            for (int t = threadIdx.x; t < H; t += blockDim.x) {
+                int p = perm[t], q = perm[M - 1 - t];
+                if (p > q) {
+                    int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                pp[t] = p;
+                qq[t] = q;
+                double apq = A[p * M + q];
+                double c = 1.0, s = 0.0;
+                if (apq != 0.0) {
+                    double theta = (A[q * M + q] - A[p * M + p]) / (2.0 * apq);
+                    double tt = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                    c = 1.0 / sqrt(tt * tt + 1.0);
+                    s = tt * c;
+                }
+                cs[t] = c;
+                sn[t] = s;
+            }
+            __syncthreads();
+            // rows: A <- J^T A
+            for (int idx = threadIdx.x; idx < H * M; idx += blockDim.x) {
+                int t = idx / M, col = idx % M;
+                int p = pp[t], q = qq[t];
+                double c = cs[t], s = sn[t];
+                double ap = A[p * M + col], aq = A[q * M + col];
+                A[p * M + col] = c * ap - s * aq;
+                A[q * M + col] = s * ap + c * aq;
+            }
+            __syncthreads();
+            // columns: A <- A J, V <- V J
+            for (int idx = threadIdx.x; idx < H * M; idx += blockDim.x) {
+                int t = idx / M, row = idx % M;
+                int p = pp[t], q = qq[t];
+                double c = cs[t], s = sn[t];
+                double ap = A[row * M + p], aq = A[row * M + q];
+                A[row * M + p] = c * ap - s * aq;
+                A[row * M + q] = s * ap + c * aq;
+                double vp = Vb[row * M + p], vq = Vb[row * M + q];
+                Vb[row * M + p] = c * vp - s * vq;
+                Vb[row * M + q] = s * vp + c * vq;
+            }
+            __syncthreads();
+            // rotate positions 1..M-1 (position 0 fixed)
+            if (threadIdx.x == 0) {
+                int last = perm[M - 1];
+                for (int i = M - 1; i > 1; --i) perm[i] = perm[i - 1];
+                perm[1] = last;
+            }
+            __syncthreads();
+        }
+    }
+    // sort ascending (selection sort by one thread; M <= 128), permute columns
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < M; ++i) perm[i] = i;
+        for (int i = 0; i < M; ++i) {
+            int best = i;
+            for (int j = i + 1; j < M; ++j)
+                if (A[perm[j] * M + perm[j]] < A[perm[best] * M + perm[best]]) best = j;
+            int tmp = perm[i];
+            perm[i] = perm[best];
+            perm[best] = tmp;
+        }
+        for (int i = 0; i < M; ++i) cs[i % H] = 0;  // no-op keeps cs in use for small M
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < M; i += blockDim.x) eb[i] = A[perm[i] * M + perm[i]];
+    // permute eigenvector columns through shared memory row by row
+    for (int row = 0; row < M; ++row) {
+        __syncthreads();
+        for (int j = threadIdx.x; j < M; j += blockDim.x) A[j] = Vb[row * M + perm[j]];
+        __syncthreads();
+        for (int j = threadIdx.x; j < M; j += blockDim.x) Vb[row * M + j] = A[j];
+    }
+}
+
+// Host wrapper: batch of n_mat symmetric m x m matrices (row-major, host),
+// returns ascending eigenvalues and eigenvector columns (host, m x m each).
+qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vector<double>& w, std::vector<double>& V,
+                       cudaStream_t st) {
+    const int M = m + (m & 1);
+    if (M > 128) return fail(QSI_INVALID_ARG, "projected matrix of size %d exceeds 128", m);
+    std::vector<double> Ap((size_t)n_mat * M * M, 0.0);
+    for (int b = 0; b < n_mat; ++b)
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j) Ap[(size_t)b * M * M + i * M + j] = A[(size_t)b * m * m + i * m + j];
+    // a padded index gets a diagonal above the spectrum so it sorts last
+    if (M != m) {
+        for (int b = 0; b < n_mat; ++b) {
+            double big = 0.0;
+            for (int i = 0; i < m; ++i) {
+                double r = 0.0;
+                for (int j = 0; j < m; ++j) r += fabs(A[(size_t)b * m * m + i * m + j]);
+                big = std::max(big, r);
+            }
+            Ap[(size_t)b * M * M + (M - 1) * M + (M - 1)] = 2.0 * big + 1.0;
+        }
+    }
+    double *dA = nullptr, *dw = nullptr, *dV = nullptr;
+    QSI_CUDA(cudaMalloc(&dA, Ap.size() * 8));
+    QSI_CUDA(cudaMalloc(&dw, (size_t)n_mat * M * 8));
+    QSI_CUDA(cudaMalloc(&dV, Ap.size() * 8));
+    QSI_CUDA(cudaMemcpyAsync(dA, Ap.data(), Ap.size() * 8, cudaMemcpyHostToDevice, st));
+    size_t smem = (size_t)M * M * 8 + (size_t)M * 8 + (size_t)M * 2 * 4 + (size_t)M * 4 + 64;
+    cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_jacobi<<<n_mat, 256, smem, st>>>(dA, M, dw, dV, 60);
+    std::vector<double> wp((size_t)n_mat * M), Vp(Ap.size());
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(wp.data(), dw, wp.size() * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Vp.data(), dV, Vp.size() * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dA);
+    cudaFree(dw);
+    cudaFree(dV);
+    if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "jacobi: %s", cudaGetErrorString(e));
+    w.assign((size_t)n_mat * m, 0.0);
+    V.assign((size_t)n_mat * m * m, 0.0);
+    for (int b = 0; b < n_mat; ++b) {
+        for (int i = 0; i < m; ++i) w[(size_t)b * m + i] = wp[(size_t)b * M + i];
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j) V[(size_t)b * m * m + i * m + j] = Vp[(size_t)b * M * M + i * M + j];
+    }
+    return QSI_OK;
+}
+
+// ------------------------------------------------------------------ vector toolkit
+struct Vecs {
+    int64_t n = 0;
+    cudaStream_t st = nullptr;
+    double* partial = nullptr;  // kRedGrid * 257
+    double* red = nullptr;      // 257
+    std::vector<double> hred;
+    qsi_status init(int64_t n_, cudaStream_t s) {
+        n = n_;
+        st = s;
+        QSI_CUDA(cudaMalloc(&partial, (size_t)kRedGrid * 257 * 8));
+        QSI_CUDA(cudaMalloc(&red, 257 * 8));
+        hred.resize(257);
+        return QSI_OK;
+    }
+    ~Vecs() {
+        cudaFree(partial);
+        cudaFree(red);
+    }
+    // h[0..k) = V_i . w and h[k] = |w|^2, copied to host
+    template <typename VT>
+    qsi_status dots(const VT* V, int64_t ldv, int k, const double* w, std::vector<double>& h) {
+        k_multidot<VT><<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, w, n, partial);
+        k_reduce_partials<<<1, 256, 0, st>>>(partial, kRedGrid, k + 1, red);
+        h.resize(k + 1);
+        QSI_CUDA(cudaMemcpyAsync(h.data(), red, (size_t)(k + 1) * 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+        return QSI_OK;
+    }
+    // w -= V h ; returns |w|^2 (device copy left in red[0])
+    template <typename VT>
+    qsi_status axpy(const VT* V, int64_t ldv, int k, const std::vector<double>& h, double* w, double& nrm2) {
+        QSI_CUDA(cudaMemcpyAsync(red + 1, h.data(), (size_t)k * 8, cudaMemcpyHostToDevice, st));
+        k_multi_axpy<VT><<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, red + 1, w, n, partial);
+        k_reduce_partials<<<1, 256, 0, st>>>(partial, kRedGrid, 1, red);
+        QSI_CUDA(cudaMemcpyAsync(&nrm2, red, 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+        return QSI_OK;
+    }
+};
+
+// w = H v with FP64 output; FP32 storage is gathered as FP32 and accumulated in FP64.
+template <typename VT>
+qsi_status apply_to_w(qsi_op* op, const VT* v, double* w, cudaStream_t st) {
+    return launch_apply_to_f64(op, v, w, sizeof(VT) == 4 ? QSI_F32 : QSI_F64, st);
+}
+
+}  // namespace qsi
+
+namespace qsi {
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t count = 0;
+    cudaError_t alloc(size_t n) {
+        count = n;
+        return cudaMalloc(&p, n * sizeof(T));
+    }
+    ~DevBuf() { cudaFree(p); }
+};
+
+// Orthonormalises the FP64 block X (k vectors of length n, vector-major) with
+// two passes of classical Gram-Schmidt per vector.
+static qsi_status orthonormalise(Vecs& vx, double* X, int k, int64_t n) {
+    std::vector<double> h;
+    for (int i = 0; i < k; ++i) {
+        double* xi = X + (size_t)i * n;
+        for (int pass = 0; pass < 2; ++pass) {
+            qsi_status s = vx.dots<double>(X, n, i, xi, h);
+            if (s) return s;
+            double nrm2 = h[i];
+            if (i > 0) {
+                h.resize(i);
+                s = vx.axpy<double>(X, n, i, h, xi, nrm2);
+                if (s) return s;
+            }
+            if (pass == 1) {
+                if (!(nrm2 > 0)) return fail(QSI_NOT_CONVERGED, "polish: Ritz vectors became linearly dependent");
+                QSI_CUDA(cudaMemcpyAsync(vx.red, &nrm2, 8, cudaMemcpyHostToDevice, vx.st));
+                k_scale_store<double><<<grid_for(n, 256), 256, 0, vx.st>>>(xi, vx.red, xi, n);
+            }
+        }
+    }
+    QSI_CUDA(cudaStreamSynchronize(vx.st));
+    return QSI_OK;
+}
+
+// Rayleigh-Ritz of H on span(S) for an orthonormal FP64 block S (k vectors),
+// with HS = H S supplied; writes the lowest `keep` Ritz vectors to X, H X to HX.
+static qsi_status rayleigh_ritz(Vecs& vx, const double* S, const double* HS, int k, int keep, int64_t n, double* X,
+                                double* HX, std::vector<double>& theta, cudaStream_t st) {
+    std::vector<double> G((size_t)k * k), h;
+    for (int j = 0; j < k; ++j) {
+        qsi_status s = vx.dots<double>(S, n, k, HS + (size_t)j * n, h);
+        if (s) return s;
+        for (int i = 0; i < k; ++i) G[(size_t)i * k + j] = h[i];
+    }
+    for (int i = 0; i < k; ++i)
+        for (int j = i + 1; j < k; ++j) {
+            double a = 0.5 * (G[(size_t)i * k + j] + G[(size_t)j * k + i]);
+            G[(size_t)i * k + j] = G[(size_t)j * k + i] = a;
+        }
+    std::vector<double> w, Y;
+    qsi_status s = jacobi_eigh(G, k, 1, w, Y, st);
+    if (s) return s;
+    std::vector<double> Yk((size_t)k * keep);
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < keep; ++j) Yk[(size_t)i * keep + j] = Y[(size_t)i * k + j];
+    DevBuf<double> dY;
+    QSI_CUDA(dY.alloc(Yk.size()));
+    QSI_CUDA(cudaMemcpyAsync(dY.p, Yk.data(), Yk.size() * 8, cudaMemcpyHostToDevice, st));
+    size_t smem = Yk.size() * 8;
+    k_ritz_vectors<double><<<grid_for(n, 128), 128, smem, st>>>(S, n, k, keep, dY.p, X, n);
+    k_ritz_vectors<double><<<grid_for(n, 128), 128, smem, st>>>(HS, n, k, keep, dY.p, HX, n);
+    QSI_CUDA(cudaGetLastError());
+    QSI_CUDA(cudaStreamSynchronize(st));
+    theta.assign(w.begin(), w.begin() + keep);
+    return QSI_OK;
+}
+
+__global__ void k_residual(const double* __restrict__ HX, const double* __restrict__ X, const double* __restrict__ th,
+                           int k, int64_t n, double* __restrict__ R) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        for (int i = 0; i < k; ++i) R[(size_t)i * n + r] = HX[(size_t)i * n + r] - th[i] * X[(size_t)i * n + r];
+}
+
+// Thick-restart Lanczos (Wu & Simon) for the nev smallest eigenpairs.
+template <typename VT>
+static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, double* evecs, qsi_report* rep) {
+    auto t0 = std::chrono::steady_clock::now();
+    const int64_t n = op->basis->n;
+    cudaStream_t st = op->stream;
+    int m = std::min<int64_t>(cfg.ncv, n);
+    int nev = std::min(cfg.nev, std::max(1, m - 1));  // compute_spectrum_iterative clamps, matrix_diag_bits.hpp:64-66
+    if (nev < 1 || m < 2) return fail(QSI_INVALID_ARG, "lanczos: need ncv >= 2 and nev >= 1");
+    if (m > 126) return fail(QSI_INVALID_ARG, "lanczos: ncv must be <= 126");
+    const double tol = cfg.tol > 0 ? cfg.tol : 1e-10;
+    const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
+    Vecs vx;
+    qsi_status s = vx.init(n, st);
+    if (s) return s;
+    DevBuf<VT> V;
+    DevBuf<double> w, dY;
+    QSI_CUDA(V.alloc((size_t)(m + 1) * n));
+    QSI_CUDA(w.alloc((size_t)n));
+    QSI_CUDA(dY.alloc((size_t)m * m));
+    auto vec = [&](int j) { return V.p + (size_t)j * n; };
+    // start vector N(0,1), normalised (stored)
+    k_randn<<<grid_for(n, 256), 256, 0, st>>>(w.p, n, cfg.seed, 0);
+    std::vector<double> h;
+    s = vx.dots<VT>(V.p, n, 0, w.p, h);
+    if (s) return s;
+    QSI_CUDA(cudaMemcpyAsync(vx.red, &h[0], 8, cudaMemcpyHostToDevice, st));
+    k_scale_store<VT><<<grid_for(n, 256), 256, 0, st>>>(w.p, vx.red, vec(0), n);
+    std::vector<double> alpha(m, 0.0), beta(m, 0.0), theta, coup;  // coup[i] = s_i couplings after restart
+    int k = 0;
+    int64_t applies = 0;
+    int restarts = 0, nconv = 0;
+    std::vector<double> Tw, TY;
+    for (;;) {
+        for (int j = k; j < m; ++j) {
+            s = apply_to_w<VT>(op, vec(j), w.p, st);
+            if (s) return s;
+            ++applies;
+            // full reorthogonalisation: classical Gram-Schmidt against v_0..v_j, repeated once
+            // when the norm drops by more than 1/sqrt(2) (DGKS criterion)
+            s = vx.dots<VT>(V.p, n, j + 1, w.p, h);
+            if (s) return s;
+            double before = h[j + 1];
+            double a = h[j];
+            std::vector<double> hh(h.begin(), h.begin() + j + 1);
+            double nrm2 = 0;
+            s = vx.axpy<VT>(V.p, n, j + 1, hh, w.p, nrm2);
+            if (s) return s;
+            if (nrm2 < 0.5 * before) {
+                s = vx.dots<VT>(V.p, n, j + 1, w.p, h);
+                if (s) return s;
+                a += h[j];
+                hh.assign(h.begin(), h.begin() + j + 1);
+                s = vx.axpy<VT>(V.p, n, j + 1, hh, w.p, nrm2);
+                if (s) return s;
+            }
+            alpha[j] = a;
+            double b = std::sqrt(std::max(nrm2, 0.0));
+            if (!(b > 1e-13 * std::max(1.0, std::fabs(a)))) {
+                // invariant subspace: continue from a fresh random direction orthogonal to V
+                b = 0.0;
+                k_randn<<<grid_for(n, 256), 256, 0, st>>>(w.p, n, cfg.seed + 7919 * (uint64_t)(j + 1 + restarts * m), 0);
+                for (int pass = 0; pass < 2; ++pass) {
+                    s = vx.dots<VT>(V.p, n, j + 1, w.p, h);
+                    if (s) return s;
+                    hh.assign(h.begin(), h.begin() + j + 1);
+                    s = vx.axpy<VT>(V.p, n, j + 1, hh, w.p, nrm2);
+                    if (s) return s;
+                }
+            }
+            beta[j] = b;
+            QSI_CUDA(cudaMemcpyAsync(vx.red, &nrm2, 8, cudaMemcpyHostToDevice, st));
+            k_scale_store<VT><<<grid_for(n, 256), 256, 0, st>>>(w.p, vx.red, vec(j + 1), n);
+        }
+        // projected matrix: arrowhead (kept Ritz values + couplings) then tridiagonal
+        std::vector<double> T((size_t)m * m, 0.0);
+        for (int i = 0; i < k; ++i) {
+            T[(size_t)i * m + i] = theta[i];
+            T[(size_t)i * m + k] = T[(size_t)k * m + i] = coup[i];
+        }
+        for (int j = k; j < m; ++j) {
+            T[(size_t)j * m + j] = alpha[j];
+            if (j + 1 < m) T[(size_t)j * m + j + 1] = T[(size_t)(j + 1) * m + j] = beta[j];
+        }
+        s = jacobi_eigh(T, m, 1, Tw, TY, st);
+        if (s) return s;
+        const double bl = beta[m - 1];
+        nconv = 0;
+        for (int i = 0; i < nev; ++i) {
+            double r = std::fabs(bl * TY[(size_t)(m - 1) * m + i]);
+            if (r < tol * std::max(eps23, std::fabs(Tw[i]))) ++nconv;
+        }
+        const bool exhausted = (m >= n);
+        if (nconv >= nev || restarts >= cfg.max_iter || exhausted) break;
+        ++restarts;
+        int knew = std::min(m - 2, nev + std::max(nconv, (m - nev) / 2));
+        knew = std::max(knew, std::min(nev, m - 2));
+        if (knew < 1) knew = 1;
+        std::vector<double> Yk((size_t)m * knew);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < knew; ++j) Yk[(size_t)i * knew + j] = TY[(size_t)i * m + j];
+        QSI_CUDA(cudaMemcpyAsync(dY.p, Yk.data(), Yk.size() * 8, cudaMemcpyHostToDevice, st));
+        size_t smem = Yk.size() * 8;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_rotate<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_rotate<VT><<<grid_for(n, 128), 128, smem, st>>>(V.p, n, m, knew, dY.p, n);
+        QSI_CUDA(cudaMemcpyAsync(vec(knew), vec(m), (size_t)n * sizeof(VT), cudaMemcpyDeviceToDevice, st));
+        theta.assign(Tw.begin(), Tw.begin() + knew);
+        coup.resize(knew);
+        for (int i = 0; i < knew; ++i) coup[i] = bl * TY[(size_t)(m - 1) * m + i];
+        k = knew;
+        QSI_CUDA(cudaGetLastError());
+    }
+    // Ritz vectors in FP64
+    DevBuf<double> X, HX;
+    QSI_CUDA(X.alloc((size_t)nev * n));
+    QSI_CUDA(HX.alloc((size_t)nev * n));
+    {
+        std::vector<double> Yk((size_t)m * nev);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < nev; ++j) Yk[(size_t)i * nev + j] = TY[(size_t)i * m + j];
+        QSI_CUDA(cudaMemcpyAsync(dY.p, Yk.data(), Yk.size() * 8, cudaMemcpyHostToDevice, st));
+        size_t smem = Yk.size() * 8;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_ritz_vectors<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_ritz_vectors<VT><<<grid_for(n, 128), 128, smem, st>>>(V.p, n, m, nev, dY.p, X.p, n);
+        QSI_CUDA(cudaGetLastError());
+    }
+    std::vector<double> th(Tw.begin(), Tw.begin() + nev);
+    // free the Krylov basis before polishing
+    cudaFree(V.p);
+    V.p = nullptr;
+    // FP64 polish: Rayleigh-Ritz on the Ritz block, then optional residual-augmented rounds
+    int rounds = std::max(cfg.polish_steps, sizeof(VT) == 4 ? 1 : 0);
+    DevBuf<double> S, HS, dth;
+    if (rounds > 0) {
+        QSI_CUDA(S.alloc((size_t)2 * nev * n));
+        QSI_CUDA(HS.alloc((size_t)2 * nev * n));
+        QSI_CUDA(dth.alloc((size_t)nev));
+        QSI_CUDA(cudaMemcpyAsync(S.p, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, st));
+        s = orthonormalise(vx, S.p, nev, n);
+        if (s) return s;
+        for (int i = 0; i < nev; ++i) {
+            s = launch_apply(op, S.p + (size_t)i * n, HS.p + (size_t)i * n, 1, QSI_F64, 0, st);
+            if (s) return s;
+            ++applies;
+        }
+        s = rayleigh_ritz(vx, S.p, HS.p, nev, nev, n, X.p, HX.p, th, st);
+        if (s) return s;
+        for (int round = 1; round < rounds; ++round) {
+            // S = [X, R], R = HX - X theta
+            QSI_CUDA(cudaMemcpyAsync(S.p, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, st));
+            QSI_CUDA(cudaMemcpyAsync(dth.p, th.data(), (size_t)nev * 8, cudaMemcpyHostToDevice, st));
+            k_residual<<<grid_for(n, 256), 256, 0, st>>>(HX.p, X.p, dth.p, nev, n, S.p + (size_t)nev * n);
+            s = orthonormalise(vx, S.p, 2 * nev, n);
+            if (s) return s;
+            for (int i = 0; i < 2 * nev; ++i) {
+                s = launch_apply(op, S.p + (size_t)i * n, HS.p + (size_t)i * n, 1, QSI_F64, 0, st);
+                if (s) return s;
+                ++applies;
+            }
+            s = rayleigh_ritz(vx, S.p, HS.p, 2 * nev, nev, n, X.p, HX.p, th, st);
+            if (s) return s;
+        }
+    } else {
+        for (int i = 0; i < nev; ++i) {
+            s = launch_apply(op, X.p + (size_t)i * n, HX.p + (size_t)i * n, 1, QSI_F64, 0, st);
+            if (s) return s;
+            ++applies;
+        }
+    }
+    // residual norms ||H x - theta x|| / ||x||
+    if (rep) {
+        DevBuf<double> R, d2;
+        QSI_CUDA(R.alloc((size_t)nev * n));
+        QSI_CUDA(d2.alloc((size_t)nev));
+        QSI_CUDA(cudaMemcpyAsync(d2.p, th.data(), (size_t)nev * 8, cudaMemcpyHostToDevice, st));
+        k_residual<<<grid_for(n, 256), 256, 0, st>>>(HX.p, X.p, d2.p, nev, n, R.p);
+        for (int i = 0; i < nev && i < 64; ++i) {
+            s = vx.dots<double>(X.p + (size_t)i * n, n, 1, R.p + (size_t)i * n, h);
+            if (s) return s;
+            std::vector<double> hx;
+            s = vx.dots<double>(X.p, n, 0, X.p + (size_t)i * n, hx);
+            if (s) return s;
+            rep->residual[i] = std::sqrt(h[1] / std::max(hx[0], 1e-300));
+        }
+        rep->converged = nconv;
+        rep->restarts = restarts;
+        rep->applies = applies;
+        rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    for (int i = 0; i < nev; ++i) evals[i] = th[i];
+    if (evecs && cfg.want_vectors) QSI_CUDA(cudaMemcpy(evecs, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToHost));
+    if (nconv < nev && !(m >= n)) return fail(QSI_NOT_CONVERGED, "lanczos: %d of %d eigenpairs converged after %d restarts", nconv, nev, restarts);
+    return QSI_OK;
+}
+
+// ------------------------------------------------------------------ eigval0 (mfeig0)
+// Lowest eigenvalue of the symmetric tridiagonal (a, b) by Sturm-count
+// multisection: each of the block's threads counts eigenvalues below one
+// point; the bracket shrinks by blockDim+1 per round.
+__global__ void k_tridiag_lowest(const double* __restrict__ a, const double* __restrict__ b, int m, double lo, double hi,
+                                 double* out) {
+    __shared__ int cnt[256];
+    __shared__ double bounds[2];
+    if (threadIdx.x == 0) bounds[0] = lo, bounds[1] = hi;
+    __syncthreads();
+    for (int round = 0; round < 12; ++round) {
+        double L = bounds[0], H = bounds[1];
+        double x = L + (H - L) * (threadIdx.x + 1) / (blockDim.x + 1);
+        int c = 0;
+        double d = 1.0;
+        for (int i = 0; i < m; ++i) {
+            double bb = (i > 0) ? b[i - 1] * b[i - 1] : 0.0;
+            d = (a[i] - x) - (i > 0 ? bb / d : 0.0);
+            if (d == 0.0) d = -1e-300;
+            c += (d < 0.0);
+        }
+        cnt[threadIdx.x] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // first point whose count >= 1 bounds the lowest eigenvalue from above
+            int t = 0;
+            while (t < (int)blockDim.x && cnt[t] < 1) ++t;
+            double nl = (t == 0) ? L : L + (H - L) * t / (blockDim.x + 1);
+            double nh = (t == (int)blockDim.x) ? H : L + (H - L) * (t + 1) / (blockDim.x + 1);
+            bounds[0] = nl;
+            bounds[1] = nh;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = 0.5 * (bounds[0] + bounds[1]);
+}
+
+// Eigenvector of the tridiagonal for eigenvalue lam by inverse iteration with
+// a partially pivoted LU of (T - lam I) (one thread; m is the Krylov length).
+__global__ void k_tridiag_vector(const double* __restrict__ a, const double* __restrict__ b, int m, double lam,
+                                 double* __restrict__ work, double* __restrict__ y) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double* u0 = work;           // diagonal of U
+    double* u1 = work + m;       // first superdiagonal
+    double* u2 = work + 2 * m;   // second superdiagonal (from pivoting)
+    double* l = work + 3 * m;    // multipliers
+    int* piv = (int*)(work + 4 * m);
+    double anorm = 0.0;
+    for (int i = 0; i < m; ++i) anorm = fmax(anorm, fabs(a[i]) + (i ? fabs(b[i - 1]) : 0.0) + (i + 1 < m ? fabs(b[i]) : 0.0));
+    double tiny = 1e-300 + 2.2e-16 * anorm;
+    // factor
+    double d = a[0] - lam, e = (m > 1) ? b[0] : 0.0, f = 0.0;
+    for (int i = 0; i < m; ++i) {
+        if (i + 1 < m) {
+            double sub = b[i];
+            double nd = a[i + 1] - lam, ne = (i + 2 < m) ? b[i + 1] : 0.0;
+            if (fabs(d) >= fabs(sub)) {
+                piv[i] = 0;
+                double mult = (d != 0.0) ? sub / d : 0.0;
+                l[i] = mult;
+                u0[i] = d, u1[i] = e, u2[i] = f;
+                d = nd - mult * e;
+                e = ne - mult * f;
+                f = 0.0;
+                if (fabs(u0[i]) < tiny) u0[i] = tiny;
+            } else {
+                piv[i] = 1;
+                double mult = d / sub;
+                l[i] = mult;
+                u0[i] = sub, u1[i] = nd, u2[i] = ne;
+                double nd2 = e - mult * nd, ne2 = f - mult * ne;
+                d = nd2;
+                e = ne2;
+                f = 0.0;
+            }
+        } else {
+            u0[i] = (fabs(d) < tiny) ? tiny : d;
+            u1[i] = 0.0;
+            u2[i] = 0.0;
+            piv[i] = 0;
+            l[i] = 0.0;
+        }
+    }
+    for (int i = 0; i < m; ++i) y[i] = 1.0;
+    for (int it = 0; it < 4; ++it) {
+        // forward: apply row operations
+        for (int i = 0; i + 1 < m; ++i) {
+            if (piv[i]) {
+                double t = y[i];
+                y[i] = y[i + 1];
+                y[i + 1] = t;
+            }
+            y[i + 1] -= l[i] * y[i];
+        }
+        // back substitution
+        for (int i = m - 1; i >= 0; --i) {
+            double v = y[i];
+            if (i + 1 < m) v -= u1[i] * y[i + 1];
+            if (i + 2 < m) v -= u2[i] * y[i + 2];
+            y[i] = v / u0[i];
+        }
+        double nrm = 0.0;
+        for (int i = 0; i < m; ++i) nrm += y[i] * y[i];
+        nrm = sqrt(nrm);
+        for (int i = 0; i < m; ++i) y[i] /= nrm;
+    }
+}
+
+__global__ void k_axpby(double* __restrict__ y, const double* __restrict__ x, double a, double b, int64_t n) {
+    // y = b*y + a*x
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        y[r] = b * y[r] + a * x[r];
+}
+
+static qsi_status lowest_of_tridiag(const std::vector<double>& al, const std::vector<double>& be, double& e0,
+                                    cudaStream_t st) {
+    const int m = (int)al.size();
+    double lo = 1e300, hi = -1e300;
+    for (int i = 0; i < m; ++i) {
+        double r = (i ? std::fabs(be[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(be[i]) : 0.0);
+        lo = std::min(lo, al[i] - r);
+        hi = std::max(hi, al[i] + r);
+    }
+    DevBuf<double> d;
+    QSI_CUDA(d.alloc((size_t)2 * m + 1));
+    QSI_CUDA(cudaMemcpyAsync(d.p, al.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
+    if (m > 1) QSI_CUDA(cudaMemcpyAsync(d.p + m, be.data(), (size_t)(m - 1) * 8, cudaMemcpyHostToDevice, st));
+    k_tridiag_lowest<<<1, 256, 0, st>>>(d.p, d.p + m, m, lo - 1e-12 * std::fabs(lo) - 1e-300, hi, d.p + 2 * m);
+    QSI_CUDA(cudaMemcpyAsync(&e0, d.p + 2 * m, 8, cudaMemcpyDeviceToHost, st));
+    QSI_CUDA(cudaStreamSynchronize(st));
+    return QSI_OK;
+}
+
+}  // namespace qsi
+
+using namespace qsi;
+
+extern "C" qsi_status qsi_lanczos_solve(qsi_op* op, const qsi_lanczos_cfg* cfg, double* evals, double* evecs,
+                                        qsi_report* report) {
+    return guarded([&]() -> qsi_status {
+        if (!op || !cfg || !evals) return fail(QSI_INVALID_ARG, "qsi_lanczos_solve: null argument");
+        if (report) std::memset(report, 0, sizeof(*report));
+        if (cfg->precision == QSI_F32) return trlan<float>(op, *cfg, evals, evecs, report);
+        return trlan<double>(op, *cfg, evals, evecs, report);
+    });
+}
+
+// projED::lanczos::eigval0 (components/linalg_routines/src/lanczos.cpp:67-227):
+// unit start vector from std::mt19937(seed) + std::normal_distribution
+// (set_random_unit, :55-62); u = -beta*u_prev + H v, alpha = <v,u>, u -= alpha v,
+// beta = |u|; stop when beta < abs_tol, or from min_iterations on when the
+// lowest Ritz value changes by less than abs_tol (absolute) or rel_tol
+// (relative); a second identical pass accumulates the Ritz vector.
+extern "C" qsi_status qsi_eigval0(qsi_op* op, const qsi_eigval0_cfg* cfg, double* e0, double* eigvec,
+                                  int32_t* iterations) {
+    return guarded([&]() -> qsi_status {
+        if (!op || !cfg || !e0) return fail(QSI_INVALID_ARG, "qsi_eigval0: null argument");
+        const int64_t n = op->basis->n;
+        cudaStream_t st = op->stream;
+        std::vector<double> v0(n);
+        {
+            std::mt19937 rng((unsigned)cfg->seed);
+            std::normal_distribution<double> dist(0.0, 1.0);
+            for (auto& x : v0) x = dist(rng);
+            double nrm = 0.0;
+            for (double x : v0) nrm += x * x;
+            nrm = std::sqrt(nrm);
+            for (auto& x : v0) x /= nrm;
+        }
+        Vecs vx;
+        qsi_status s = vx.init(n, st);
+        if (s) return s;
+        DevBuf<double> v, u, ev;
+        QSI_CUDA(v.alloc(n));
+        QSI_CUDA(u.alloc(n));
+        std::vector<double> alphas, betas, ritz, h;
+        double eig = 1e308, e0_pass0 = 0.0;
+        int its = 0;
+        for (int pass = 0; pass < (cfg->calc_eigenvector ? 2 : 1); ++pass) {
+            QSI_CUDA(cudaMemcpyAsync(v.p, v0.data(), (size_t)n * 8, cudaMemcpyHostToDevice, st));
+            QSI_CUDA(cudaMemsetAsync(u.p, 0, (size_t)n * 8, st));
+            if (pass == 1) {
+                QSI_CUDA(ev.alloc(n));
+                QSI_CUDA(cudaMemsetAsync(ev.p, 0, (size_t)n * 8, st));
+            }
+            std::vector<double> al, be;
+            double beta = 0.0;
+            int it;
+            if (pass == 1) eig = 1e308;
+            for (it = 0; it < cfg->max_iterations; ++it) {
+                if (pass == 1 && it < (int)ritz.size())
+                    k_axpby<<<grid_for(n, 256), 256, 0, st>>>(ev.p, v.p, ritz[it], 1.0, n);
+                if (it > 0) k_axpby<<<grid_for(n, 256), 256, 0, st>>>(u.p, v.p, 0.0, -beta, n);
+                s = launch_apply(op, v.p, u.p, 1, QSI_F64, 1, st);
+                if (s) return s;
+                s = vx.dots<double>(v.p, n, 1, u.p, h);
+                if (s) return s;
+                double alpha = h[0];
+                k_axpby<<<grid_for(n, 256), 256, 0, st>>>(u.p, v.p, -alpha, 1.0, n);
+                s = vx.dots<double>(v.p, n, 0, u.p, h);
+                if (s) return s;
+                beta = std::sqrt(h[0]);
+                if (beta < cfg->abs_tol) break;
+                std::swap(v.p, u.p);
+                k_axpby<<<grid_for(n, 256), 256, 0, st>>>(v.p, v.p, 0.0, 1.0 / beta, n);
+                al.push_back(alpha);
+                be.push_back(beta);
+                // The first pass never stops on convergence (lanczos.cpp:163-167 breaks
+                // only when a Ritz vector is being accumulated); the second pass does.
+                if (pass == 1 && it >= cfg->min_iterations) {
+                    double old = eig;
+                    std::vector<double> b2(be.begin(), be.end() - 1);
+                    s = lowest_of_tridiag(al, b2, eig, st);
+                    if (s) return s;
+                    double err = std::fabs(eig - old);
+                    double rel = err / std::max(std::fabs(eig), 1e-10);
+                    if (err < cfg->abs_tol || rel < cfg->rel_tol) break;
+                }
+            }
+            if (pass == 0) {
+                its = it;
+                alphas = al;
+                betas = be;
+                std::vector<double> b2(be.begin(), be.empty() ? be.end() : be.end() - 1);
+                s = lowest_of_tridiag(al, b2, eig, st);
+                if (s) return s;
+                e0_pass0 = eig;
+                if (cfg->calc_eigenvector) {
+                    const int m = (int)al.size();
+                    DevBuf<double> d, work, y;
+                    QSI_CUDA(d.alloc((size_t)2 * m));
+                    QSI_CUDA(work.alloc((size_t)5 * m + 8));
+                    QSI_CUDA(y.alloc((size_t)m));
+                    QSI_CUDA(cudaMemcpyAsync(d.p, al.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
+                    if (m > 1) QSI_CUDA(cudaMemcpyAsync(d.p + m, b2.data(), (size_t)(m - 1) * 8, cudaMemcpyHostToDevice, st));
+                    k_tridiag_vector<<<1, 32, 0, st>>>(d.p, d.p + m, m, eig, work.p, y.p);
+                    ritz.resize(m);
+                    QSI_CUDA(cudaMemcpyAsync(ritz.data(), y.p, (size_t)m * 8, cudaMemcpyDeviceToHost, st));
+                    QSI_CUDA(cudaStreamSynchronize(st));
+                }
+            }
+        }
+        *e0 = e0_pass0;
+        if (iterations) *iterations = its;
+        if (cfg->calc_eigenvector && eigvec) {
+            QSI_CUDA(cudaMemcpy(eigvec, ev.p, (size_t)n * 8, cudaMemcpyDeviceToHost));
+        }
+        return QSI_OK;
+    });
+}
+
+// ------------------------------------------------------------------ FTLM
+namespace qsi {
+
+// Rademacher start vectors +-1/sqrt(n), one per column r: [row][R] layout.
+template <typename VT>
+__global__ void k_ftlm_init(VT* __restrict__ cur, VT* __restrict__ prev, int64_t n, int R, uint64_t seed) {
+    const double inv = rsqrt((double)n);
+    const int64_t total = n * R;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / R;
+        const int r = (int)(e % R);
+        uint64_t h = splitmix64(seed ^ splitmix64(((uint64_t)r << 40) ^ (uint64_t)i));
+        cur[e] = (VT)((h >> 63) ? inv : -inv);
+        prev[e] = (VT)0;
+    }
+}
+
+// Column dot products over [row][R] data: partial[b*R + r] = sum_i a[i][r] b[i][r].
+template <typename VT, typename WT>
+__global__ void __launch_bounds__(256) k_col_dots(const VT* __restrict__ a, const WT* __restrict__ b, int64_t n, int R,
+                                                  double* __restrict__ partial) {
+    extern __shared__ double sh[];  // blockDim.x
+    const int rows_per_pass = blockDim.x / R;  // R divides blockDim (R <= 256, power of two)
+    const int r = threadIdx.x % R, sub = threadIdx.x / R;
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+    double acc = 0.0;
+    for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) acc += (double)a[i * R + r] * (double)b[i * R + r];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    if (sub == 0) {
+        double t = 0.0;
+        for (int s = 0; s < rows_per_pass; ++s) t += sh[s * R + r];
+        partial[(int64_t)blockIdx.x * R + r] = t;
+    }
+}
+
+__global__ void k_col_reduce(const double* __restrict__ partial, int nblocks, int R, double* __restrict__ out,
+                             int sqrt_out) {
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        double t = 0.0;
+        for (int b = 0; b < nblocks; ++b) t += partial[(int64_t)b * R + r];
+        out[r] = sqrt_out ? sqrt(t) : t;
+    }
+}
+
+// prev <- w - alpha cur - beta_prev prev (per column), partial column sums of its square.
+template <typename VT, typename WT>
+__global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, const VT* __restrict__ cur,
+                                                     const WT* __restrict__ w, const double* __restrict__ alpha,
+                                                     const double* __restrict__ beta_prev, int64_t n, int R,
+                                                     double* __restrict__ partial) {
+    extern __shared__ double sh[];
+    const int rows_per_pass = blockDim.x / R;
+    const int r = threadIdx.x % R, sub = threadIdx.x / R;
+    const double a = alpha[r], b = beta_prev ? beta_prev[r] : 0.0;
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+    double acc = 0.0;
+    for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) {
+        const int64_t e = i * R + r;
+        double v = (double)w[e] - a * (double)cur[e] - b * (double)prev[e];
+        prev[e] = (VT)v;
+        acc += v * v;
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    if (sub == 0) {
+        double t = 0.0;
+        for (int s = 0; s < rows_per_pass; ++s) t += sh[s * R + r];
+        partial[(int64_t)blockIdx.x * R + r] = t;
+    }
+}
+
+template <typename VT>
+__global__ void k_col_scale(VT* __restrict__ v, const double* __restrict__ beta, int64_t n, int R) {
+    const int64_t total = n * R;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const double b = beta[e % R];
+        v[e] = (VT)((double)v[e] / (b > 0 ? b : 1.0));
+    }
+}
+
+constexpr int kColGrid = 512;
+
+template <typename VT>
+static qsi_status ftlm_sector(qsi_op* op, int R, int M, uint64_t seed, double* alphas, double* betas,
+                              cudaStream_t st) {
+    const int64_t n = op->basis->n;
+    if (R <= 0 || R > 256 || (R & (R - 1))) return fail(QSI_INVALID_ARG, "ftlm: R must be a power of two in [1,256]");
+    DevBuf<VT> P, C, W;
+    DevBuf<double> partial, ab;
+    QSI_CUDA(P.alloc((size_t)n * R));
+    QSI_CUDA(C.alloc((size_t)n * R));
+    QSI_CUDA(W.alloc((size_t)n * R));
+    QSI_CUDA(partial.alloc((size_t)kColGrid * R));
+    QSI_CUDA(ab.alloc((size_t)2 * M * R));
+    double* dA = ab.p;          // [M][R]
+    double* dB = ab.p + M * R;  // [M][R]
+    k_ftlm_init<VT><<<grid_for(n * R, 256), 256, 0, st>>>(C.p, P.p, n, R, seed);
+    const int blk = 256;
+    const size_t sh = (size_t)blk * 8;
+    // the whole M-step recurrence is captured into one CUDA graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    QSI_CUDA(cudaStreamSynchronize(st));
+    QSI_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    VT *prev = P.p, *cur = C.p;
+    qsi_status s = QSI_OK;
+    for (int j = 0; j < M && s == QSI_OK; ++j) {
+        s = launch_apply(op, cur, W.p, R, sizeof(VT) == 4 ? QSI_F32 : QSI_F64, 0, st);
+        k_col_dots<VT, VT><<<kColGrid, blk, sh, st>>>(cur, W.p, n, R, partial.p);
+        k_col_reduce<<<1, 256, 0, st>>>(partial.p, kColGrid, R, dA + (size_t)j * R, 0);
+        k_ftlm_update<VT, VT><<<kColGrid, blk, sh, st>>>(prev, cur, W.p, dA + (size_t)j * R,
+                                                         j ? dB + (size_t)(j - 1) * R : nullptr, n, R, partial.p);
+        k_col_reduce<<<1, 256, 0, st>>>(partial.p, kColGrid, R, dB + (size_t)j * R, 1);
+        k_col_scale<VT><<<grid_for(n * R, 256), 256, 0, st>>>(prev, dB + (size_t)j * R, n, R);
+        std::swap(prev, cur);
+    }
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (s != QSI_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return s;
+    }
+    QSI_CUDA(ce);
+    QSI_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    cudaError_t e = cudaGraphLaunch(exec, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "ftlm graph: %s", cudaGetErrorString(e));
+    std::vector<double> h((size_t)2 * M * R);
+    QSI_CUDA(cudaMemcpy(h.data(), ab.p, h.size() * 8, cudaMemcpyDeviceToHost));
+    for (int r = 0; r < R; ++r)
+        for (int j = 0; j < M; ++j) {
+            alphas[(size_t)r * M + j] = h[(size_t)j * R + r];
+            betas[(size_t)r * M + j] = h[(size_t)M * R + (size_t)j * R + r];
+        }
+    return QSI_OK;
+}
+
+}  // namespace qsi
+
+extern "C" qsi_status qsi_ftlm_run(qsi_op** ops, int32_t n_sectors, const int32_t* R, int32_t M, uint64_t seed,
+                                   int32_t precision, double* alphas, double* betas) {
+    return guarded([&]() -> qsi_status {
+        if (!ops || n_sectors <= 0 || !R || M <= 0 || !alphas || !betas) return fail(QSI_INVALID_ARG, "qsi_ftlm_run: bad argument");
+        size_t off = 0;
+        for (int s = 0; s < n_sectors; ++s) {
+            if (!ops[s]) return fail(QSI_INVALID_ARG, "qsi_ftlm_run: null operator");
+            uint64_t sseed = seed + (uint64_t)s;  // sector s alone with seed+s gives the same vectors
+            qsi_status st = (precision == QSI_F32)
+                                ? ftlm_sector<float>(ops[s], R[s], M, sseed, alphas + off, betas + off, ops[s]->stream)
+                                : ftlm_sector<double>(ops[s], R[s], M, sseed, alphas + off, betas + off, ops[s]->stream);
+            if (st) return st;
+            off += (size_t)R[s] * M;
+        }
+        return QSI_OK;
+    });
+}
+
+// Batched eigen-decomposition of symmetric tridiagonals (FTLM Ritz data).
+extern "C" qsi_status qsi_tridiag_ritz(const double* a, const double* b, int32_t m, int32_t n_mat, double* evals,
+                                       double* first) {
+    return guarded([&]() -> qsi_status {
+        if (!a || !b || m <= 0 || n_mat <= 0 || !evals || !first) return fail(QSI_INVALID_ARG, "qsi_tridiag_ritz: bad argument");
+        std::vector<double> A((size_t)n_mat * m * m, 0.0), w, V;
+        for (int k = 0; k < n_mat; ++k)
+            for (int i = 0; i < m; ++i) {
+                A[(size_t)k * m * m + i * m + i] = a[(size_t)k * m + i];
+                if (i + 1 < m) {
+                    A[(size_t)k * m * m + i * m + i + 1] = b[(size_t)k * m + i];
+                    A[(size_t)k * m * m + (i + 1) * m + i] = b[(size_t)k * m + i];
+                }
+            }
+        qsi_status s = jacobi_eigh(A, m, n_mat, w, V, nullptr);
+        if (s) return s;
+        for (int k = 0; k < n_mat; ++k)
+            for (int j = 0; j < m; ++j) {
+                evals[(size_t)k * m + j] = w[(size_t)k * m + j];
+                first[(size_t)k * m + j] = V[(size_t)k * m * m + j];
+            }
+        return QSI_OK;
+    });
+}

@@ -1,0 +1,116 @@
+// Device-side data structures shared by the CUDA translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "qsi_internal.h"
+
+namespace qsi {
+
+// A 128-bit basis state as stored in HBM: x = low word, y = high word.
+using state2 = ulonglong2;
+
+// Pull-form off-diagonal term: applicability masks are those of the
+// transposed operator, so a row state s is admitted when
+// (s & down) == 0 && (s & up) == up, and its column is s ^ X.
+// The matrix element is cs * (-1)^popcount(~s & Z).
+struct PullTerm {
+    uint64_t x0, x1, z0, z1, up0, up1, dn0, dn1;
+    double cs;  // coefficient times construction sign
+    int32_t has_z;
+    int32_t pad;
+};
+
+// Push-form term (the reference's own orientation; used for connectivity
+// export and for generic diagonal terms).
+struct PushTerm {
+    uint64_t x0, x1, z0, z1, up0, up1, dn0, dn1;
+    double c;
+    int32_t sign;
+    int32_t pad;
+};
+
+// Diagonal part: single-site pure-z terms grouped by weight w into masks,
+// contributing w * (2 * popcount(s & M) - popcount(M)); remaining diagonal
+// terms are evaluated one by one.
+constexpr int kMaxZClasses = 32;
+struct DiagSpec {
+    int n_cls;
+    int n_generic;
+    double w2[kMaxZClasses];  // 2*w
+    uint64_t m0[kMaxZClasses], m1[kMaxZClasses];
+    double constant;  // -sum_k w_k * popcount(M_k)
+};
+
+// Sorted basis with a direct bucket table over the top `bits` bits below
+// `shift`: bucket(s) = s >> shift; bstart[v] .. bstart[v+1] is the index
+// range of states in bucket v.
+struct BasisView {
+    const state2* states;
+    const uint32_t* bstart;
+    int64_t n;
+    int shift;
+    uint32_t n_buckets;
+};
+
+__device__ __forceinline__ bool less128(uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi) {
+    return ahi < bhi || (ahi == bhi && alo < blo);
+}
+
+__device__ __forceinline__ uint64_t bucket_of(const BasisView& B, uint64_t lo, uint64_t hi, bool& in_range) {
+    uint64_t v;
+    if (B.shift >= 64) {
+        v = hi >> (B.shift - 64);
+    } else if (B.shift == 0) {
+        v = lo;
+        if (hi) v = ~0ULL;
+    } else {
+        if (hi >> B.shift) v = ~0ULL;
+        else v = (hi << (64 - B.shift)) | (lo >> B.shift);
+    }
+    in_range = v < B.n_buckets;
+    return v;
+}
+
+// Exact index of state (lo, hi) in the basis, or -1.
+__device__ __forceinline__ int64_t basis_find(const BasisView& B, uint64_t lo, uint64_t hi) {
+    bool ok;
+    uint64_t v = bucket_of(B, lo, hi, ok);
+    if (!ok) return -1;
+    uint32_t a = __ldg(B.bstart + v), b = __ldg(B.bstart + v + 1);
+    while (a < b) {
+        uint32_t m = (a + b) >> 1;
+        state2 e = __ldg(B.states + m);
+        if (less128(e.x, e.y, lo, hi)) a = m + 1;
+        else b = m;
+    }
+    if (a < (uint32_t)B.n) {
+        state2 e = __ldg(B.states + a);
+        if (e.x == lo && e.y == hi) return (int64_t)a;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ double diag_value(const DiagSpec& D, const PushTerm* gen, uint64_t s0, uint64_t s1) {
+    double d = D.constant;
+    for (int k = 0; k < D.n_cls; ++k) d += D.w2[k] * (double)(__popcll(s0 & D.m0[k]) + __popcll(s1 & D.m1[k]));
+    for (int k = 0; k < D.n_generic; ++k) {
+        const PushTerm& T = gen[k];
+        bool ok = ((s0 & T.dn0) | (s1 & T.dn1)) == 0 && (s0 & T.up0) == T.up0 && (s1 & T.up1) == T.up1;
+        if (!ok) continue;
+        int par = (__popcll(~s0 & T.z0) + __popcll(~s1 & T.z1)) & 1;
+        d += T.c * (double)(T.sign * (1 - 2 * par));
+    }
+    return d;
+}
+
+}  // namespace qsi
+
+#define QSI_CUDA(call)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            return ::qsi::fail(e_ == cudaErrorMemoryAllocation ? QSI_OOM : QSI_CUDA_ERROR,        \
+                               "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+        }                                                                                         \
+    } while (0)

@@ -1,0 +1,38 @@
+// Handle layouts behind the opaque qsi_basis / qsi_op pointers of the C-ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <vector>
+
+#include "qsi_device.cuh"
+
+struct qsi_basis {
+    int64_t n = 0;
+    int bits = 0, shift = 0;
+    uint32_t n_buckets = 0;
+    qsi::state2* d_states = nullptr;
+    uint32_t* d_bstart = nullptr;
+    qsi::BasisView view() const { return qsi::BasisView{d_states, d_bstart, n, shift, n_buckets}; }
+};
+
+struct qsi_op {
+    qsi_basis* basis = nullptr;
+    qsi::PullTerm* d_pull = nullptr;        // transposed off-diagonal terms (apply)
+    qsi::PushTerm* d_push_off = nullptr;    // off-diagonal terms as given (export)
+    qsi::PushTerm* d_push_diag = nullptr;   // diagonal terms as given (export)
+    qsi::PushTerm* d_diag_generic = nullptr;
+    int n_pull = 0, n_push_off = 0, n_push_diag = 0, n_diag_generic = 0;
+    qsi::DiagSpec diag{};
+    size_t smem_bytes = 0;
+    cudaStream_t stream = nullptr;
+    void* d_x = nullptr;   // staging for host-pointer applies
+    void* d_y = nullptr;
+    size_t staging_bytes = 0;
+};
+
+namespace qsi {
+int grid_for(int64_t n, int block);
+qsi_status launch_apply(qsi_op* op, const void* x, void* y, int R, int dtype, int accumulate, cudaStream_t st);
+// y = H x with x stored as xdtype and y always FP64 (single vector).
+qsi_status launch_apply_to_f64(qsi_op* op, const void* x, double* y, int xdtype, cudaStream_t st);
+qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vector<double>& w, std::vector<double>& V, cudaStream_t st);
+}  // namespace qsi

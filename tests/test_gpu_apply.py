@@ -1,0 +1,146 @@
+"""GPU apply, lookup and connectivity through the C-ABI against the oracle."""
+import numpy as np
+import pytest
+
+import qsi_subspace_ed_gb300 as q
+from helpers import GOLDEN, cases, golden_json
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["golden48_JpmB", "ref32_g", "ref32_JpmB", "cfg1", "s4444"]
+
+
+@pytest.fixture(scope="module")
+def built():
+    out = {}
+    for name, (basis, H) in cases().items():
+        b = q.ZBasis(basis)
+        out[name] = (basis, H, b, q.LazyOpSum(b, H))
+    return out
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_triplets_bit_exact(built, name):
+    basis, H, b, op = built[name]
+    r, c, v = op.triplets()
+    ref = golden_json("triplets.json")[name]
+    assert len(r) == ref["n_triplets"]
+    assert O.triplet_digest(r, c, v) == ref["sha256"]
+    ro, co, vo = O.triplets_port(basis, H.specs())
+    assert np.array_equal(r, ro) and np.array_equal(c, co) and np.array_equal(v, vo)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_search_exact(built, name):
+    basis, H, b, op = built[name]
+    idx = b.search(basis)
+    assert np.array_equal(idx, np.arange(len(basis)))
+    # flipped non-members: not found
+    rng = np.random.default_rng(1)
+    probe = basis[rng.integers(0, len(basis), 500)].copy()
+    probe[:, 0] ^= np.uint64(1)
+    member = {tuple(x) for x in basis.tolist()}
+    expect = np.array([(-1 if tuple(p) not in member else None) for p in probe.tolist()], dtype=object)
+    got = b.search(probe)
+    for e, g, p in zip(expect, got, probe.tolist()):
+        if e is None:
+            assert basis[g].tolist() == p
+        else:
+            assert g == -1
+    # beyond the top bucket and the empty state
+    assert b.search(np.array([[0, 2**63]], np.uint64))[0] == -1
+    assert q.ZBasis(basis[:1]).search(basis[:2]).tolist() == [0, -1]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_apply_fp64_matches_oracle(built, name):
+    basis, H, b, op = built[name]
+    x = np.random.default_rng(7).standard_normal(len(basis))
+    y_ref = O.apply_port(basis, H.specs(), x, threads=1)
+    y = np.zeros_like(x)
+    op.evaluate(x, y)
+    np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+    # deterministic (pull form, fixed summation order)
+    y2 = np.zeros_like(x)
+    op.evaluate(x, y2)
+    assert np.array_equal(y, y2)
+    # accumulate: y += H x
+    y3 = x.copy()
+    op.evaluate_add(x, y3)
+    np.testing.assert_allclose(y3, x + y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+
+
+def test_apply_matches_reference_stored_applies(built):
+    for fname, name in [("apply_ref32.npy", "ref32_g"), ("apply_cfg1.npy", "cfg1")]:
+        x, y_ref = np.load(GOLDEN / fname)
+        y = np.zeros_like(x)
+        built[name][3].evaluate(x, y)
+        np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+
+
+def test_apply_tol_skips_tiny_sources(built):
+    basis, H, b, op = built["cfg1"]
+    x = np.zeros(len(basis))
+    x[5] = 1.0
+    x[17] = 5e-16  # below APPLY_TOL: its off-diagonal pushes are dropped
+    y = np.zeros_like(x)
+    op.evaluate(x, y)
+    np.testing.assert_allclose(y, O.apply_port(basis, H.specs(), x, threads=1), rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("R", [1, 3, 32, 64, 100])
+def test_batched_apply(built, R):
+    basis, H, b, op = built["golden48_JpmB"]
+    n = len(basis)
+    X = np.random.default_rng(R).standard_normal((n, R))
+    Y = np.zeros_like(X)
+    op.apply_batched(X, Y)
+    cols = [0, R - 1, R // 2]
+    for c in cols:
+        y = np.zeros(n)
+        op.evaluate(np.ascontiguousarray(X[:, c]), y)
+        np.testing.assert_allclose(Y[:, c], y, rtol=0, atol=1e-12 * np.abs(y).max())
+    X32 = X.astype(np.float32)
+    Y32 = np.zeros_like(X32)
+    op.apply_batched(X32, Y32)
+    Yd = np.zeros_like(X)
+    op.apply_batched(X32.astype(np.float64), Yd)
+    np.testing.assert_allclose(Y32, Yd, rtol=2e-6, atol=2e-6 * np.abs(Yd).max())
+
+
+def test_device_pointers_and_stream(built):
+    torch = pytest.importorskip("torch")
+    basis, H, b, op = built["cfg1"]
+    x = torch.randn(len(basis), dtype=torch.float64, device="cuda")
+    y = torch.zeros_like(x)
+    op.evaluate(x, y)
+    torch.cuda.synchronize()
+    y_ref = O.apply_port(basis, H.specs(), x.cpu().numpy(), threads=1)
+    np.testing.assert_allclose(y.cpu().numpy(), y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+
+
+def test_projected_hopping_drops_misses():
+    """Bond hopping leaves the ice manifold: misses are dropped, as the reference's push loop does."""
+    from qsi_subspace_ed_gb300 import workloads
+
+    lat = workloads.lattice("pyro_1x2x1")
+    basis = q.enumerate_basis(lat)
+    H = q.build_ring_zeeman(lat, [1, .8, .6, .4], [0.1, 0.2, -0.1], Jpm=0.05)
+    b = q.ZBasis(basis)
+    op = q.LazyOpSum(b, H)
+    assert op.count_misses() > 0
+    x = np.random.default_rng(3).standard_normal(len(basis))
+    y = np.zeros_like(x)
+    op.evaluate(x, y)
+    y_ref = O.apply_port(basis, H.specs(), x, threads=1)
+    np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+    r, c, v = op.triplets()
+    assert O.triplet_digest(r, c, v) == O.triplet_digest(*O.triplets_port(basis, H.specs()))
+
+
+def test_basis_errors():
+    with pytest.raises(q.QsiError):
+        q.ZBasis(np.array([[5, 0], [3, 0]], np.uint64))  # not increasing
+    with pytest.raises(q.QsiError):
+        q.ZBasis(np.zeros((0, 2), np.uint64))

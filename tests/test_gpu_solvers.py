@@ -1,0 +1,98 @@
+"""GPU Lanczos / FTLM against the FP64 oracles and the reference's golden answer."""
+import numpy as np
+import pytest
+
+import qsi_subspace_ed_gb300 as q
+from helpers import GOLDEN, cases, golden_json
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def test_golden_e0_through_eigval0():
+    """test/test_correct.sh: 48 spins, Jpm=0.02, B=(0.1,0.1,0.1), mfeig0, seed 11, atol/rtol 1e-9."""
+    g = golden_json("golden48.json")
+    basis, H = cases()["golden48_JpmB"]
+    b = q.ZBasis(basis)
+    op = q.LazyOpSum(b, H)
+    e0, vec, its = q.eigval0(op, seed=g["rng_seed"], abs_tol=g["atol"], rel_tol=g["rtol"], min_iterations=10)
+    assert abs(e0 - g["E0"]) <= g["eigval_tol"]
+    ref = np.load(GOLDEN / "golden48_evec.npy").astype(np.float64)
+    ov = abs(vec @ ref) / (np.linalg.norm(vec) * np.linalg.norm(ref))
+    assert ov > 1 - 1e-6
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_config1_lowest_five(precision):
+    """Config 1: ncv=15, 5 eigenvalues, tol 1e-10, against the FP64 dense oracle."""
+    basis, H = cases()["cfg1"]
+    ref = golden_json("eigs_cfg1.json")["evals"]
+    op = q.LazyOpSum(q.ZBasis(basis), H)
+    w, V, rep = q.diagonalise(op, nev=5, ncv=15, tol=1e-10, seed=1, precision=precision,
+                              polish_steps=2 if precision == "mixed" else 0)
+    np.testing.assert_allclose(w, ref[:5], atol=1e-9)
+    assert np.all(rep.residual[:5] < 1e-6)
+    # eigenvectors: H v = lambda v
+    for k in range(5):
+        y = np.zeros(len(basis))
+        op.evaluate(np.ascontiguousarray(V[:, k]), y)
+        assert np.linalg.norm(y - w[k] * V[:, k]) < 1e-6 * np.linalg.norm(V[:, k])
+
+
+def test_lanczos_small_dimension_exhausts_krylov_space():
+    basis, H = cases()["s4444"]
+    op = q.LazyOpSum(q.ZBasis(basis[:40]), H)
+    w, V, rep = q.diagonalise(op, nev=3, ncv=60, tol=1e-12)
+    r, c, v = O.triplets_port(basis[:40], H.specs())
+    ref = np.linalg.eigvalsh(O.csr_from_triplets(r, c, v, 40).toarray())
+    np.testing.assert_allclose(w, ref[:3], atol=1e-10)
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_ftlm_against_exact_thermodynamics(precision):
+    basis, H = cases()["s4444"]
+    th = np.load(GOLDEN / "thermo_s4444.npz")
+    op = q.LazyOpSum(q.ZBasis(basis), H)
+    (al, be), = q.ftlm([op], [64], M=60, seed=5, precision=precision)
+    assert al.shape == (64, 60)
+    out = q.ftlm_thermo(al, be, len(basis), th["T"])
+    hi = th["T"] > 0.5
+    np.testing.assert_allclose(out["C"][hi], th["C"][hi], rtol=0.15, atol=0.02)
+    # the FTLM ground-state estimate is the exact one
+    r, c, v = O.triplets_port(basis, H.specs())
+    e_exact = np.linalg.eigvalsh(O.csr_from_triplets(r, c, v, len(basis)).toarray())[0]
+    assert abs(out["e_ref"] - e_exact) < 1e-8
+
+
+def test_ftlm_mixed_matches_fp64():
+    basis, H = cases()["cfg1"]
+    op = q.LazyOpSum(q.ZBasis(basis), H)
+    T = np.logspace(-2, 1, 200)
+    (a64, b64), = q.ftlm([op], [32], M=50, seed=9, precision="f64")
+    (a32, b32), = q.ftlm([op], [32], M=50, seed=9, precision="mixed")
+    t64 = q.ftlm_thermo(a64, b64, len(basis), T)
+    t32 = q.ftlm_thermo(a32, b32, len(basis), T)
+    np.testing.assert_allclose(a32[:, :10], a64[:, :10], atol=1e-5)
+    np.testing.assert_allclose(t32["C"], t64["C"], rtol=1e-3, atol=1e-4)
+
+
+def test_ftlm_multi_sector_batch():
+    cs = cases()
+    ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["cfg1", "s4444"]]
+    res = q.ftlm(ops, [32, 16], M=30, seed=2, precision="mixed")
+    assert [r[0].shape for r in res] == [(32, 30), (16, 30)]
+    # each sector alone (seed + sector index) gives bit-identical recurrences
+    alone = q.ftlm([ops[1]], [16], M=30, seed=3, precision="mixed")
+    assert np.array_equal(alone[0][0], res[1][0]) and np.array_equal(alone[0][1], res[1][1])
+
+
+def test_tridiag_ritz_matches_numpy():
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal((5, 40))
+    b = np.abs(rng.standard_normal((5, 40))) + 0.1
+    ev, first = q.tridiag_ritz(a, b)
+    for k in range(5):
+        T = np.diag(a[k]) + np.diag(b[k, :-1], 1) + np.diag(b[k, :-1], -1)
+        w, Y = np.linalg.eigh(T)
+        np.testing.assert_allclose(ev[k], w, atol=1e-12)
+        np.testing.assert_allclose(first[k] ** 2, Y[0] ** 2, atol=1e-10)

@@ -1,0 +1,144 @@
+"""Host logic of libqsi_ed.so (no GPU): exports, term compiler, enumerator, file IO, builders."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import qsi_subspace_ed_gb300 as q
+from qsi_subspace_ed_gb300 import _lib, workloads
+from helpers import GOLDEN, golden_json, sha
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_library_exports_every_header_symbol():
+    import ctypes
+
+    header = (ROOT / "include" / "qsi_ed.h").read_text()
+    declared = set(re.findall(r"^\s*(?:qsi_status|void|const char\*)\s+(qsi_\w+)\s*\(", header, re.M))
+    assert declared, "no declarations parsed"
+    lib = ctypes.CDLL(str(_lib.LIB_PATH))
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+    assert declared == set(_lib.SIGNATURES), declared ^ set(_lib.SIGNATURES)
+
+
+def _spec(spec):
+    return q.SymbolicPMROperator(spec)
+
+
+def test_term_compiler_matches_reference_kats():
+    for kat in golden_json("term_kats.json"):
+        op = _spec(kat["spec"])
+        words = [op.t.x[0], op.t.x[1], op.t.z[0], op.t.z[1], op.t.up[0], op.t.up[1], op.t.down[0], op.t.down[1]]
+        assert [str(int(w)) for w in words] == kat["masks"], kat["spec"]
+        assert op.sign == kat["sign"]
+        for s0, s1, sign in kat["apply"]:
+            assert op.applyState(int(s0)) == (int(s1), sign), (kat["spec"], s0)
+
+
+def test_operator_algebra_kats():
+    # test/test_PMR_construct.cpp:164-191
+    a, b = _spec("0Z 1X"), _spec("1Z")
+    assert a * b == _spec("0Z 1X 1Z")
+    assert (_spec("0+") * _spec("0-")).sign == 1
+    assert (_spec("0+") * _spec("0+")).sign == 0
+    assert (_spec("0-") * _spec("0-")).sign == 0
+    assert _spec("0+ 1- 2+ 3-") * _spec("0- 1+ 4- 5+") == _spec("0+ 0- 1- 1+ 2+ 3- 4- 5+")
+    assert _spec("0+ 1- 2+ 3-").applyState(0b111010) == (0b110101, 1)
+    assert _spec("").applyState(12345) == (12345, 1)
+
+
+def test_bad_operator_spec_raises():
+    with pytest.raises(q.QsiError) as e:
+        _spec("3y")
+    assert e.value.status == _lib.QSI_INVALID_ARG
+    with pytest.raises(q.QsiError):
+        _spec("5")
+    with pytest.raises(q.QsiError):
+        _spec("4+ 3k")
+    # the reference tokeniser reads "x+" as op 'x' on spin 0
+    assert _spec("x+") == _spec("0x")
+
+
+def test_enumerator_reproduces_reference_bases():
+    ref = golden_json("bases.json")
+    for name in ["ref16", "ref32", "golden48"]:
+        b = q.enumerate_basis(q.Lattice.load(GOLDEN / "lattices" / f"{name}.json"))
+        assert len(b) == ref[name]["n"] and sha(b) == ref[name]["sha256"], name
+    assert np.array_equal(q.enumerate_basis(q.Lattice.load(GOLDEN / "lattices" / "ref32.json")),
+                          np.load(GOLDEN / "basis_ref32.npy"))
+
+
+def test_enumerator_counts_on_cubic_cells():
+    l32, l64 = workloads.lattice("pyro_1x2x1"), workloads.lattice("pyro_1x2x2")
+    assert len(q.enumerate_basis(l32)) == 3618
+    assert len(q.enumerate_basis(l32, sector=[4, 4, 4, 4])) == 388
+    assert len(q.enumerate_basis(l64, sector=[8, 8, 8, 8])) == 221628
+    b = q.enumerate_basis(l64)
+    assert len(b) == 2891562
+    hi = b[:, 1].astype(object) * 2**64 + b[:, 0].astype(object)
+    assert all(hi[1:] > hi[:-1])
+    # every state obeys the ice rule
+    tets = l64.tetrahedra
+    for s in b[:: 9973]:
+        v = int(s[0]) | (int(s[1]) << 64)
+        assert all(sum((v >> int(k)) & 1 for k in t) == 2 for t in tets)
+
+
+def test_enumerator_spinon_rule_and_orders():
+    l32 = workloads.lattice("pyro_1x2x1")
+    b0 = q.enumerate_basis(l32)
+    b1 = q.enumerate_basis(l32, n_spinon_pairs=1)
+    s0 = {tuple(r) for r in b0.tolist()}
+    assert s0 <= {tuple(r) for r in b1.tolist()}
+    # without spinon pairs the set does not depend on the visiting order
+    assert np.array_equal(q.enumerate_basis(l32, ordering="none"), b0)
+
+
+def test_h5_roundtrip_and_errors(tmp_path):
+    b = np.load(GOLDEN / "basis_ref32.npy")
+    p = tmp_path / "x.h5"
+    q.write_basis_h5(p, b)
+    assert np.array_equal(q.read_basis_h5(p), b)
+    q.write_basis_h5(p, b[:10], dataset="basis_s1.1.1.1", append=True)
+    assert np.array_equal(q.read_basis_h5(p, "basis_s1.1.1.1"), b[:10])
+    assert np.array_equal(q.read_basis_h5(p), b)
+    with pytest.raises(q.QsiError) as e:
+        q.read_basis_h5(p, "nope")
+    assert e.value.status == _lib.QSI_NOT_FOUND
+    with pytest.raises(q.QsiError) as e:
+        q.read_basis_h5(tmp_path / "missing.h5")
+    assert e.value.status == _lib.QSI_IO_ERROR
+    (tmp_path / "trunc.h5").write_bytes(p.read_bytes()[:700])
+    with pytest.raises(q.QsiError):
+        q.read_basis_h5(tmp_path / "trunc.h5")
+    e = tmp_path / "o.eigs.h5"
+    vecs = np.arange(12.0).reshape(6, 2)
+    q.write_eigs_h5(e, [1.0, 2.0], vecs, "lat.json", "basis")
+    assert np.array_equal(q.read_f64_h5(e, "eigenvalues"), [1.0, 2.0])
+    assert np.array_equal(q.read_f64_h5(e, "eigenvectors").reshape(-1), vecs.T.reshape(-1))
+
+
+def test_csv_reader(tmp_path):
+    b = np.load(GOLDEN / "basis_ref32.npy")
+    p = tmp_path / "b.csv"
+    p.write_text("".join(f"0x{int(h):016x}{int(l):016x}\n" for l, h in b))
+    assert np.array_equal(q.read_basis_csv(p), b)
+
+
+def test_hamiltonian_builders():
+    lat = q.Lattice.load(GOLDEN / "lattices" / "golden48.json")
+    H = q.build_hamiltonian(lat, 0.02, [0.1, 0.1, 0.1])
+    assert len(H.off_diag_terms) == 2 * 48 and len(H.diagonal_terms) == 144
+    g = q.g_vals(0.02, [0.1, 0.1, 0.1])
+    assert H.off_diag_terms[0][0] == g[lat.rings[0]["sl"]]
+    # ring pairs are mutual conjugates: equal coefficient, swapped up/down masks
+    for k in range(0, len(H.off_diag_terms), 2):
+        (c1, a), (c2, b) = H.off_diag_terms[k], H.off_diag_terms[k + 1]
+        assert c1 == c2 and a.X_mask == b.X_mask and a.up_mask == b.down_mask
+    Hz = q.build_ring_zeeman(workloads.lattice("pyro_1x2x1"), [1, .8, .6, .4], [0.1, 0.0, 0.0])
+    assert len(Hz.diagonal_terms) == 32 and len(Hz.off_diag_terms) == 64
+    with pytest.raises(RuntimeError):
+        q.build_hamiltonian(q.Lattice.from_dict({**lat.data, "__version__": "1.0"}), 0.02, [0, 0, 0])

@@ -1,0 +1,61 @@
+"""The oracle (CPU restatement) against the reference's golden data."""
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, cases, golden_json, sha
+from oracle import oracle as O
+
+
+def test_oracle_term_compiler_matches_reference_masks():
+    for kat in golden_json("term_kats.json"):
+        toks = kat["spec"].split()
+        t = O.terms_array([(1.0, "".join(x[-1] for x in toks), [int(x[:-1]) for x in toks])])
+        words = t[0, 8:72].view(np.uint64)
+        assert [str(int(w)) for w in words] == kat["masks"], kat["spec"]
+        assert int(t[0, 72:76].view(np.int32)[0]) == kat["sign"], kat["spec"]
+
+
+@pytest.mark.parametrize("name", ["golden48_JpmB", "ref32_g", "ref32_JpmB", "cfg1", "s4444"])
+def test_oracle_triplets_match_reference_digest(name):
+    basis, H = cases()[name]
+    ref = golden_json("triplets.json")[name]
+    assert len(basis) == ref["n_basis"] and sha(basis) == ref["basis_sha256"]
+    r, c, v = O.triplets_port(basis, H.specs())
+    assert len(r) == ref["n_triplets"]
+    assert O.triplet_digest(r, c, v) == ref["sha256"]
+
+
+def test_oracle_apply_matches_reference_apply():
+    cs = cases()
+    for fname, case in [("apply_ref32.npy", "ref32_g"), ("apply_cfg1.npy", "cfg1")]:
+        x, y_ref = np.load(GOLDEN / fname)
+        basis, H = cs[case]
+        y = O.apply_port(basis, H.specs(), x, threads=1)
+        np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-13 * np.abs(y_ref).max())
+
+
+def test_oracle_golden_ground_state_energy():
+    basis, H = cases()["golden48_JpmB"]
+    g = golden_json("golden48.json")
+    r, c, v = O.triplets_port(basis, H.specs())
+    w, V = O.lowest_eigs(r, c, v, len(basis), k=1)
+    assert abs(w[0] - g["E0"]) <= 1e-10
+    ev = np.load(GOLDEN / "golden48_evec.npy").astype(np.float64)
+    assert abs(abs(ev @ V[:, 0]) / np.linalg.norm(ev) - 1.0) < 1e-6
+
+
+def test_oracle_config1_eigs():
+    basis, H = cases()["cfg1"]
+    ref = golden_json("eigs_cfg1.json")["evals"]
+    r, c, v = O.triplets_port(basis, H.specs())
+    w, _ = O.lowest_eigs(r, c, v, len(basis), k=5)
+    np.testing.assert_allclose(w, ref[:5], atol=1e-12)
+
+
+def test_oracle_ftlm_formula_approaches_exact():
+    basis, H = cases()["s4444"]
+    th = np.load(GOLDEN / "thermo_s4444.npz")
+    r, c, v = O.triplets_port(basis, H.specs())
+    f = O.ftlm_oracle(r, c, v, len(basis), R=32, M=60, seed=0, temps=th["T"])
+    hi = th["T"] > 0.5  # FTLM with few vectors is accurate at high T
+    np.testing.assert_allclose(f["C"][hi], th["C"][hi], rtol=0.15, atol=0.02)

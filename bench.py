@@ -202,7 +202,7 @@ def run_ours(args):
     hits, misses = op.connectivity()
     h = hits / n
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.current_stream(dev)  # the applies below are launched on this stream too
     x = torch.randn(n, dtype=torch.float64, device=dev)
     y = torch.zeros_like(x)
     l2_flush = torch.empty(256 * 2**20, dtype=torch.uint8, device=dev)

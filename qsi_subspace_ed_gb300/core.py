@@ -295,10 +295,13 @@ class LazyOpSum:
         return _lib.QSI_PTR_DEVICE if hasattr(a, "is_cuda") and a.is_cuda else _lib.QSI_PTR_HOST
 
     def _stream(self, a):
+        """torch's current stream; its legacy default stream (handle 0) is passed as cudaStreamLegacy,
+        since NULL selects the operator's own stream in the C-ABI."""
         if self._kind(a) == _lib.QSI_PTR_DEVICE:
             import torch
 
-            return C.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+            h = torch.cuda.current_stream(a.device).cuda_stream
+            return C.c_void_p(h if h else _lib.CUDA_STREAM_LEGACY)
         return None
 
     def evaluate_add(self, x, y) -> None:

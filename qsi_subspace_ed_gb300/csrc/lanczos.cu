@@ -271,7 +271,6 @@ __global__ void __launch_bounds__(256) k_jacobi(const double* __restrict__ Ain, 
             perm[i] = perm[best];
             perm[best] = tmp;
         }
-        for (int i = 0; i < M; ++i) cs[i % H] = 0;  // no-op keeps cs in use for small M
     }
     __syncthreads();
     for (int i = threadIdx.x; i < M; i += blockDim.x) eb[i] = A[perm[i] * M + perm[i]];
@@ -738,7 +737,11 @@ __global__ void k_tridiag_vector(const double* __restrict__ a, const double* __r
             l[i] = 0.0;
         }
     }
-    for (int i = 0; i < m; ++i) y[i] = 1.0;
+    // Start from e_0: without reorthogonalisation the long recurrence holds
+    // near-degenerate copies of the lowest Ritz value; the component of e_0 in
+    // that cluster is the copy built from the start of the Lanczos sequence,
+    // which is the part the second pass accumulates.
+    for (int i = 0; i < m; ++i) y[i] = (i == 0) ? 1.0 : 0.0;
     for (int it = 0; it < 4; ++it) {
         // forward: apply row operations
         for (int i = 0; i + 1 < m; ++i) {

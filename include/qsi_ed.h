@@ -127,6 +127,14 @@ qsi_status qsi_basis_create(const uint64_t* lohi, int64_t n, int32_t bucket_bits
                             qsi_basis** out);
 qsi_status qsi_basis_destroy(qsi_basis* b);
 qsi_status qsi_basis_dim(const qsi_basis* b, int64_t* dim);
+/* Rebuilds the lookup index: a top-bits bucket table with bucket_bits bits
+ * (<= 0 keeps the current table) and, with use_hash, an open-addressing
+ * hash index of the states (states of at most 96 bits).  Column lookups use
+ * the hash index when present and enabled on the operator, else the bucket
+ * table plus a binary search of the bucket. */
+qsi_status qsi_basis_index(qsi_basis* b, int32_t use_hash, int32_t bucket_bits);
+qsi_status qsi_basis_info(const qsi_basis* b, int32_t* bucket_bits, int32_t* has_hash,
+                          int64_t* index_bytes);
 /* Exact index lookup of n states (ZBasisBST::search, operator.cpp:4-34):
  * idx[k] = position of states[k] in the basis, or -1 on a miss. */
 qsi_status qsi_basis_search(qsi_basis* b, const uint64_t* states_lohi, int64_t n,
@@ -148,6 +156,11 @@ qsi_status qsi_op_apply(qsi_op* op, const double* x, double* y, int32_t accumula
 qsi_status qsi_op_apply_batched(qsi_op* op, const void* X, void* Y, int32_t R,
                                 int32_t dtype, int32_t accumulate, int32_t flags,
                                 void* stream);
+/* Kernel selection (autotuning): kernel 0 = one row per thread (single
+ * vector) / one warp per row (batched); kernel 1 = bit-sliced 32-row tiles
+ * (default).  use_hash selects the hash index for column lookups;
+ * list_cap (> 0) sets the per-warp hit-list size of the batched tile kernel. */
+qsi_status qsi_op_set_kernel(qsi_op* op, int32_t kernel, int32_t use_hash, int32_t list_cap);
 /* Connectivity export in the order of LazyOpSum::toSparseMatrix
  * (operator_matrix.hpp:79-105): for each basis index j, each off-diagonal
  * term with |c*sign| > tol gives (J, j, c*sign); then (j, j, sum of diagonal

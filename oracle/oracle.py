@@ -29,9 +29,15 @@ REF_SO = HERE / "_ref" / "libqsi_ref.so"
 
 
 def build_port() -> Path:
-    src = HERE / "qsi_oracle.c"
-    if not PORT_SO.exists() or PORT_SO.stat().st_mtime < src.stat().st_mtime:
-        subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", str(src), "-o", str(PORT_SO)], check=True)
+    srcs = [HERE / "qsi_oracle.c", HERE / "start_vector.cpp"]
+    if not PORT_SO.exists() or PORT_SO.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
+        tmp = PORT_SO.with_suffix(".tmp.so")
+        subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-c", str(srcs[0]), "-o", str(HERE / "qsi_oracle.o")],
+                       check=True)
+        subprocess.run(["g++", "-O2", "-fPIC", "-c", str(srcs[1]), "-o", str(HERE / "start_vector.o")], check=True)
+        subprocess.run(["g++", "-shared", "-fopenmp", str(HERE / "qsi_oracle.o"), str(HERE / "start_vector.o"),
+                        "-o", str(tmp)], check=True)
+        os.replace(tmp, PORT_SO)
     return PORT_SO
 
 
@@ -66,6 +72,8 @@ def port():
                                             C.c_int]
         lib.oracle_term_compile.argtypes = [C.c_char_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]
         lib.oracle_apply_state.argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_set_random_unit.restype = None
+        lib.oracle_set_random_unit.argtypes = [C.c_void_p, C.c_int64, C.c_uint]
         lib.oracle_evaluate_add_rows.restype = C.c_int
         lib.oracle_evaluate_add_rows.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_int,
                                                  C.c_void_p, C.c_void_p, C.c_int]
@@ -255,6 +263,60 @@ def ftlm_oracle(r, c, v, n, R, M, seed, temps):
     E2 = (bf @ (ww * x * x)) / Z
     return {"T": np.asarray(temps), "E": E1 + e0, "C": (E2 - E1 * E1) / np.asarray(temps) ** 2, "ritz": ev,
             "weights": w}
+
+
+def set_random_unit(n: int, seed: int) -> np.ndarray:
+    v = np.zeros(n)
+    port().oracle_set_random_unit(_p(v), n, seed)
+    return v
+
+
+def eigval0_oracle(r, c, v, n, seed, abs_tol=1e-8, rel_tol=1e-8, min_iterations=10, max_iterations=5000):
+    """projED::lanczos::eigval0 restated in numpy (components/linalg_routines/src/lanczos.cpp:67-227):
+    first pass to max_iterations (or beta < abs_tol) without stopping on convergence, lowest
+    Ritz pair of the full tridiagonal, second pass accumulating the Ritz vector until the
+    lowest Ritz value changes by less than abs_tol / rel_tol.  Returns (E0, eigvec, iterations)."""
+    from scipy.linalg import eigh_tridiagonal
+
+    A = csr_from_triplets(r, c, v, n)
+    v0 = set_random_unit(n, seed)
+
+    def run(ritz):
+        vv, u = v0.copy(), np.zeros(n)
+        al, be = [], []
+        beta, eig = 0.0, np.inf
+        ev = np.zeros(n) if ritz is not None else None
+        it = 0
+        for it in range(max_iterations + 1):
+            if it == max_iterations:  # loop ran out: n_iterations == max_iterations, as in C
+                break
+            if ritz is not None and it < len(ritz):
+                ev += ritz[it] * vv
+            if it > 0:
+                u *= -beta
+            u += A @ vv
+            a = vv @ u
+            u -= a * vv
+            beta = np.sqrt(u @ u)
+            if beta < abs_tol:
+                break
+            vv, u = u, vv
+            vv *= 1 / beta
+            al.append(a)
+            be.append(beta)
+            if ritz is not None and it >= min_iterations:
+                e = eigh_tridiagonal(np.array(al), np.array(be[:-1]), eigvals_only=True, select="i",
+                                     select_range=(0, 0))[0]
+                err = abs(e - eig)
+                eig = e
+                if err < abs_tol or err / max(abs(e), 1e-10) < rel_tol:
+                    break
+        return al, be, ev, it
+
+    al, be, _, its = run(None)
+    w, Y = eigh_tridiagonal(np.array(al), np.array(be[:-1]), select="i", select_range=(0, 0))
+    _, _, ev, _ = run(Y[:, 0])
+    return float(w[0]), ev, its
 
 
 def cpu_threads() -> int:

@@ -99,10 +99,13 @@ SIGNATURES = {
     "qsi_basis_destroy": [_P],
     "qsi_basis_dim": [_P, C.POINTER(_I64)],
     "qsi_basis_search": [_P, _P, _I64, _P, _I32, _P],
+    "qsi_basis_index": [_P, _I32, _I32],
+    "qsi_basis_info": [_P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I64)],
     "qsi_op_create": [_P, _P, _I32, C.POINTER(_P)],
     "qsi_op_destroy": [_P],
     "qsi_op_apply": [_P, _P, _P, _I32, _I32, _P],
     "qsi_op_apply_batched": [_P, _P, _P, _I32, _I32, _I32, _I32, _P],
+    "qsi_op_set_kernel": [_P, _I32, _I32, _I32],
     "qsi_op_triplets": [_P, _D, _P, _P, _P, _I64, C.POINTER(_I64)],
     "qsi_op_count_misses": [_P, C.POINTER(_I64)],
     "qsi_op_connectivity": [_P, C.POINTER(_I64), C.POINTER(_I64)],

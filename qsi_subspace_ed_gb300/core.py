@@ -256,6 +256,15 @@ class ZBasis:
     def __getitem__(self, i) -> int:
         return int(self.states[i, 0]) | (int(self.states[i, 1]) << 64)
 
+    def set_index(self, use_hash: bool = True, bucket_bits: int = 0) -> None:
+        """Rebuilds the lookup index (top-bits table with bucket_bits bits; optional hash index)."""
+        call("qsi_basis_index", self._h, int(use_hash), int(bucket_bits))
+
+    def index_info(self) -> dict:
+        b, h, nb = C.c_int32(), C.c_int32(), C.c_int64()
+        call("qsi_basis_info", self._h, C.byref(b), C.byref(h), C.byref(nb))
+        return {"bucket_bits": b.value, "hash": bool(h.value), "index_bytes": nb.value}
+
     def search(self, lohi: np.ndarray) -> np.ndarray:
         """Exact indices (or -1) of many states."""
         q = np.ascontiguousarray(lohi, dtype=np.uint64).reshape(-1, 2)
@@ -289,6 +298,10 @@ class LazyOpSum:
         return self.basis.dim()
 
     cols = rows
+
+    def set_kernel(self, kernel: int = 1, use_hash: bool = True, list_cap: int = 0) -> None:
+        """kernel 0: row per thread / warp per row; 1: bit-sliced 32-row tiles (default)."""
+        call("qsi_op_set_kernel", self._h, int(kernel), int(use_hash), int(list_cap))
 
     @staticmethod
     def _kind(a):

@@ -1,0 +1,343 @@
+// Bit-sliced tile kernels of the pull-gather apply, and the hash index.
+//
+// A warp owns a tile of 32 consecutive basis rows.  The tile's 32 states are
+// transposed with warp shuffles into one 32-bit word per spin (bit l = spin
+// of row l), so one lane evaluates one off-diagonal term for all 32 rows with
+// a few AND/XOR operations over that term's literals (the spins its
+// transposed up/down masks constrain).  A second transpose hands each row its
+// admitted terms as a bit set, visited in term order, so every row is summed
+// in the same fixed order as the one-row-per-thread kernel (deterministic,
+// bit-identical results).
+//
+// Single vector: each lane finds its own row's columns and gathers x.
+// Batched (R vectors, [row][R] layout): lanes first look up all columns of
+// the tile into a shared-memory hit list; then the warp walks the list row
+// by row and gathers each column's R values with coalesced loads.
+#include <algorithm>
+
+#include "qsi_device.cuh"
+#include "qsi_handles.h"
+
+namespace qsi {
+
+struct TileParams {
+    BasisView B;
+    const PullTerm* terms;
+    const uint16_t* lit_off;
+    const uint8_t* lits;
+    const PushTerm* dgen;
+    DiagSpec D;
+    int n_off, n_lits, nwords;
+};
+
+// Shared-memory layout common to both tile kernels.
+struct TileSmem {
+    PullTerm* terms;
+    PushTerm* dgen;
+    uint16_t* off;
+    uint8_t* lit;
+    unsigned char* tail;  // per-warp scratch follows
+};
+
+__device__ __forceinline__ TileSmem stage_terms(const TileParams& P, unsigned char* smem) {
+    TileSmem S;
+    S.terms = reinterpret_cast<PullTerm*>(smem);
+    S.dgen = reinterpret_cast<PushTerm*>(S.terms + P.n_off);
+    S.off = reinterpret_cast<uint16_t*>(S.dgen + P.D.n_generic);
+    S.lit = reinterpret_cast<uint8_t*>(S.off + P.n_off + 1);
+    size_t used = (size_t)P.n_off * sizeof(PullTerm) + (size_t)P.D.n_generic * sizeof(PushTerm) +
+                  (size_t)(P.n_off + 1) * 2 + (size_t)P.n_lits;
+    S.tail = smem + ((used + 15) & ~(size_t)15);
+    for (int k = threadIdx.x; k < P.n_off; k += blockDim.x) S.terms[k] = P.terms[k];
+    for (int k = threadIdx.x; k < P.D.n_generic; k += blockDim.x) S.dgen[k] = P.dgen[k];
+    for (int k = threadIdx.x; k <= P.n_off; k += blockDim.x) S.off[k] = P.lit_off[k];
+    for (int k = threadIdx.x; k < P.n_lits; k += blockDim.x) S.lit[k] = P.lits[k];
+    __syncthreads();
+    return S;
+}
+
+// Transposes the tile's states into per-spin words spinw[0 .. 32*nwords).
+__device__ __forceinline__ void tile_spin_words(const state2 s, int nwords, int lane, uint32_t* spinw) {
+    const uint32_t w[4] = {(uint32_t)s.x, (uint32_t)(s.x >> 32), (uint32_t)s.y, (uint32_t)(s.y >> 32)};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k < nwords) spinw[32 * k + lane] = warp_transpose32(w[k], lane);
+    __syncwarp();
+}
+
+// Admission bits of terms t0..t0+31 for this lane's row (bit j = term t0+j).
+__device__ __forceinline__ uint32_t tile_admitted(const TileSmem& S, int n_off, int t0, int lane, uint32_t vmask,
+                                                  const uint32_t* spinw) {
+    const int t = t0 + lane;
+    uint32_t A = 0;
+    if (t < n_off) {
+        A = vmask;
+        const int e = S.off[t + 1];
+        for (int k = S.off[t]; k < e; ++k) {
+            const uint8_t L = S.lit[k];
+            A &= spinw[L & 127] ^ ((L & 128) ? 0xFFFFFFFFu : 0u);
+        }
+    }
+    return warp_transpose32(A, lane);
+}
+
+__device__ __forceinline__ double term_coeff(const PullTerm& T, const state2 s) {
+    double cs = T.cs;
+    if (T.has_z && ((__popcll(~s.x & T.z0) + __popcll(~s.y & T.z1)) & 1)) cs = -cs;
+    return cs;
+}
+
+template <typename XT, typename YT, class LK>
+__global__ void __launch_bounds__(256) k_apply_tile(TileParams P, LK lk, const XT* __restrict__ x,
+                                                    YT* __restrict__ y, int accumulate) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const TileSmem S = stage_terms(P, smem_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t* spinw = reinterpret_cast<uint32_t*>(S.tail) + wid * 128;
+    const int64_t ntiles = (P.B.n + 31) >> 5;
+    for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
+        const int64_t row = tile * 32 + lane;
+        const bool valid = row < P.B.n;
+        const state2 s = valid ? P.B.states[row] : make_ulonglong2(0, 0);
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        tile_spin_words(s, P.nwords, lane, spinw);
+        double acc = valid ? diag_value(P.D, S.dgen, s.x, s.y) * (double)x[row] : 0.0;
+        for (int t0 = 0; t0 < P.n_off; t0 += 32) {
+            uint32_t hits = tile_admitted(S, P.n_off, t0, lane, vmask, spinw);
+            while (hits) {
+                const int j = __ffs(hits) - 1;
+                hits &= hits - 1;
+                const PullTerm& T = S.terms[t0 + j];
+                const int64_t J = lk.find(s.x ^ T.x0, s.y ^ T.x1);
+                if (J < 0) continue;
+                const double xj = (double)x[J];
+                if (fabs(xj) > 1e-15) acc += term_coeff(T, s) * xj;
+            }
+        }
+        if (valid) {
+            if (accumulate) acc += (double)y[row];
+            y[row] = (YT)acc;
+        }
+        __syncwarp();
+    }
+}
+
+template <typename XT, class LK>
+__global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
+                                                            XT* __restrict__ y, int R, int accumulate, int cap) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const TileSmem S = stage_terms(P, smem_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n_rounds = (P.n_off + 31) >> 5;
+    // per-warp scratch: spin words (128 u32), admission words (n_rounds*32 u32), hit list
+    unsigned char* mine = S.tail + (size_t)wid * (512 + (size_t)n_rounds * 128 + (size_t)cap * 12);
+    uint32_t* spinw = reinterpret_cast<uint32_t*>(mine);
+    uint32_t* adm = spinw + 128;
+    double* hc = reinterpret_cast<double*>(adm + n_rounds * 32);  // coefficients (8-byte aligned)
+    uint32_t* hJ = reinterpret_cast<uint32_t*>(hc + cap);
+    constexpr int KM = 4;  // up to 128 vectors per pass
+    const int64_t ntiles = (P.B.n + 31) >> 5;
+    for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
+        const int64_t row = tile * 32 + lane;
+        const bool valid = row < P.B.n;
+        const state2 s = valid ? P.B.states[row] : make_ulonglong2(0, 0);
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        tile_spin_words(s, P.nwords, lane, spinw);
+        int cnt = 0;
+        for (int r = 0; r < n_rounds; ++r) {
+            const uint32_t a = tile_admitted(S, P.n_off, r * 32, lane, vmask, spinw);
+            adm[r * 32 + lane] = a;
+            cnt += __popc(a);
+        }
+        const double d = valid ? diag_value(P.D, S.dgen, s.x, s.y) : 0.0;
+        int row_start = 0;
+        while (row_start < 32) {
+            // rows [row_start, row_end) whose hits fit the list (at least one row; cap >= n_off)
+            int c = (lane >= row_start) ? cnt : 0;
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const bool in_chunk = lane >= row_start && (incl <= cap || lane == row_start);
+            const uint32_t cm = __ballot_sync(0xffffffffu, in_chunk);
+            const int row_end = 32 - __clz(cm);
+            int base = incl - c;
+            if (in_chunk) {
+                int k = base;
+                for (int r = 0; r < n_rounds; ++r) {
+                    uint32_t a = adm[r * 32 + lane];
+                    while (a) {
+                        const int j = __ffs(a) - 1;
+                        a &= a - 1;
+                        const PullTerm& T = S.terms[r * 32 + j];
+                        const int64_t J = lk.find(s.x ^ T.x0, s.y ^ T.x1);
+                        hJ[k] = (J < 0) ? kEmpty : (uint32_t)J;
+                        hc[k] = term_coeff(T, s);
+                        ++k;
+                    }
+                }
+            }
+            __syncwarp();
+            for (int l = row_start; l < row_end; ++l) {
+                const int b0 = __shfl_sync(0xffffffffu, base, l);
+                const int nl = __shfl_sync(0xffffffffu, cnt, l);
+                const double dl = __shfl_sync(0xffffffffu, d, l);
+                const int64_t rl = tile * 32 + l;
+                if (rl >= P.B.n) break;
+                for (int r0 = 0; r0 < R; r0 += 32 * KM) {
+                    double acc[KM];
+#pragma unroll
+                    for (int m = 0; m < KM; ++m) {
+                        const int rr = r0 + lane + 32 * m;
+                        acc[m] = (rr < R) ? dl * (double)x[rl * R + rr] : 0.0;
+                    }
+                    for (int k = b0; k < b0 + nl; ++k) {
+                        const uint32_t J = hJ[k];
+                        if (J == kEmpty) continue;
+                        const double ck = hc[k];
+                        const XT* xr = x + (int64_t)J * R;
+#pragma unroll
+                        for (int m = 0; m < KM; ++m) {
+                            const int rr = r0 + lane + 32 * m;
+                            if (rr < R) {
+                                const double xj = (double)xr[rr];
+                                if (fabs(xj) > 1e-15) acc[m] += ck * xj;
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int m = 0; m < KM; ++m) {
+                        const int rr = r0 + lane + 32 * m;
+                        if (rr < R) {
+                            double v = acc[m];
+                            if (accumulate) v += (double)y[rl * R + rr];
+                            y[rl * R + rr] = (XT)v;
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            row_start = row_end;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ hash index build
+__global__ void k_hash_clear(HashSlot* slots, uint64_t n_slots) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_slots; i += (uint64_t)gridDim.x * blockDim.x) {
+        slots[i].lo = 0;
+        slots[i].hi = 0;
+        slots[i].idx = kEmpty;
+    }
+}
+
+__global__ void k_hash_insert(const state2* __restrict__ states, int64_t n, HashSlot* slots, uint64_t mask,
+                              int* overflow) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const state2 s = states[i];
+        uint64_t p = state_mix(s.x, s.y) & mask;
+        bool done = false;
+        for (uint64_t probe = 0; probe <= mask; ++probe) {
+            if (atomicCAS(&slots[p].idx, kEmpty, (uint32_t)i) == kEmpty) {
+                slots[p].lo = s.x;
+                slots[p].hi = (uint32_t)s.y;
+                done = true;
+                break;
+            }
+            p = (p + 1) & mask;
+        }
+        if (!done) atomicOr(overflow, 1);
+    }
+}
+
+qsi_status build_hash(qsi_basis* b) {
+    if (b->hb >= 96) return fail(QSI_INVALID_ARG, "hash index needs states of at most 96 bits");
+    uint64_t cap = 1;
+    while (cap < (uint64_t)b->n * 2) cap <<= 1;
+    if (cap < 1024) cap = 1024;
+    if (b->d_hash) cudaFree(b->d_hash);
+    b->d_hash = nullptr;
+    QSI_CUDA(cudaMalloc(&b->d_hash, cap * sizeof(HashSlot)));
+    b->hash_mask = cap - 1;
+    int* d_over = nullptr;
+    QSI_CUDA(cudaMalloc(&d_over, sizeof(int)));
+    QSI_CUDA(cudaMemset(d_over, 0, sizeof(int)));
+    k_hash_clear<<<grid_for((int64_t)cap, 256), 256>>>(b->d_hash, cap);
+    k_hash_insert<<<grid_for(b->n, 256), 256>>>(b->d_states, b->n, b->d_hash, b->hash_mask, d_over);
+    int over = 0;
+    cudaError_t e = cudaMemcpy(&over, d_over, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_over);
+    if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "hash build: %s", cudaGetErrorString(e));
+    if (over) return fail(QSI_CUDA_ERROR, "hash build: table overflow");
+    return QSI_OK;
+}
+
+// ------------------------------------------------------------------ launchers
+static size_t term_smem(const qsi_op* op) {
+    size_t used = (size_t)op->n_pull * sizeof(PullTerm) + (size_t)op->n_diag_generic * sizeof(PushTerm) +
+                  (size_t)(op->n_pull + 1) * 2 + (size_t)op->n_lits;
+    return (used + 15) & ~(size_t)15;
+}
+
+template <class K>
+static void set_smem(K kernel, size_t smem) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <class LK>
+static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int R, int xdtype, int ydtype,
+                                  int accumulate, cudaStream_t st) {
+    TileParams P{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
+                 op->n_pull, op->n_lits, op->nwords};
+    const int block = 256, nw = block / 32;
+    const int64_t ntiles = (P.B.n + 31) / 32;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (R == 1) {
+        const size_t smem = term_smem(op) + (size_t)nw * 512;
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
+        if (xdtype == QSI_F64) {
+            auto k = k_apply_tile<double, double, LK>;
+            set_smem(k, smem);
+            k<<<grid, block, smem, st>>>(P, lk, (const double*)x, (double*)y, accumulate);
+        } else if (ydtype == QSI_F64) {
+            auto k = k_apply_tile<float, double, LK>;
+            set_smem(k, smem);
+            k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (double*)y, accumulate);
+        } else {
+            auto k = k_apply_tile<float, float, LK>;
+            set_smem(k, smem);
+            k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, accumulate);
+        }
+    } else {
+        const int cap = (std::max(op->list_cap, op->n_pull) + 7) & ~7;
+        const int n_rounds = (op->n_pull + 31) / 32;
+        const size_t per_warp = 512 + (size_t)n_rounds * 128 + (size_t)cap * 12;
+        const size_t smem = term_smem(op) + (size_t)nw * per_warp;
+        if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "batched apply: %zu bytes of shared memory needed", smem);
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
+        if (xdtype == QSI_F64) {
+            auto k = k_apply_tile_batched<double, LK>;
+            set_smem(k, smem);
+            k<<<grid, block, smem, st>>>(P, lk, (const double*)x, (double*)y, R, accumulate, cap);
+        } else {
+            auto k = k_apply_tile_batched<float, LK>;
+            set_smem(k, smem);
+            k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
+        }
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "tile apply launch: %s", cudaGetErrorString(e));
+    return QSI_OK;
+}
+
+qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
+                              cudaStream_t st) {
+    if (op->basis->d_hash && op->use_hash) return launch_tiles_lk(op, LookupHash{op->basis->hview()}, x, y, R, xdtype, ydtype, accumulate, st);
+    return launch_tiles_lk(op, LookupTable{op->basis->view()}, x, y, R, xdtype, ydtype, accumulate, st);
+}
+
+}  // namespace qsi

@@ -256,6 +256,7 @@ extern "C" qsi_status qsi_basis_create(const uint64_t* lohi, int64_t n, int32_t 
         }
         bits = std::min(bits, std::min(30, hb + 1));
         b->bits = bits;
+        b->hb = hb;
         b->shift = hb + 1 - bits;
         b->n_buckets = 1u << bits;
         cudaError_t e = cudaMalloc(&b->d_states, (size_t)n * sizeof(state2));
@@ -281,6 +282,14 @@ extern "C" qsi_status qsi_basis_create(const uint64_t* lohi, int64_t n, int32_t 
         if (cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
             return cleanup(fail(QSI_CUDA_ERROR, "qsi_basis_create: %s", cudaGetErrorString(cudaGetLastError())));
         if (bad) return cleanup(fail(QSI_INVALID_ARG, "qsi_basis_create: basis states are not strictly increasing"));
+        // hash index for states of at most 96 bits (skipped, not fatal, when it does not fit in memory)
+        if (hb < 96) {
+            if (build_hash(b) != QSI_OK) {
+                if (b->d_hash) cudaFree(b->d_hash);
+                b->d_hash = nullptr;
+                cudaGetLastError();
+            }
+        }
         *out = b;
         return cleanup(QSI_OK);
     });
@@ -290,6 +299,7 @@ extern "C" qsi_status qsi_basis_destroy(qsi_basis* b) {
     if (!b) return QSI_OK;
     if (b->d_states) cudaFree(b->d_states);
     if (b->d_bstart) cudaFree(b->d_bstart);
+    if (b->d_hash) cudaFree(b->d_hash);
     delete b;
     return QSI_OK;
 }
@@ -438,6 +448,34 @@ extern "C" qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t
             return fail(QSI_INVALID_ARG, "qsi_op_create: %zu terms exceed the shared-memory term table", pull.size());
         }
         op->smem_bytes = smem;
+        // literal lists for the bit-sliced admission test
+        std::vector<uint16_t> lit_off{0};
+        std::vector<uint8_t> lits;
+        int maxbit = b->hb;
+        for (const PullTerm& t : pull) {
+            const uint64_t um[2] = {t.up0, t.up1}, dm[2] = {t.dn0, t.dn1}, xm[2] = {t.x0, t.x1};
+            for (int w = 0; w < 2; ++w) {
+                for (int bit = 0; bit < 64; ++bit) {
+                    if ((um[w] >> bit) & 1) lits.push_back((uint8_t)(64 * w + bit));
+                    if ((dm[w] >> bit) & 1) lits.push_back((uint8_t)(0x80 | (64 * w + bit)));
+                    if (((um[w] | dm[w] | xm[w]) >> bit) & 1) maxbit = std::max(maxbit, 64 * w + bit);
+                }
+            }
+            if (lits.size() > 65535) {
+                qsi_op_destroy(op);
+                return fail(QSI_INVALID_ARG, "qsi_op_create: more than 65535 literals in the term list");
+            }
+            lit_off.push_back((uint16_t)lits.size());
+        }
+        op->n_lits = (int)lits.size();
+        op->nwords = maxbit / 32 + 1;
+        if (lits.empty()) lits.push_back(0);
+        e = upload((void**)&op->d_lit_off, lit_off.data(), lit_off.size() * 2);
+        if (e == cudaSuccess) e = upload((void**)&op->d_lits, lits.data(), lits.size());
+        if (e != cudaSuccess) {
+            qsi_op_destroy(op);
+            return fail(e == cudaErrorMemoryAllocation ? QSI_OOM : QSI_CUDA_ERROR, "qsi_op_create: %s", cudaGetErrorString(e));
+        }
         *out = op;
         return QSI_OK;
     });
@@ -450,6 +488,8 @@ extern "C" qsi_status qsi_op_destroy(qsi_op* op) {
     cudaFree(op->d_push_off);
     cudaFree(op->d_push_diag);
     cudaFree(op->d_diag_generic);
+    cudaFree(op->d_lit_off);
+    cudaFree(op->d_lits);
     cudaFree(op->d_x);
     cudaFree(op->d_y);
     if (op->stream) cudaStreamDestroy(op->stream);
@@ -461,6 +501,7 @@ namespace qsi {
 
 // Enqueues y (+)= H x on `st` for device pointers.
 qsi_status launch_apply(qsi_op* op, const void* x, void* y, int R, int dtype, int accumulate, cudaStream_t st) {
+    if (op->kernel == 1) return launch_apply_tiles(op, x, y, R, dtype, dtype, accumulate, st);
     BasisView V = op->basis->view();
     const int block = 256;
     const size_t smem = op->smem_bytes;
@@ -498,6 +539,7 @@ qsi_status launch_apply(qsi_op* op, const void* x, void* y, int R, int dtype, in
 
 qsi_status launch_apply_to_f64(qsi_op* op, const void* x, double* y, int xdtype, cudaStream_t st) {
     if (xdtype == QSI_F64) return launch_apply(op, x, y, 1, QSI_F64, 0, st);
+    if (op->kernel == 1) return launch_apply_tiles(op, x, y, 1, xdtype, QSI_F64, 0, st);
     BasisView V = op->basis->view();
     const size_t smem = op->smem_bytes;
     auto k = k_apply_rowthread<float, double>;
@@ -619,4 +661,45 @@ extern "C" qsi_status qsi_op_connectivity(qsi_op* op, int64_t* hits, int64_t* mi
 extern "C" qsi_status qsi_op_count_misses(qsi_op* op, int64_t* misses) {
     if (!misses) return fail(QSI_INVALID_ARG, "qsi_op_count_misses: null argument");
     return qsi_op_connectivity(op, nullptr, misses);
+}
+
+extern "C" qsi_status qsi_basis_index(qsi_basis* b, int32_t use_hash, int32_t bucket_bits) {
+    return guarded([&]() -> qsi_status {
+        if (!b) return fail(QSI_INVALID_ARG, "qsi_basis_index: null basis");
+        if (bucket_bits > 0 && bucket_bits != b->bits) {
+            int bits = std::min<int>(bucket_bits, std::min(30, b->hb + 1));
+            uint32_t* nb = nullptr;
+            QSI_CUDA(cudaMalloc(&nb, ((size_t)(1u << bits) + 1) * sizeof(uint32_t)));
+            cudaFree(b->d_bstart);
+            b->d_bstart = nb;
+            b->bits = bits;
+            b->shift = b->hb + 1 - bits;
+            b->n_buckets = 1u << bits;
+            k_fill_buckets<<<grid_for(b->n + 1, 256), 256>>>(b->view(), b->d_bstart);
+            QSI_CUDA(cudaDeviceSynchronize());
+        }
+        if (use_hash && !b->d_hash) return build_hash(b);
+        if (!use_hash && b->d_hash) {
+            cudaFree(b->d_hash);
+            b->d_hash = nullptr;
+        }
+        return QSI_OK;
+    });
+}
+
+extern "C" qsi_status qsi_basis_info(const qsi_basis* b, int32_t* bucket_bits, int32_t* has_hash, int64_t* index_bytes) {
+    if (!b) return fail(QSI_INVALID_ARG, "qsi_basis_info: null basis");
+    if (bucket_bits) *bucket_bits = b->bits;
+    if (has_hash) *has_hash = b->d_hash != nullptr;
+    if (index_bytes)
+        *index_bytes = (int64_t)(((size_t)b->n_buckets + 1) * 4 + (b->d_hash ? (b->hash_mask + 1) * sizeof(HashSlot) : 0));
+    return QSI_OK;
+}
+
+extern "C" qsi_status qsi_op_set_kernel(qsi_op* op, int32_t kernel, int32_t use_hash, int32_t list_cap) {
+    if (!op || kernel < 0 || kernel > 1 || list_cap < 0) return fail(QSI_INVALID_ARG, "qsi_op_set_kernel: bad argument");
+    op->kernel = kernel;
+    op->use_hash = use_hash;
+    if (list_cap > 0) op->list_cap = list_cap;
+    return QSI_OK;
 }

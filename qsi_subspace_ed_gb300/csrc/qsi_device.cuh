@@ -53,6 +53,29 @@ struct BasisView {
     uint32_t n_buckets;
 };
 
+// Open-addressing index of the basis (states of at most 96 bits): slot =
+// {low word, high 32 bits, position in the sorted basis}; idx == kEmpty marks a
+// free slot.  Linear probing from mix(state); built once per basis.
+struct HashSlot {
+    uint64_t lo;
+    uint32_t hi;
+    uint32_t idx;
+};
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+
+__host__ __device__ __forceinline__ uint64_t state_mix(uint64_t lo, uint64_t hi) {
+    uint64_t h = lo * 0x9E3779B97F4A7C15ULL ^ (hi + 0x632BE59BD9B4E019ULL) * 0xC2B2AE3D27D4EB4FULL;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ULL;
+    h ^= h >> 29;
+    return h;
+}
+
+struct HashView {
+    const HashSlot* slots;
+    uint64_t mask;
+};
+
 __device__ __forceinline__ bool less128(uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi) {
     return ahi < bhi || (ahi == bhi && alo < blo);
 }
@@ -89,6 +112,45 @@ __device__ __forceinline__ int64_t basis_find(const BasisView& B, uint64_t lo, u
         if (e.x == lo && e.y == hi) return (int64_t)a;
     }
     return -1;
+}
+
+// Exact position of (lo, hi) through the hash index, or -1.  The probe count
+// is bounded by the table size (the table always has free slots).
+__device__ __forceinline__ int64_t hash_find(const HashView& Hv, uint64_t lo, uint64_t hi) {
+    if (hi >> 32) return -1;
+    uint64_t s = state_mix(lo, hi) & Hv.mask;
+    for (uint64_t probe = 0; probe <= Hv.mask; ++probe) {
+        const uint4 e = __ldg(reinterpret_cast<const uint4*>(Hv.slots + s));
+        if (e.w == kEmpty) return -1;
+        if (e.x == (uint32_t)lo && e.y == (uint32_t)(lo >> 32) && e.z == (uint32_t)hi) return (int64_t)e.w;
+        s = (s + 1) & Hv.mask;
+    }
+    return -1;
+}
+
+struct LookupTable {
+    BasisView B;
+    __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return basis_find(B, lo, hi); }
+};
+
+struct LookupHash {
+    HashView H;
+    __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return hash_find(H, lo, hi); }
+};
+
+// 32x32 bit-matrix transpose across a warp: lane r holds row r (bit c = [r][c]);
+// on return lane r holds column r (bit c = [c][r]).  Five shuffle stages,
+// each swapping the off-diagonal j x j blocks.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t w, int lane) {
+    const uint32_t m0[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const int j = 16 >> k;
+        const uint32_t m = m0[k];
+        const uint32_t x = __shfl_xor_sync(0xffffffffu, w, j);
+        w = (lane & j) ? ((w & ~m) | ((x & ~m) >> j)) : ((w & m) | ((x & m) << j));
+    }
+    return w;
 }
 
 __device__ __forceinline__ double diag_value(const DiagSpec& D, const PushTerm* gen, uint64_t s0, uint64_t s1) {

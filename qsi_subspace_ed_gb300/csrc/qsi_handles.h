@@ -11,7 +11,11 @@ struct qsi_basis {
     uint32_t n_buckets = 0;
     qsi::state2* d_states = nullptr;
     uint32_t* d_bstart = nullptr;
+    int hb = 0;                        // highest bit used by any state
+    qsi::HashSlot* d_hash = nullptr;   // optional hash index (states <= 96 bits)
+    uint64_t hash_mask = 0;
     qsi::BasisView view() const { return qsi::BasisView{d_states, d_bstart, n, shift, n_buckets}; }
+    qsi::HashView hview() const { return qsi::HashView{d_hash, hash_mask}; }
 };
 
 struct qsi_op {
@@ -23,6 +27,14 @@ struct qsi_op {
     int n_pull = 0, n_push_off = 0, n_push_diag = 0, n_diag_generic = 0;
     qsi::DiagSpec diag{};
     size_t smem_bytes = 0;
+    // bit-sliced admission tests: per pull term, literals (spin | 0x80 when the spin must be down)
+    uint16_t* d_lit_off = nullptr;  // n_pull + 1 offsets
+    uint8_t* d_lits = nullptr;
+    int n_lits = 0;
+    int nwords = 4;                 // 32-bit words that hold any basis or term bit
+    int kernel = 1;                 // 0 = row-per-thread / warp-per-row, 1 = bit-sliced tiles
+    int list_cap = 512;             // hit-list entries per warp in the batched tile kernel
+    int use_hash = 1;               // look columns up through the basis hash index when it exists
     cudaStream_t stream = nullptr;
     void* d_x = nullptr;   // staging for host-pointer applies
     void* d_y = nullptr;
@@ -34,5 +46,8 @@ int grid_for(int64_t n, int block);
 qsi_status launch_apply(qsi_op* op, const void* x, void* y, int R, int dtype, int accumulate, cudaStream_t st);
 // y = H x with x stored as xdtype and y always FP64 (single vector).
 qsi_status launch_apply_to_f64(qsi_op* op, const void* x, double* y, int xdtype, cudaStream_t st);
+qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
+                              cudaStream_t st);
+qsi_status build_hash(qsi_basis* b);
 qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vector<double>& w, std::vector<double>& V, cudaStream_t st);
 }  // namespace qsi

@@ -144,3 +144,50 @@ def test_basis_errors():
         q.ZBasis(np.array([[5, 0], [3, 0]], np.uint64))  # not increasing
     with pytest.raises(q.QsiError):
         q.ZBasis(np.zeros((0, 2), np.uint64))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_kernel_variants_bit_identical(built, name):
+    """Row-per-thread, bit-sliced tiles, table and hash lookups: same sums in the same order."""
+    basis, H, b, op = built[name]
+    x = np.random.default_rng(11).standard_normal(len(basis))
+    X = np.random.default_rng(12).standard_normal((len(basis), 40))
+    outs, bouts = [], []
+    for kernel, use_hash in [(0, 0), (1, 0), (1, 1), (0, 1)]:
+        op.set_kernel(kernel, use_hash)
+        y = np.zeros_like(x)
+        op.evaluate(x, y)
+        outs.append(y)
+        Y = np.zeros_like(X)
+        op.apply_batched(X, Y)
+        bouts.append(Y)
+    op.set_kernel(1, 1)
+    for y in outs[1:]:
+        assert np.array_equal(y, outs[0])
+    for Y in bouts[1:]:
+        assert np.array_equal(Y, bouts[0])
+
+
+def test_hash_index_and_table_sizes(built):
+    basis, H, b, op = built["golden48_JpmB"]
+    info = b.index_info()
+    assert info["hash"]
+    for bits in (8, 12, 20):
+        b.set_index(use_hash=False, bucket_bits=bits)
+        assert b.index_info()["bucket_bits"] == bits and not b.index_info()["hash"]
+        assert np.array_equal(b.search(basis[::97]), np.arange(0, len(basis), 97))
+    b.set_index(use_hash=True, bucket_bits=0)
+    assert b.index_info()["hash"]
+
+
+def test_batched_hit_list_overflow_chunks(built):
+    """A small hit list forces the batched tile kernel to split tiles into row chunks."""
+    basis, H, b, op = built["golden48_JpmB"]
+    X = np.random.default_rng(5).standard_normal((len(basis), 8))
+    Y1, Y2 = np.zeros_like(X), np.zeros_like(X)
+    op.set_kernel(1, 1, list_cap=512)
+    op.apply_batched(X, Y1)
+    op.set_kernel(1, 1, list_cap=8)  # raised to the term count internally
+    op.apply_batched(X, Y2)
+    op.set_kernel(1, 1, list_cap=512)
+    assert np.array_equal(Y1, Y2)

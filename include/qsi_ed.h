@@ -118,6 +118,14 @@ qsi_status qsi_enumerate_basis(int32_t n_spins, const int32_t* tetra_spins,
                                int32_t ordering, int32_t n_threads,
                                uint64_t** out_lohi, int64_t* n_out);
 void qsi_free_host(void* p);
+/* The same enumeration on the GPU for bases without spinon pairs (ordering is
+ * the greedy order; states of at most 128 spins, at most 128 tetrahedra and
+ * 8 sublattices).  The sorted result is returned in host memory
+ * (release with qsi_free_host). */
+qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* tetra_spins,
+                                   int32_t n_tetra, int32_t tetra_size,
+                                   const int32_t* sublattice, int32_t n_sublattices,
+                                   const int32_t* sector, uint64_t** out_lohi, int64_t* n_out);
 
 /* ---------------------------------------------------------------- device basis */
 /* Copies a sorted basis to the device and builds its top-bits bucket table.
@@ -158,7 +166,10 @@ qsi_status qsi_op_apply_batched(qsi_op* op, const void* X, void* Y, int32_t R,
                                 void* stream);
 /* Kernel selection (autotuning): kernel 0 = one row per thread (single
  * vector) / one warp per row (batched); kernel 1 = bit-sliced 32-row tiles
- * (default).  use_hash selects the hash index for column lookups;
+ * (default).  use_hash bit 0 selects the hash index for column lookups; bit 1
+ * makes FP32 batched applies accumulate rows in FP64 instead of double-float
+ * (two FP32 words, about 2^-48 relative; the default, since FP64 issue is
+ * slow on this GPU);
  * list_cap (> 0) sets the per-warp hit-list size of the batched tile kernel. */
 qsi_status qsi_op_set_kernel(qsi_op* op, int32_t kernel, int32_t use_hash, int32_t list_cap);
 /* Connectivity export in the order of LazyOpSum::toSparseMatrix

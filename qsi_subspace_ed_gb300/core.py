@@ -227,6 +227,25 @@ def enumerate_basis(lattice, n_spinon_pairs: int = 0, sector=None, ordering: str
     return a
 
 
+def enumerate_basis_gpu(lattice, sector=None) -> np.ndarray:
+    """Sorted spin-ice basis without spinon pairs, enumerated on the GPU (same set as enumerate_basis)."""
+    from .lattice import Lattice
+
+    L = lattice if isinstance(lattice, Lattice) else Lattice.load(lattice)
+    tets = np.ascontiguousarray(L.tetrahedra, dtype=np.int32)
+    sl = np.ascontiguousarray(L.sublattice, dtype=np.int32)
+    sec = None if sector is None else np.ascontiguousarray(sector, dtype=np.int32)
+    out = C.POINTER(C.c_uint64)()
+    n = C.c_int64()
+    call("qsi_enumerate_basis_gpu", L.n_spins, ptr(tets), tets.shape[0], tets.shape[1], ptr(sl), int(sl.max()) + 1,
+         ptr(sec) if sec is not None else None, C.byref(out), C.byref(n))
+    try:
+        a = np.ctypeslib.as_array(out, shape=(max(1, n.value) * 2,))[: n.value * 2].reshape(-1, 2).copy()
+    finally:
+        _lib.load().qsi_free_host(C.cast(out, C.c_void_p))
+    return a
+
+
 class ZBasis:
     """Sorted 128-bit basis resident on the GPU with its bucket table."""
 

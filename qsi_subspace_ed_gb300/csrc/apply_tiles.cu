@@ -27,8 +27,39 @@ struct TileParams {
     const uint8_t* lits;
     const PushTerm* dgen;
     DiagSpec D;
+    const double* diag;  // per-row diagonal, precomputed with diag_value
     int n_off, n_lits, nwords;
 };
+
+// |x| > 1e-15 (APPLY_TOL, operator_matrix.hpp:113) as integer compares on the
+// bit pattern: magnitude above the threshold and not a NaN.  For FP32 x the
+// threshold is the largest float whose value is <= 1e-15, so the test equals
+// fabs((double)x) > 1e-15 exactly.
+constexpr uint64_t kTolBitsF64 = 0x3CD203AF9EE75616ULL;  // 1e-15
+constexpr uint32_t kTolBitsF32 = 0x26901D7CU;            // largest float <= 1e-15
+__device__ __forceinline__ bool above_tol(double v) {
+    const uint64_t m = (uint64_t)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+    return m > kTolBitsF64 && m <= 0x7FF0000000000000ULL;
+}
+__device__ __forceinline__ bool above_tol(float v) {
+    const uint32_t m = __float_as_uint(v) & 0x7FFFFFFFu;
+    return m > kTolBitsF32 && m <= 0x7F800000u;
+}
+
+// Double-float accumulator (hi + lo, two FP32 words, ~2^-48 relative):
+// error-free product c*x with c = ch + cl and error-free sum into hi.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ void ff_fma(FF& a, float ch, float cl, float x) {
+    const float p = ch * x;
+    const float e = fmaf(ch, x, -p) + cl * x;
+    const float s = a.hi + p;
+    const float bb = s - a.hi;
+    const float err = (a.hi - (s - bb)) + (p - bb);
+    a.hi = s;
+    a.lo += err + e;
+}
 
 // Shared-memory layout common to both tile kernels.
 struct TileSmem {
@@ -101,7 +132,7 @@ __global__ void __launch_bounds__(256) k_apply_tile(TileParams P, LK lk, const X
         const state2 s = valid ? P.B.states[row] : make_ulonglong2(0, 0);
         const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
         tile_spin_words(s, P.nwords, lane, spinw);
-        double acc = valid ? diag_value(P.D, S.dgen, s.x, s.y) * (double)x[row] : 0.0;
+        double acc = valid ? P.diag[row] * (double)x[row] : 0.0;
         for (int t0 = 0; t0 < P.n_off; t0 += 32) {
             uint32_t hits = tile_admitted(S, P.n_off, t0, lane, vmask, spinw);
             while (hits) {
@@ -110,8 +141,8 @@ __global__ void __launch_bounds__(256) k_apply_tile(TileParams P, LK lk, const X
                 const PullTerm& T = S.terms[t0 + j];
                 const int64_t J = lk.find(s.x ^ T.x0, s.y ^ T.x1);
                 if (J < 0) continue;
-                const double xj = (double)x[J];
-                if (fabs(xj) > 1e-15) acc += term_coeff(T, s) * xj;
+                const XT xj = x[J];
+                if (above_tol(xj)) acc += term_coeff(T, s) * (double)xj;
             }
         }
         if (valid) {
@@ -122,7 +153,7 @@ __global__ void __launch_bounds__(256) k_apply_tile(TileParams P, LK lk, const X
     }
 }
 
-template <typename XT, class LK>
+template <typename XT, class LK, bool kFF>
 __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
                                                             XT* __restrict__ y, int R, int accumulate, int cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -134,6 +165,7 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
     uint32_t* spinw = reinterpret_cast<uint32_t*>(mine);
     uint32_t* adm = spinw + 128;
     double* hc = reinterpret_cast<double*>(adm + n_rounds * 32);  // coefficients (8-byte aligned)
+    float2* hcf = reinterpret_cast<float2*>(hc);                   // the same slots as (hi, lo) floats
     uint32_t* hJ = reinterpret_cast<uint32_t*>(hc + cap);
     constexpr int KM = 4;  // up to 128 vectors per pass
     const int64_t ntiles = (P.B.n + 31) >> 5;
@@ -149,7 +181,7 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
             adm[r * 32 + lane] = a;
             cnt += __popc(a);
         }
-        const double d = valid ? diag_value(P.D, S.dgen, s.x, s.y) : 0.0;
+        const double d = valid ? P.diag[row] : 0.0;
         int row_start = 0;
         while (row_start < 32) {
             // rows [row_start, row_end) whose hits fit the list (at least one row; cap >= n_off)
@@ -174,7 +206,13 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                         const PullTerm& T = S.terms[r * 32 + j];
                         const int64_t J = lk.find(s.x ^ T.x0, s.y ^ T.x1);
                         hJ[k] = (J < 0) ? kEmpty : (uint32_t)J;
-                        hc[k] = term_coeff(T, s);
+                        const double cf = term_coeff(T, s);
+                        if constexpr (kFF) {
+                            const float ch = (float)cf;
+                            hcf[k] = make_float2(ch, (float)(cf - (double)ch));
+                        } else {
+                            hc[k] = cf;
+                        }
                         ++k;
                     }
                 }
@@ -187,33 +225,67 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                 const int64_t rl = tile * 32 + l;
                 if (rl >= P.B.n) break;
                 for (int r0 = 0; r0 < R; r0 += 32 * KM) {
-                    double acc[KM];
+                    if constexpr (kFF) {
+                        // FP32 storage, double-float row accumulation (no FP64 instructions)
+                        FF acc[KM];
+                        const float dh = (float)dl, dlo = (float)(dl - (double)dh);
 #pragma unroll
-                    for (int m = 0; m < KM; ++m) {
-                        const int rr = r0 + lane + 32 * m;
-                        acc[m] = (rr < R) ? dl * (double)x[rl * R + rr] : 0.0;
-                    }
-                    for (int k = b0; k < b0 + nl; ++k) {
-                        const uint32_t J = hJ[k];
-                        if (J == kEmpty) continue;
-                        const double ck = hc[k];
-                        const XT* xr = x + (int64_t)J * R;
+                        for (int m = 0; m < KM; ++m) {
+                            const int rr = r0 + lane + 32 * m;
+                            acc[m] = FF{0.f, 0.f};
+                            if (rr < R) ff_fma(acc[m], dh, dlo, (float)x[rl * R + rr]);
+                        }
+                        for (int k = b0; k < b0 + nl; ++k) {
+                            const uint32_t J = hJ[k];
+                            if (J == kEmpty) continue;
+                            const float2 ck = hcf[k];
+                            const XT* xr = x + (int64_t)J * R;
+#pragma unroll
+                            for (int m = 0; m < KM; ++m) {
+                                const int rr = r0 + lane + 32 * m;
+                                if (rr < R) {
+                                    const float xj = (float)xr[rr];
+                                    if (above_tol(xj)) ff_fma(acc[m], ck.x, ck.y, xj);
+                                }
+                            }
+                        }
 #pragma unroll
                         for (int m = 0; m < KM; ++m) {
                             const int rr = r0 + lane + 32 * m;
                             if (rr < R) {
-                                const double xj = (double)xr[rr];
-                                if (fabs(xj) > 1e-15) acc[m] += ck * xj;
+                                if (accumulate) ff_fma(acc[m], 1.0f, 0.0f, (float)y[rl * R + rr]);
+                                y[rl * R + rr] = (XT)(acc[m].hi + acc[m].lo);
                             }
                         }
-                    }
+                    } else {
+                        double acc[KM];
 #pragma unroll
-                    for (int m = 0; m < KM; ++m) {
-                        const int rr = r0 + lane + 32 * m;
-                        if (rr < R) {
-                            double v = acc[m];
-                            if (accumulate) v += (double)y[rl * R + rr];
-                            y[rl * R + rr] = (XT)v;
+                        for (int m = 0; m < KM; ++m) {
+                            const int rr = r0 + lane + 32 * m;
+                            acc[m] = (rr < R) ? dl * (double)x[rl * R + rr] : 0.0;
+                        }
+                        for (int k = b0; k < b0 + nl; ++k) {
+                            const uint32_t J = hJ[k];
+                            if (J == kEmpty) continue;
+                            const double ck = hc[k];
+                            const XT* xr = x + (int64_t)J * R;
+#pragma unroll
+                            for (int m = 0; m < KM; ++m) {
+                                const int rr = r0 + lane + 32 * m;
+                                if (rr < R) {
+                                    const XT xj = xr[rr];
+                                    if (above_tol(xj)) acc[m] += ck * (double)xj;
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int m = 0; m < KM; ++m) {
+                            const int rr = r0 + lane + 32 * m;
+                            if (rr < R) {
+                                double v = acc[m];
+                                if (accumulate) v += (double)y[rl * R + rr];
+                                y[rl * R + rr] = (XT)v;
+                            }
                         }
                     }
                 }
@@ -222,6 +294,23 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
             row_start = row_end;
         }
     }
+}
+
+// Per-row diagonal, evaluated once per operator with the same arithmetic as
+// diag_value in the row kernels.
+__global__ void k_diag_precompute(BasisView B, DiagSpec D, const PushTerm* __restrict__ dgen, double* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < B.n; i += (int64_t)gridDim.x * blockDim.x) {
+        const state2 s = B.states[i];
+        out[i] = diag_value(D, dgen, s.x, s.y);
+    }
+}
+
+qsi_status build_diag(qsi_op* op) {
+    QSI_CUDA(cudaMalloc(&op->d_diag, (size_t)op->basis->n * sizeof(double)));
+    k_diag_precompute<<<grid_for(op->basis->n, 256), 256>>>(op->basis->view(), op->diag, op->d_diag_generic, op->d_diag);
+    QSI_CUDA(cudaGetLastError());
+    QSI_CUDA(cudaDeviceSynchronize());
+    return QSI_OK;
 }
 
 // ------------------------------------------------------------------ hash index build
@@ -290,7 +379,7 @@ template <class LK>
 static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int R, int xdtype, int ydtype,
                                   int accumulate, cudaStream_t st) {
     TileParams P{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
-                 op->n_pull, op->n_lits, op->nwords};
+                 op->d_diag, op->n_pull, op->n_lits, op->nwords};
     const int block = 256, nw = block / 32;
     const int64_t ntiles = (P.B.n + 31) / 32;
     int dev = 0, sms = 148;
@@ -320,11 +409,15 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
         if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "batched apply: %zu bytes of shared memory needed", smem);
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
         if (xdtype == QSI_F64) {
-            auto k = k_apply_tile_batched<double, LK>;
+            auto k = k_apply_tile_batched<double, LK, false>;
             set_smem(k, smem);
             k<<<grid, block, smem, st>>>(P, lk, (const double*)x, (double*)y, R, accumulate, cap);
+        } else if (op->ff_accumulate) {
+            auto k = k_apply_tile_batched<float, LK, true>;
+            set_smem(k, smem);
+            k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
         } else {
-            auto k = k_apply_tile_batched<float, LK>;
+            auto k = k_apply_tile_batched<float, LK, false>;
             set_smem(k, smem);
             k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
         }

@@ -1,0 +1,381 @@
+// Spin-ice basis enumeration on the GPU (bases without spinon pairs).
+//
+// The host walks the search tree (same visiting order and admission tests as
+// enumerate.cpp's fast search) down to a prefix depth with enough subtree
+// roots to fill the GPU; then every root is searched to the leaves by one
+// GPU thread with an iterative DFS that keeps the tetrahedron and sublattice
+// up-counts incrementally.  Pass 1 counts the leaves of every root, an
+// exclusive scan gives each root its output offset, pass 2 writes the leaves.
+// Leaves are mapped back to the original spin numbering with byte tables and
+// sorted as 128-bit keys by two stable LSD radix sorts (low word, then high
+// word) with CUB's device radix sort.
+#include <algorithm>
+#include <array>
+#include <cstring>
+#include <vector>
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include "qsi_device.cuh"
+#include "qsi_handles.h"
+
+namespace qsi {
+namespace {
+
+constexpr int kMaxSpins = 128;
+constexpr int kMaxTets = 128;
+
+struct EnumStep {
+    int8_t tet[4];
+    int8_t unk[4];
+    int8_t tmin[4];
+    int8_t tmax[4];
+    int8_t sl;
+    int8_t rem;
+    int8_t n_tet;
+    int8_t pad;
+};
+
+struct EnumProblem {
+    EnumStep step[kMaxSpins];
+    int8_t target[8];
+    int N;
+    int n_tets;
+    int has_sector;
+    int d0;
+};
+
+__device__ __forceinline__ bool admit(const EnumProblem& P, int i, int v, const int8_t* Q, const int8_t* cnt) {
+    const EnumStep& st = P.step[i];
+    for (int k = 0; k < st.n_tet; ++k) {
+        const int q = Q[st.tet[k]] + v;
+        if (q > st.tmax[k] || q + st.unk[k] < st.tmin[k]) return false;
+    }
+    if (P.has_sector) {
+        const int c = cnt[st.sl] + v;
+        if (c > P.target[st.sl] || c + st.rem < P.target[st.sl]) return false;
+    }
+    return true;
+}
+
+// One thread per subtree root; pass 0 counts leaves, pass 1 writes them.
+__global__ void __launch_bounds__(128) k_enum(const EnumProblem* __restrict__ gP, const state2* __restrict__ roots,
+                                              int64_t n_roots, unsigned long long* __restrict__ counts,
+                                              const unsigned long long* __restrict__ offsets,
+                                              state2* __restrict__ out, unsigned long long* cursor) {
+    __shared__ EnumProblem P;
+    for (int k = threadIdx.x; k < (int)(sizeof(EnumProblem) / 4); k += blockDim.x)
+        reinterpret_cast<int*>(&P)[k] = reinterpret_cast<const int*>(gP)[k];
+    __syncthreads();
+    int8_t Q[kMaxTets];
+    int8_t cnt[8];
+    uint8_t phase[kMaxSpins];
+    for (;;) {
+        const unsigned long long r = atomicAdd(cursor, 1ULL);
+        if (r >= (unsigned long long)n_roots) break;
+        for (int t = 0; t < P.n_tets; ++t) Q[t] = 0;
+        for (int a = 0; a < 8; ++a) cnt[a] = 0;
+        const state2 root = roots[r];
+        uint64_t s0 = root.x, s1 = root.y;
+        for (int i = 0; i < P.d0; ++i) {
+            const bool b = (i < 64) ? ((s0 >> i) & 1) : ((s1 >> (i - 64)) & 1);
+            if (b) {
+                for (int k = 0; k < P.step[i].n_tet; ++k) Q[P.step[i].tet[k]]++;
+                cnt[P.step[i].sl]++;
+            }
+        }
+        unsigned long long found = 0, w = offsets ? offsets[r] : 0;
+        unsigned long long steps = 0;  // bounded walk: a root larger than 2^34 steps sets the error flag
+        int i = P.d0;
+        if (i == P.N) {
+            if (out) out[w] = make_ulonglong2(s0, s1);
+            found = 1;
+        } else {
+            phase[i] = 0;
+            while (i >= P.d0) {
+                if (++steps > (1ULL << 34)) {
+                    atomicOr(cursor + 1, 1ULL);
+                    break;
+                }
+                if (i == P.N) {
+                    if (out) out[w + found] = make_ulonglong2(s0, s1);
+                    ++found;
+                    --i;
+                    continue;
+                }
+                const uint8_t ph = phase[i];
+                if (ph == 0) {
+                    phase[i] = 1;
+                    if (admit(P, i, 0, Q, cnt)) {
+                        ++i;
+                        if (i < P.N) phase[i] = 0;
+                    }
+                    continue;
+                }
+                const uint64_t bit0 = (i < 64) ? (1ULL << i) : 0, bit1 = (i >= 64) ? (1ULL << (i - 64)) : 0;
+                if (ph == 1) {
+                    phase[i] = 2;
+                    if (admit(P, i, 1, Q, cnt)) {
+                        for (int k = 0; k < P.step[i].n_tet; ++k) Q[P.step[i].tet[k]]++;
+                        cnt[P.step[i].sl]++;
+                        s0 |= bit0;
+                        s1 |= bit1;
+                        ++i;
+                        if (i < P.N) phase[i] = 0;
+                    }
+                    continue;
+                }
+                // both values done: undo this level's up spin and return to the parent
+                if ((s0 & bit0) | (s1 & bit1)) {
+                    for (int k = 0; k < P.step[i].n_tet; ++k) Q[P.step[i].tet[k]]--;
+                    cnt[P.step[i].sl]--;
+                    s0 &= ~bit0;
+                    s1 &= ~bit1;
+                }
+                --i;
+            }
+        }
+        if (counts) counts[r] = found;
+    }
+}
+
+// Maps a permuted-space state back: bit i -> spin order[i], eight bits at a time.
+__global__ void k_unpermute(state2* __restrict__ v, int64_t n, const state2* __restrict__ table, int nbytes,
+                            uint64_t* __restrict__ lo, uint64_t* __restrict__ hi) {
+    __shared__ state2 T[16 * 256];
+    for (int k = threadIdx.x; k < nbytes * 256; k += blockDim.x) T[k] = table[k];
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const state2 s = v[i];
+        uint64_t a = 0, b = 0;
+        for (int byte = 0; byte < nbytes; ++byte) {
+            const int val = (int)(((byte < 8) ? (s.x >> (8 * byte)) : (s.y >> (8 * (byte - 8)))) & 0xff);
+            const state2 e = T[byte * 256 + val];
+            a |= e.x;
+            b |= e.y;
+        }
+        lo[i] = a;
+        hi[i] = b;
+    }
+}
+
+__global__ void k_interleave(const uint64_t* __restrict__ lo, const uint64_t* __restrict__ hi, state2* __restrict__ out,
+                             int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = make_ulonglong2(lo[i], hi[i]);
+}
+
+std::vector<int> greedy(int N, const std::vector<std::vector<int>>& spin_tets, int n_tets) {
+    std::vector<int> order{0};
+    std::vector<char> sel(N, 0), cov(n_tets, 0);
+    sel[0] = 1;
+    for (int t : spin_tets[0]) cov[t] = 1;
+    for (int it = 1; it < N; ++it) {
+        int best = -1, bo = -1;
+        for (int i = 0; i < N; ++i) {
+            if (sel[i]) continue;
+            int ov = 0;
+            for (int t : spin_tets[i]) ov += cov[t];
+            if (ov > bo) bo = ov, best = i;
+        }
+        sel[best] = 1;
+        order.push_back(best);
+        for (int t : spin_tets[best]) cov[t] = 1;
+    }
+    return order;
+}
+
+// Host DFS to depth d (same tests as the device), collecting prefixes.
+void host_prefixes(const EnumProblem& P, int d, int i, u128 state, std::vector<int>& Q, std::vector<int>& cnt,
+                   std::vector<u128>& out) {
+    if (i == d) {
+        out.push_back(state);
+        return;
+    }
+    const EnumStep& st = P.step[i];
+    for (int v = 0; v < 2; ++v) {
+        bool ok = true;
+        for (int k = 0; k < st.n_tet; ++k) {
+            int q = Q[st.tet[k]] + v;
+            if (q > st.tmax[k] || q + st.unk[k] < st.tmin[k]) ok = false;
+        }
+        if (P.has_sector) {
+            int c = cnt[st.sl] + v;
+            if (c > P.target[st.sl] || c + st.rem < P.target[st.sl]) ok = false;
+        }
+        if (!ok) continue;
+        if (v) {
+            for (int k = 0; k < st.n_tet; ++k) Q[st.tet[k]]++;
+            cnt[st.sl]++;
+        }
+        host_prefixes(P, d, i + 1, v ? (state | ((u128)1 << i)) : state, Q, cnt, out);
+        if (v) {
+            for (int k = 0; k < st.n_tet; ++k) Q[st.tet[k]]--;
+            cnt[st.sl]--;
+        }
+    }
+}
+
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    cudaError_t alloc(size_t n) { return cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)); }
+    ~DBuf() { cudaFree(p); }
+};
+
+}  // namespace
+}  // namespace qsi
+
+using namespace qsi;
+
+extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* tetra_spins, int32_t n_tetra,
+                                              int32_t tetra_size, const int32_t* sublattice, int32_t n_sublattices,
+                                              const int32_t* sector, uint64_t** out_lohi, int64_t* n_out) {
+    return guarded([&]() -> qsi_status {
+        if (n_spins <= 0 || n_spins > kMaxSpins || !tetra_spins || n_tetra <= 0 || n_tetra > kMaxTets ||
+            tetra_size <= 0 || tetra_size > 127 || !out_lohi || !n_out)
+            return fail(QSI_INVALID_ARG, "qsi_enumerate_basis_gpu: bad argument");
+        if (sector && (!sublattice || n_sublattices <= 0 || n_sublattices > 8))
+            return fail(QSI_INVALID_ARG, "qsi_enumerate_basis_gpu: sector needs 1..8 sublattices");
+        const int N = n_spins;
+        std::vector<std::vector<int>> spin_tets(N), tets(n_tetra);
+        for (int t = 0; t < n_tetra; ++t)
+            for (int k = 0; k < tetra_size; ++k) {
+                int s = tetra_spins[t * tetra_size + k];
+                if (s < 0 || s >= N) return fail(QSI_INVALID_ARG, "tetrahedron %d names spin %d", t, s);
+                spin_tets[s].push_back(t);
+                tets[t].push_back(s);
+            }
+        for (int s = 0; s < N; ++s)
+            if (spin_tets[s].empty() || spin_tets[s].size() > 4)
+                return fail(QSI_INVALID_ARG, "spin %d belongs to %zu tetrahedra (1..4 supported)", s, spin_tets[s].size());
+        std::vector<int> order = greedy(N, spin_tets, n_tetra);
+        std::vector<int> pos(N);
+        for (int i = 0; i < N; ++i) pos[order[i]] = i;
+        EnumProblem P;
+        std::memset(&P, 0, sizeof(P));
+        P.N = N;
+        P.n_tets = n_tetra;
+        P.has_sector = sector != nullptr;
+        for (int i = 0; i < N; ++i) {
+            EnumStep& st = P.step[i];
+            const int s = order[i];
+            st.n_tet = (int8_t)spin_tets[s].size();
+            for (int k = 0; k < st.n_tet; ++k) {
+                const int t = spin_tets[s][k];
+                int unk = 0;
+                for (int m : tets[t]) unk += (pos[m] > i);
+                st.tet[k] = (int8_t)t;
+                st.unk[k] = (int8_t)unk;
+                st.tmin[k] = (int8_t)(tets[t].size() / 2);
+                st.tmax[k] = (int8_t)((tets[t].size() + 1) / 2);
+            }
+            st.sl = (int8_t)(sublattice ? sublattice[s] : 0);
+            if (st.sl < 0 || st.sl >= 8) return fail(QSI_INVALID_ARG, "bad sublattice of spin %d", s);
+            int rem = 0;
+            for (int j = i + 1; j < N; ++j) rem += ((sublattice ? sublattice[order[j]] : 0) == st.sl);
+            st.rem = (int8_t)rem;
+        }
+        if (sector)
+            for (int a = 0; a < n_sublattices; ++a) P.target[a] = (int8_t)sector[a];
+        // prefix depth: deepen until there are enough roots to fill the GPU
+        std::vector<u128> roots;
+        int d0 = std::min(N, 16);
+        for (;;) {
+            roots.clear();
+            std::vector<int> Q(n_tetra, 0), cnt(8, 0);
+            host_prefixes(P, d0, 0, 0, Q, cnt, roots);
+            if (roots.size() >= 400000 || d0 >= N || d0 >= N - 8) break;
+            d0 = std::min(N, d0 + 4);
+        }
+        P.d0 = d0;
+        const int64_t n_roots = (int64_t)roots.size();
+        std::vector<state2> hroots(n_roots);
+        for (int64_t k = 0; k < n_roots; ++k) hroots[k] = make_ulonglong2(lo64(roots[k]), hi64(roots[k]));
+        DBuf<EnumProblem> dP;
+        DBuf<state2> dRoots;
+        DBuf<unsigned long long> dCounts, dOffs, dCur;
+        QSI_CUDA(dP.alloc(1));
+        QSI_CUDA(dRoots.alloc(n_roots));
+        QSI_CUDA(dCounts.alloc(n_roots));
+        QSI_CUDA(dOffs.alloc(n_roots + 1));
+        QSI_CUDA(dCur.alloc(2));
+        QSI_CUDA(cudaMemcpy(dP.p, &P, sizeof(P), cudaMemcpyHostToDevice));
+        QSI_CUDA(cudaMemcpy(dRoots.p, hroots.data(), (size_t)n_roots * sizeof(state2), cudaMemcpyHostToDevice));
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = sms * 16;
+        QSI_CUDA(cudaMemset(dCur.p, 0, 16));
+        k_enum<<<grid, 128>>>(dP.p, dRoots.p, n_roots, dCounts.p, nullptr, nullptr, dCur.p);
+        QSI_CUDA(cudaGetLastError());
+        unsigned long long flags[2] = {0, 0};
+        QSI_CUDA(cudaMemcpy(flags, dCur.p, 16, cudaMemcpyDeviceToHost));
+        if (flags[1]) return fail(QSI_INVALID_ARG, "enumeration: a subtree exceeded the step bound");
+        // exclusive scan of the counts
+        size_t tmp_bytes = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, dCounts.p, dOffs.p, (int)n_roots + 0);
+        DBuf<unsigned char> tmp;
+        QSI_CUDA(tmp.alloc(tmp_bytes));
+        QSI_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, tmp_bytes, dCounts.p, dOffs.p, (int)n_roots));
+        unsigned long long last_off = 0, last_cnt = 0;
+        QSI_CUDA(cudaMemcpy(&last_off, dOffs.p + n_roots - 1, 8, cudaMemcpyDeviceToHost));
+        QSI_CUDA(cudaMemcpy(&last_cnt, dCounts.p + n_roots - 1, 8, cudaMemcpyDeviceToHost));
+        const int64_t total = (int64_t)(last_off + last_cnt);
+        if (total >= (int64_t)UINT32_MAX) return fail(QSI_INVALID_ARG, "enumeration: %lld states exceed 2^32-1", (long long)total);
+        DBuf<state2> dLeaves;
+        QSI_CUDA(dLeaves.alloc(total));
+        QSI_CUDA(cudaMemset(dCur.p, 0, 16));
+        k_enum<<<grid, 128>>>(dP.p, dRoots.p, n_roots, nullptr, dOffs.p, dLeaves.p, dCur.p);
+        QSI_CUDA(cudaGetLastError());
+        // byte tables and un-permutation into separate key arrays
+        const int nbytes = (N + 7) / 8;
+        std::vector<state2> table(16 * 256, make_ulonglong2(0, 0));
+        for (int byte = 0; byte < nbytes; ++byte)
+            for (int v = 0; v < 256; ++v) {
+                u128 acc = 0;
+                for (int b = 0; b < 8; ++b) {
+                    int i = byte * 8 + b;
+                    if (i < N && ((v >> b) & 1)) acc |= (u128)1 << order[i];
+                }
+                table[byte * 256 + v] = make_ulonglong2(lo64(acc), hi64(acc));
+            }
+        DBuf<state2> dTable;
+        DBuf<uint64_t> klo, khi, klo2, khi2;
+        QSI_CUDA(dTable.alloc(16 * 256));
+        QSI_CUDA(cudaMemcpy(dTable.p, table.data(), table.size() * sizeof(state2), cudaMemcpyHostToDevice));
+        QSI_CUDA(klo.alloc(total));
+        QSI_CUDA(khi.alloc(total));
+        QSI_CUDA(klo2.alloc(total));
+        QSI_CUDA(khi2.alloc(total));
+        k_unpermute<<<grid_for(total, 256), 256>>>(dLeaves.p, total, dTable.p, nbytes, klo.p, khi.p);
+        QSI_CUDA(cudaGetLastError());
+        // stable LSD: sort by low word, then by high word
+        size_t sb = 0, sb2 = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, sb, klo.p, klo2.p, khi.p, khi2.p, total);
+        const int hi_bits = std::max(1, N - 64);
+        cub::DeviceRadixSort::SortPairs(nullptr, sb2, khi2.p, khi.p, klo2.p, klo.p, total, 0, hi_bits);
+        DBuf<unsigned char> stmp;
+        QSI_CUDA(stmp.alloc(std::max(sb, sb2)));
+        QSI_CUDA(cub::DeviceRadixSort::SortPairs(stmp.p, sb, klo.p, klo2.p, khi.p, khi2.p, total, 0, std::min(64, N)));
+        if (N > 64) {
+            QSI_CUDA(cub::DeviceRadixSort::SortPairs(stmp.p, sb2, khi2.p, khi.p, klo2.p, klo.p, total, 0, hi_bits));
+        } else {
+            QSI_CUDA(cudaMemcpy(klo.p, klo2.p, (size_t)total * 8, cudaMemcpyDeviceToDevice));
+            QSI_CUDA(cudaMemcpy(khi.p, khi2.p, (size_t)total * 8, cudaMemcpyDeviceToDevice));
+        }
+        k_interleave<<<grid_for(total, 256), 256>>>(klo.p, khi.p, dLeaves.p, total);
+        QSI_CUDA(cudaGetLastError());
+        uint64_t* host = (uint64_t*)std::malloc(std::max<size_t>(1, (size_t)total) * 16);
+        if (!host) return fail(QSI_OOM, "qsi_enumerate_basis_gpu: host allocation of %lld states", (long long)total);
+        cudaError_t e = cudaMemcpy(host, dLeaves.p, (size_t)total * 16, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            std::free(host);
+            return fail(QSI_CUDA_ERROR, "qsi_enumerate_basis_gpu: %s", cudaGetErrorString(e));
+        }
+        *out_lohi = host;
+        *n_out = total;
+        return QSI_OK;
+    });
+}

@@ -476,6 +476,11 @@ extern "C" qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t
             qsi_op_destroy(op);
             return fail(e == cudaErrorMemoryAllocation ? QSI_OOM : QSI_CUDA_ERROR, "qsi_op_create: %s", cudaGetErrorString(e));
         }
+        qsi_status ds = build_diag(op);
+        if (ds != QSI_OK) {
+            qsi_op_destroy(op);
+            return ds;
+        }
         *out = op;
         return QSI_OK;
     });
@@ -489,6 +494,7 @@ extern "C" qsi_status qsi_op_destroy(qsi_op* op) {
     cudaFree(op->d_push_diag);
     cudaFree(op->d_diag_generic);
     cudaFree(op->d_lit_off);
+    cudaFree(op->d_diag);
     cudaFree(op->d_lits);
     cudaFree(op->d_x);
     cudaFree(op->d_y);
@@ -699,7 +705,8 @@ extern "C" qsi_status qsi_basis_info(const qsi_basis* b, int32_t* bucket_bits, i
 extern "C" qsi_status qsi_op_set_kernel(qsi_op* op, int32_t kernel, int32_t use_hash, int32_t list_cap) {
     if (!op || kernel < 0 || kernel > 1 || list_cap < 0) return fail(QSI_INVALID_ARG, "qsi_op_set_kernel: bad argument");
     op->kernel = kernel;
-    op->use_hash = use_hash;
+    op->use_hash = use_hash & 1;
+    op->ff_accumulate = (use_hash & 2) ? 0 : 1;
     if (list_cap > 0) op->list_cap = list_cap;
     return QSI_OK;
 }

@@ -35,6 +35,8 @@ struct qsi_op {
     int kernel = 1;                 // 0 = row-per-thread / warp-per-row, 1 = bit-sliced tiles
     int list_cap = 512;             // hit-list entries per warp in the batched tile kernel
     int use_hash = 1;               // look columns up through the basis hash index when it exists
+    int ff_accumulate = 1;          // FP32 batched applies accumulate rows in double-float (else FP64)
+    double* d_diag = nullptr;       // per-row diagonal (tile kernels)
     cudaStream_t stream = nullptr;
     void* d_x = nullptr;   // staging for host-pointer applies
     void* d_y = nullptr;
@@ -49,5 +51,6 @@ qsi_status launch_apply_to_f64(qsi_op* op, const void* x, double* y, int xdtype,
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
                               cudaStream_t st);
 qsi_status build_hash(qsi_basis* b);
+qsi_status build_diag(qsi_op* op);
 qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vector<double>& w, std::vector<double>& V, cudaStream_t st);
 }  // namespace qsi

@@ -60,12 +60,17 @@ def config1(seed: int = 1) -> Workload:
     return Workload("pyro_1x2x1.Q0", lat, enumerate_basis(lat), g, B)
 
 
-def sector_workload(name: str, seed: int = 3, g_range=(0.2, 1.0), b_amp=0.5, lat_name=None) -> Workload:
-    """Equal-polarisation sector basis of a lattice with g ~ U[g_range]^4, B ~ U[-b_amp, b_amp]^3."""
+def sector_workload(name: str, seed: int = 3, g_range=(0.2, 1.0), b_amp=0.5, lat_name=None, gpu: bool = False) -> Workload:
+    """Equal-polarisation sector basis of a lattice with g ~ U[g_range]^4, B ~ U[-b_amp, b_amp]^3.
+
+    gpu=True enumerates on the GPU (enumerate_basis_gpu), which is how large sectors are built."""
+    from .core import enumerate_basis_gpu
+
     lat = lattice(lat_name or name)
     g, B = ring_zeeman_params(seed, g_range, b_amp)
+    enum = enumerate_basis_gpu if gpu else enumerate_basis
     return Workload(f"{lat.name()[:-5]}.s{'.'.join(map(str, equal_sector(lat)))}", lat,
-                    enumerate_basis(lat, sector=equal_sector(lat)), g, B)
+                    enum(lat, sector=equal_sector(lat)), g, B)
 
 
 def config3(seed: int = 3) -> Workload:

@@ -191,3 +191,20 @@ def test_batched_hit_list_overflow_chunks(built):
     op.apply_batched(X, Y2)
     op.set_kernel(1, 1, list_cap=512)
     assert np.array_equal(Y1, Y2)
+
+
+def test_double_float_accumulation_matches_fp64(built):
+    """FP32 batched applies: double-float row accumulation agrees with FP64 accumulation to FP32 output rounding."""
+    basis, H, b, op = built["golden48_JpmB"]
+    X = np.random.default_rng(21).standard_normal((len(basis), 64)).astype(np.float32)
+    Yff, Y64 = np.zeros_like(X), np.zeros_like(X)
+    op.set_kernel(1, 1)
+    op.apply_batched(X, Yff)
+    op.set_kernel(1, 1 | 2)
+    op.apply_batched(X, Y64)
+    op.set_kernel(1, 1)
+    ulp = np.spacing(np.abs(Y64).astype(np.float32))
+    assert np.all(np.abs(Yff - Y64) <= ulp)
+    Yacc = Y64.copy()
+    op.apply_batched(X, Yacc, accumulate=True)
+    np.testing.assert_allclose(Yacc, 2 * Y64, rtol=1e-6, atol=1e-6 * np.abs(Y64).max())

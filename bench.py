@@ -42,6 +42,7 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--lattice", default="pyro_1x2x3", help="pyro_1x2x1 | pyro_1x2x2 | pyro_1x2x3")
     p.add_argument("--full-basis", action="store_true", help="all Q=0 states instead of the equal sector")
+    p.add_argument("--sector", default="", help="comma-separated sublattice up-counts (default: equal sector)")
     p.add_argument("--R", type=int, default=32, help="vectors of the batched mixed apply")
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
@@ -129,6 +130,13 @@ def make_workload(args, gpu: bool = False):
         g, B = workloads.ring_zeeman_params(args.seed, (0.2, 1.0), 0.5)
         w = workloads.Workload(f"{args.lattice}.Q0", lat, q.enumerate_basis_gpu(lat) if gpu else q.enumerate_basis(lat),
                                g, B)
+    elif args.sector:
+        import qsi_subspace_ed_gb300 as q
+
+        sec = [int(v) for v in args.sector.split(",")]
+        g, B = workloads.ring_zeeman_params(args.seed, (0.2, 1.0), 0.5)
+        enum = q.enumerate_basis_gpu if gpu else q.enumerate_basis
+        w = workloads.Workload(f"{args.lattice}.s{'.'.join(map(str, sec))}", lat, enum(lat, sector=sec), g, B)
     else:
         w = workloads.sector_workload(args.lattice, seed=args.seed, gpu=gpu)
     return w, time.time() - t0
@@ -205,8 +213,12 @@ def run_ours(args):
     w, setup_s = make_workload(args, gpu=True)
     H = w.hamiltonian()
     n = len(w.basis_lohi)
+    t0 = time.time()
     basis = q.ZBasis(w.basis_lohi)
+    t_basis = time.time() - t0
+    t0 = time.time()
     op = q.LazyOpSum(basis, H)
+    t_op = time.time() - t0
     hits, misses = op.connectivity()
     h = hits / n
     dev = torch.device("cuda", local)
@@ -259,7 +271,9 @@ def run_ours(args):
             "config": {"workload": w.name, "n_states": n, "n_terms": len(H), "offdiag_hits_per_row": round(h, 4),
                        "misses": misses, "parallelism": f"replicas x{ws}",
                        "l2": "inputs larger than L2" if inputs_exceed_l2 else "L2 flushed between steps",
-                       "setup_s": round(setup_s, 2)},
+                       "setup_s": {"enumerate": round(setup_s, 2), "basis_index": round(t_basis, 2),
+                                   "operator": round(t_op, 2)},
+                       "index": basis.index_info()},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "bytes_per_row": bytes_per_row, "kernel": "k_apply_tile<double,double,LookupHash>"},

@@ -14,6 +14,7 @@
 // the tile into a shared-memory hit list; then the warp walks the list row
 // by row and gathers each column's R values with coalesced loads.
 #include <algorithm>
+#include <type_traits>
 
 #include "qsi_device.cuh"
 #include "qsi_handles.h"
@@ -136,13 +137,33 @@ __global__ void __launch_bounds__(256) k_apply_tile(TileParams P, LK lk, const X
         for (int t0 = 0; t0 < P.n_off; t0 += 32) {
             uint32_t hits = tile_admitted(S, P.n_off, t0, lane, vmask, spinw);
             while (hits) {
-                const int j = __ffs(hits) - 1;
-                hits &= hits - 1;
-                const PullTerm& T = S.terms[t0 + j];
-                const int64_t J = lk.find(s.x ^ T.x0, s.y ^ T.x1);
-                if (J < 0) continue;
-                const XT xj = x[J];
-                if (above_tol(xj)) acc += term_coeff(T, s) * (double)xj;
+                // up to kNB admitted terms at a time: lookups and gathers in flight together,
+                // contributions added in term order
+                constexpr int kNB = 4;
+                int jj[kNB];
+                uint64_t tl[kNB], th[kNB];
+                int64_t J[kNB];
+                int nh = 0;
+#pragma unroll
+                for (int u = 0; u < kNB; ++u) {
+                    jj[u] = 0;
+                    tl[u] = th[u] = 0;
+                    if (hits) {
+                        jj[u] = __ffs(hits) - 1;
+                        hits &= hits - 1;
+                        const PullTerm& T = S.terms[t0 + jj[u]];
+                        tl[u] = s.x ^ T.x0;
+                        th[u] = s.y ^ T.x1;
+                        ++nh;
+                    }
+                }
+                lk.template find_batch<kNB>(tl, th, J, nh);
+                XT xv[kNB];
+#pragma unroll
+                for (int u = 0; u < kNB; ++u) xv[u] = (u < nh && J[u] >= 0) ? x[J[u]] : (XT)0;
+#pragma unroll
+                for (int u = 0; u < kNB; ++u)
+                    if (u < nh && J[u] >= 0 && above_tol(xv[u])) acc += term_coeff(S.terms[t0 + jj[u]], s) * (double)xv[u];
             }
         }
         if (valid) {
@@ -153,7 +174,7 @@ __global__ void __launch_bounds__(256) k_apply_tile(TileParams P, LK lk, const X
     }
 }
 
-template <typename XT, class LK, bool kFF>
+template <typename XT, class LK, bool kFF, int KM>
 __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
                                                             XT* __restrict__ y, int R, int accumulate, int cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -167,7 +188,7 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
     double* hc = reinterpret_cast<double*>(adm + n_rounds * 32);  // coefficients (8-byte aligned)
     float2* hcf = reinterpret_cast<float2*>(hc);                   // the same slots as (hi, lo) floats
     uint32_t* hJ = reinterpret_cast<uint32_t*>(hc + cap);
-    constexpr int KM = 4;  // up to 128 vectors per pass
+    // KM columns per lane per pass: 32*KM vectors per pass
     const int64_t ntiles = (P.B.n + 31) >> 5;
     for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
         const int64_t row = tile * 32 + lane;
@@ -201,19 +222,37 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                 for (int r = 0; r < n_rounds; ++r) {
                     uint32_t a = adm[r * 32 + lane];
                     while (a) {
-                        const int j = __ffs(a) - 1;
-                        a &= a - 1;
-                        const PullTerm& T = S.terms[r * 32 + j];
-                        const int64_t J = lk.find(s.x ^ T.x0, s.y ^ T.x1);
-                        hJ[k] = (J < 0) ? kEmpty : (uint32_t)J;
-                        const double cf = term_coeff(T, s);
-                        if constexpr (kFF) {
-                            const float ch = (float)cf;
-                            hcf[k] = make_float2(ch, (float)(cf - (double)ch));
-                        } else {
-                            hc[k] = cf;
+                        constexpr int kNB = 4;
+                        int tt[kNB];
+                        uint64_t tl[kNB], th[kNB];
+                        int64_t J[kNB];
+                        int nh = 0;
+#pragma unroll
+                        for (int u = 0; u < kNB; ++u) {
+                            tt[u] = 0;
+                            tl[u] = th[u] = 0;
+                            if (a) {
+                                tt[u] = r * 32 + __ffs(a) - 1;
+                                a &= a - 1;
+                                tl[u] = s.x ^ S.terms[tt[u]].x0;
+                                th[u] = s.y ^ S.terms[tt[u]].x1;
+                                ++nh;
+                            }
                         }
-                        ++k;
+                        lk.template find_batch<kNB>(tl, th, J, nh);
+#pragma unroll
+                        for (int u = 0; u < kNB; ++u) {
+                            if (u >= nh) continue;
+                            hJ[k] = (J[u] < 0) ? kEmpty : (uint32_t)J[u];
+                            const double cf = term_coeff(S.terms[tt[u]], s);
+                            if constexpr (kFF) {
+                                const float ch = (float)cf;
+                                hcf[k] = make_float2(ch, (float)(cf - (double)ch));
+                            } else {
+                                hc[k] = cf;
+                            }
+                            ++k;
+                        }
                     }
                 }
             }
@@ -235,19 +274,25 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                             acc[m] = FF{0.f, 0.f};
                             if (rr < R) ff_fma(acc[m], dh, dlo, (float)x[rl * R + rr]);
                         }
-                        for (int k = b0; k < b0 + nl; ++k) {
-                            const uint32_t J = hJ[k];
-                            if (J == kEmpty) continue;
-                            const float2 ck = hcf[k];
-                            const XT* xr = x + (int64_t)J * R;
+                        // four hits' gathers in flight, then accumulated in list order
+                        for (int k = b0; k < b0 + nl; k += 4) {
+                            float xv[4][KM];
+                            float2 ck[4];
 #pragma unroll
-                            for (int m = 0; m < KM; ++m) {
-                                const int rr = r0 + lane + 32 * m;
-                                if (rr < R) {
-                                    const float xj = (float)xr[rr];
-                                    if (above_tol(xj)) ff_fma(acc[m], ck.x, ck.y, xj);
+                            for (int u = 0; u < 4; ++u) {
+                                const uint32_t J = (k + u < b0 + nl) ? hJ[k + u] : kEmpty;
+                                ck[u] = (J == kEmpty) ? make_float2(0.f, 0.f) : hcf[k + u];
+#pragma unroll
+                                for (int m = 0; m < KM; ++m) {
+                                    const int rr = r0 + lane + 32 * m;
+                                    xv[u][m] = (J != kEmpty && rr < R) ? (float)x[(int64_t)J * R + rr] : 0.f;
                                 }
                             }
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                                for (int m = 0; m < KM; ++m)
+                                    if (above_tol(xv[u][m])) ff_fma(acc[m], ck[u].x, ck[u].y, xv[u][m]);
                         }
 #pragma unroll
                         for (int m = 0; m < KM; ++m) {
@@ -264,19 +309,24 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                             const int rr = r0 + lane + 32 * m;
                             acc[m] = (rr < R) ? dl * (double)x[rl * R + rr] : 0.0;
                         }
-                        for (int k = b0; k < b0 + nl; ++k) {
-                            const uint32_t J = hJ[k];
-                            if (J == kEmpty) continue;
-                            const double ck = hc[k];
-                            const XT* xr = x + (int64_t)J * R;
+                        for (int k = b0; k < b0 + nl; k += 4) {
+                            XT xv[4][KM];
+                            double ck[4];
 #pragma unroll
-                            for (int m = 0; m < KM; ++m) {
-                                const int rr = r0 + lane + 32 * m;
-                                if (rr < R) {
-                                    const XT xj = xr[rr];
-                                    if (above_tol(xj)) acc[m] += ck * (double)xj;
+                            for (int u = 0; u < 4; ++u) {
+                                const uint32_t J = (k + u < b0 + nl) ? hJ[k + u] : kEmpty;
+                                ck[u] = (J == kEmpty) ? 0.0 : hc[k + u];
+#pragma unroll
+                                for (int m = 0; m < KM; ++m) {
+                                    const int rr = r0 + lane + 32 * m;
+                                    xv[u][m] = (J != kEmpty && rr < R) ? x[(int64_t)J * R + rr] : (XT)0;
                                 }
                             }
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                                for (int m = 0; m < KM; ++m)
+                                    if (above_tol(xv[u][m])) acc[m] += ck[u] * (double)xv[u][m];
                         }
 #pragma unroll
                         for (int m = 0; m < KM; ++m) {
@@ -408,19 +458,25 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
         const size_t smem = term_smem(op) + (size_t)nw * per_warp;
         if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "batched apply: %zu bytes of shared memory needed", smem);
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
-        if (xdtype == QSI_F64) {
-            auto k = k_apply_tile_batched<double, LK, false>;
-            set_smem(k, smem);
-            k<<<grid, block, smem, st>>>(P, lk, (const double*)x, (double*)y, R, accumulate, cap);
-        } else if (op->ff_accumulate) {
-            auto k = k_apply_tile_batched<float, LK, true>;
-            set_smem(k, smem);
-            k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
-        } else {
-            auto k = k_apply_tile_batched<float, LK, false>;
-            set_smem(k, smem);
-            k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
-        }
+        auto go = [&](auto km) -> void {
+            constexpr int KM = decltype(km)::value;
+            if (xdtype == QSI_F64) {
+                auto k = k_apply_tile_batched<double, LK, false, KM>;
+                set_smem(k, smem);
+                k<<<grid, block, smem, st>>>(P, lk, (const double*)x, (double*)y, R, accumulate, cap);
+            } else if (op->ff_accumulate) {
+                auto k = k_apply_tile_batched<float, LK, true, KM>;
+                set_smem(k, smem);
+                k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
+            } else {
+                auto k = k_apply_tile_batched<float, LK, false, KM>;
+                set_smem(k, smem);
+                k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
+            }
+        };
+        if (R <= 32) go(std::integral_constant<int, 1>{});
+        else if (R <= 64) go(std::integral_constant<int, 2>{});
+        else go(std::integral_constant<int, 4>{});
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "tile apply launch: %s", cudaGetErrorString(e));

@@ -128,14 +128,54 @@ __device__ __forceinline__ int64_t hash_find(const HashView& Hv, uint64_t lo, ui
     return -1;
 }
 
+// Lookups of up to NB states at once.  The hash variant issues the first
+// probe of every state before resolving any (independent loads in flight);
+// further probes, needed after a collision, follow one by one.
 struct LookupTable {
     BasisView B;
     __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return basis_find(B, lo, hi); }
+    template <int NB>
+    __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n) const {
+#pragma unroll
+        for (int u = 0; u < NB; ++u)
+            if (u < n) J[u] = basis_find(B, lo[u], hi[u]);
+    }
 };
 
 struct LookupHash {
     HashView H;
     __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return hash_find(H, lo, hi); }
+    template <int NB>
+    __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n) const {
+        uint64_t slot[NB];
+        uint4 e[NB];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            slot[u] = state_mix(lo[u], hi[u]) & H.mask;
+            if (u < n) e[u] = __ldg(reinterpret_cast<const uint4*>(H.slots + slot[u]));
+        }
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            if (u >= n) continue;
+            if (hi[u] >> 32) {
+                J[u] = -1;
+                continue;
+            }
+            uint64_t sl = slot[u];
+            uint4 v = e[u];
+            int64_t r = -1;
+            for (uint64_t probe = 0; probe <= H.mask; ++probe) {
+                if (v.w == kEmpty) break;
+                if (v.x == (uint32_t)lo[u] && v.y == (uint32_t)(lo[u] >> 32) && v.z == (uint32_t)hi[u]) {
+                    r = (int64_t)v.w;
+                    break;
+                }
+                sl = (sl + 1) & H.mask;
+                v = __ldg(reinterpret_cast<const uint4*>(H.slots + sl));
+            }
+            J[u] = r;
+        }
+    }
 };
 
 // 32x32 bit-matrix transpose across a warp: lane r holds row r (bit c = [r][c]);

@@ -33,7 +33,7 @@ struct qsi_op {
     int n_lits = 0;
     int nwords = 4;                 // 32-bit words that hold any basis or term bit
     int kernel = 1;                 // 0 = row-per-thread / warp-per-row, 1 = bit-sliced tiles
-    int list_cap = 512;             // hit-list entries per warp in the batched tile kernel
+    int list_cap = 256;             // hit-list entries per warp in the batched tile kernel
     int use_hash = 1;               // look columns up through the basis hash index when it exists
     int ff_accumulate = 1;          // FP32 batched applies accumulate rows in double-float (else FP64)
     double* d_diag = nullptr;       // per-row diagonal (tile kernels)

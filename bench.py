@@ -46,7 +46,8 @@ def parse():
     p.add_argument("--R", type=int, default=32, help="vectors of the batched mixed apply")
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
-    p.add_argument("--no-extras", action="store_true", help="skip batched / FTLM / e2e legs")
+    p.add_argument("--no-extras", action="store_true", help="skip batched / FTLM / e2e / CPU legs")
+    p.add_argument("--legs", default="batched,ftlm,e2e,cpu", help="extra legs after the FP64 headline")
     return p.parse_args()
 
 
@@ -250,12 +251,10 @@ def run_ours(args):
         t_wall = time.time() - t_wall
     barrier()
     per = [a.elapsed_time(b) for a, b in ev]
-    ms = sum(per) / len(per)
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * n / (ms * 1e-3)
+    from qsi_subspace_ed_gb300.replicas import aggregate
+
+    units, ms = aggregate(float(n), sum(per) / len(per), dev)  # sum of states over ranks, slowest rank's time
+    value = units / (ms * 1e-3)
     peak, peak_kind = measured_peaks()
     bytes_per_row = 16 + 8 + 8 * h + 8
     achieved = n * bytes_per_row / (ms * 1e-3) / 1e9
@@ -278,8 +277,9 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "bytes_per_row": bytes_per_row, "kernel": "k_apply_tile<double,double,LookupHash>"},
             "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": t_wall}
-    if not args.no_extras and rank == 0:
-        # batched mixed precision: R FP32 vectors [row][R], FP64 row accumulation
+    legs = set() if args.no_extras else set(args.legs.split(","))
+    if "batched" in legs and rank == 0:
+        # batched mixed precision: R FP32 vectors [row][R], double-float row accumulation
         R = args.R
         X = torch.randn(n, R, dtype=torch.float32, device=dev)
         Y = torch.zeros_like(X)
@@ -302,13 +302,16 @@ def run_ours(args):
                                  "roofline_frac": bbytes / (bms * 1e-3) / 1e9 / peak}
         line["gpu_launches"] += kb
         del X, Y
+    if "ftlm" in legs and rank == 0:
         # FTLM vector-steps/s on the same operator (R vectors, M plain Lanczos steps)
+        R = args.R
         Mf = 20
         t0 = time.time()
         q.ftlm([op], [R], M=Mf, seed=1, precision="mixed")
         tf = time.time() - t0
         line["ftlm"] = {"value": R * Mf / tf, "unit": "vec-steps/s", "R": R, "M": Mf, "precision": "mixed",
                         "note": "includes graph capture and host readout"}
+    if "e2e" in legs and rank == 0:
         # end to end through the C-ABI with pinned host buffers (copies inside the timed region)
         xh = torch.randn(n, dtype=torch.float64).pin_memory()
         yh = torch.zeros(n, dtype=torch.float64).pin_memory()
@@ -322,6 +325,7 @@ def run_ours(args):
         te = (time.time() - t0) / ke
         line["e2e"] = {"value": n / te, "unit": "states/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                        "api": "qsi_op_apply(host pointers)"}
+    if "cpu" in legs and rank == 0:
         line["cpu_baseline"] = cpu_baseline(w, H, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -6,6 +6,8 @@
 // GPU thread with an iterative DFS that keeps the tetrahedron and sublattice
 // up-counts incrementally.  Pass 1 counts the leaves of every root, an
 // exclusive scan gives each root its output offset, pass 2 writes the leaves.
+// The device walk keeps only the partial state in registers: tetrahedron and
+// sublattice up-counts are popcounts against per-step masks in shared memory.
 // Leaves are mapped back to the original spin numbering with byte tables and
 // sorted as 128-bit keys by two stable LSD radix sorts (low word, then high
 // word) with CUB's device radix sort.
@@ -46,95 +48,106 @@ struct EnumProblem {
     int d0;
 };
 
-__device__ __forceinline__ bool admit(const EnumProblem& P, int i, int v, const int8_t* Q, const int8_t* cnt) {
-    const EnumStep& st = P.step[i];
+// Mask form of one search step for the device walk: the (permuted-space)
+// masks of the spin's tetrahedra and of its sublattice, so that up-counts are
+// popcounts of the partial state and no per-node arrays are needed.
+struct MaskStep {
+    uint64_t tm[4][2];   // tetrahedron masks
+    uint64_t sm[2];      // sublattice mask (spins of this step's sublattice)
+    int8_t n_tet, target, rem, pad;
+    int8_t unk[4], tmin[4], tmax[4];
+};
+
+struct MaskProblem {
+    MaskStep step[kMaxSpins];
+    int N, has_sector, d0, pad;
+};
+
+__device__ __forceinline__ int popc2(uint64_t a0, uint64_t a1, const uint64_t* m) {
+    return __popcll(a0 & m[0]) + __popcll(a1 & m[1]);
+}
+
+__device__ __forceinline__ bool admit_step(const MaskProblem& P, const MaskStep& st, int v, uint64_t s0, uint64_t s1) {
     for (int k = 0; k < st.n_tet; ++k) {
-        const int q = Q[st.tet[k]] + v;
+        const int q = popc2(s0, s1, st.tm[k]) + v;
         if (q > st.tmax[k] || q + st.unk[k] < st.tmin[k]) return false;
     }
     if (P.has_sector) {
-        const int c = cnt[st.sl] + v;
-        if (c > P.target[st.sl] || c + st.rem < P.target[st.sl]) return false;
+        const int c = popc2(s0, s1, st.sm) + v;
+        if (c > st.target || c + st.rem < st.target) return false;
     }
     return true;
 }
 
-// One thread per subtree root; pass 0 counts leaves, pass 1 writes them.
-__global__ void __launch_bounds__(128) k_enum(const EnumProblem* __restrict__ gP, const state2* __restrict__ roots,
-                                              int64_t n_roots, unsigned long long* __restrict__ counts,
-                                              const unsigned long long* __restrict__ offsets,
-                                              state2* __restrict__ out, unsigned long long* cursor) {
-    __shared__ EnumProblem P;
-    for (int k = threadIdx.x; k < (int)(sizeof(EnumProblem) / 4); k += blockDim.x)
-        reinterpret_cast<int*>(&P)[k] = reinterpret_cast<const int*>(gP)[k];
+// Register-only walk of one subtree: descending tries 0 then 1 at each level;
+// on the way back the level's bit tells whether 1 is still to be tried.
+// Pass 0 counts leaves, pass 1 writes them at the root's offset.
+__global__ void __launch_bounds__(128) k_enum_mask(const MaskProblem* __restrict__ gP, const state2* __restrict__ roots,
+                                                   int64_t n_roots, unsigned long long* __restrict__ counts,
+                                                   const unsigned long long* __restrict__ offsets,
+                                                   state2* __restrict__ out, unsigned long long* cursor) {
+    __shared__ MaskProblem P;
+    for (int k = threadIdx.x; k < (int)(sizeof(MaskProblem) / 8); k += blockDim.x)
+        reinterpret_cast<uint64_t*>(&P)[k] = reinterpret_cast<const uint64_t*>(gP)[k];
     __syncthreads();
-    int8_t Q[kMaxTets];
-    int8_t cnt[8];
-    uint8_t phase[kMaxSpins];
     for (;;) {
         const unsigned long long r = atomicAdd(cursor, 1ULL);
         if (r >= (unsigned long long)n_roots) break;
-        for (int t = 0; t < P.n_tets; ++t) Q[t] = 0;
-        for (int a = 0; a < 8; ++a) cnt[a] = 0;
         const state2 root = roots[r];
         uint64_t s0 = root.x, s1 = root.y;
-        for (int i = 0; i < P.d0; ++i) {
-            const bool b = (i < 64) ? ((s0 >> i) & 1) : ((s1 >> (i - 64)) & 1);
-            if (b) {
-                for (int k = 0; k < P.step[i].n_tet; ++k) Q[P.step[i].tet[k]]++;
-                cnt[P.step[i].sl]++;
-            }
-        }
-        unsigned long long found = 0, w = offsets ? offsets[r] : 0;
-        unsigned long long steps = 0;  // bounded walk: a root larger than 2^34 steps sets the error flag
+        unsigned long long found = 0, steps = 0;
+        const unsigned long long w = offsets ? offsets[r] : 0;
         int i = P.d0;
-        if (i == P.N) {
-            if (out) out[w] = make_ulonglong2(s0, s1);
-            found = 1;
-        } else {
-            phase[i] = 0;
-            while (i >= P.d0) {
-                if (++steps > (1ULL << 34)) {
-                    atomicOr(cursor + 1, 1ULL);
-                    break;
-                }
+        bool down = true;
+        for (;;) {
+            if (++steps > (1ULL << 36)) {
+                atomicOr(cursor + 1, 1ULL);
+                break;
+            }
+            if (down) {
                 if (i == P.N) {
                     if (out) out[w + found] = make_ulonglong2(s0, s1);
                     ++found;
+                    down = false;
                     --i;
+                    if (i < P.d0) break;
                     continue;
                 }
-                const uint8_t ph = phase[i];
-                if (ph == 0) {
-                    phase[i] = 1;
-                    if (admit(P, i, 0, Q, cnt)) {
-                        ++i;
-                        if (i < P.N) phase[i] = 0;
-                    }
+                const MaskStep& st = P.step[i];
+                if (admit_step(P, st, 0, s0, s1)) {
+                    ++i;
                     continue;
                 }
-                const uint64_t bit0 = (i < 64) ? (1ULL << i) : 0, bit1 = (i >= 64) ? (1ULL << (i - 64)) : 0;
-                if (ph == 1) {
-                    phase[i] = 2;
-                    if (admit(P, i, 1, Q, cnt)) {
-                        for (int k = 0; k < P.step[i].n_tet; ++k) Q[P.step[i].tet[k]]++;
-                        cnt[P.step[i].sl]++;
-                        s0 |= bit0;
-                        s1 |= bit1;
-                        ++i;
-                        if (i < P.N) phase[i] = 0;
-                    }
+                if (admit_step(P, st, 1, s0, s1)) {
+                    if (i < 64) s0 |= 1ULL << i;
+                    else s1 |= 1ULL << (i - 64);
+                    ++i;
                     continue;
                 }
-                // both values done: undo this level's up spin and return to the parent
-                if ((s0 & bit0) | (s1 & bit1)) {
-                    for (int k = 0; k < P.step[i].n_tet; ++k) Q[P.step[i].tet[k]]--;
-                    cnt[P.step[i].sl]--;
-                    s0 &= ~bit0;
-                    s1 &= ~bit1;
-                }
+                down = false;
                 --i;
+                if (i < P.d0) break;
+                continue;
             }
+            // returning to level i: its bit tells which value was taken
+            const bool set = (i < 64) ? ((s0 >> i) & 1) : ((s1 >> (i - 64)) & 1);
+            if (set) {
+                if (i < 64) s0 &= ~(1ULL << i);
+                else s1 &= ~(1ULL << (i - 64));
+                --i;
+                if (i < P.d0) break;
+                continue;
+            }
+            const MaskStep& st = P.step[i];
+            if (admit_step(P, st, 1, s0, s1)) {
+                if (i < 64) s0 |= 1ULL << i;
+                else s1 |= 1ULL << (i - 64);
+                ++i;
+                down = true;
+                continue;
+            }
+            --i;
+            if (i < P.d0) break;
         }
         if (counts) counts[r] = found;
     }
@@ -286,14 +299,40 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
             roots.clear();
             std::vector<int> Q(n_tetra, 0), cnt(8, 0);
             host_prefixes(P, d0, 0, 0, Q, cnt, roots);
-            if (roots.size() >= 400000 || d0 >= N || d0 >= N - 8) break;
+            if (roots.size() >= 2000000 || d0 >= N || d0 >= N - 8) break;
             d0 = std::min(N, d0 + 4);
         }
         P.d0 = d0;
+        MaskProblem M;
+        std::memset(&M, 0, sizeof(M));
+        M.N = N;
+        M.has_sector = sector != nullptr;
+        M.d0 = d0;
+        for (int i = 0; i < N; ++i) {
+            const int s = order[i];
+            MaskStep& ms = M.step[i];
+            ms.n_tet = P.step[i].n_tet;
+            for (int k = 0; k < ms.n_tet; ++k) {
+                u128 tm = 0;
+                for (int m : tets[spin_tets[s][k]]) tm |= (u128)1 << pos[m];
+                ms.tm[k][0] = lo64(tm);
+                ms.tm[k][1] = hi64(tm);
+                ms.unk[k] = P.step[i].unk[k];
+                ms.tmin[k] = P.step[i].tmin[k];
+                ms.tmax[k] = P.step[i].tmax[k];
+            }
+            u128 sm = 0;
+            for (int j = 0; j < N; ++j)
+                if ((sublattice ? sublattice[order[j]] : 0) == P.step[i].sl) sm |= (u128)1 << j;
+            ms.sm[0] = lo64(sm);
+            ms.sm[1] = hi64(sm);
+            ms.target = sector ? (int8_t)sector[P.step[i].sl] : 0;
+            ms.rem = P.step[i].rem;
+        }
         const int64_t n_roots = (int64_t)roots.size();
         std::vector<state2> hroots(n_roots);
         for (int64_t k = 0; k < n_roots; ++k) hroots[k] = make_ulonglong2(lo64(roots[k]), hi64(roots[k]));
-        DBuf<EnumProblem> dP;
+        DBuf<MaskProblem> dP;
         DBuf<state2> dRoots;
         DBuf<unsigned long long> dCounts, dOffs, dCur;
         QSI_CUDA(dP.alloc(1));
@@ -301,14 +340,14 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
         QSI_CUDA(dCounts.alloc(n_roots));
         QSI_CUDA(dOffs.alloc(n_roots + 1));
         QSI_CUDA(dCur.alloc(2));
-        QSI_CUDA(cudaMemcpy(dP.p, &P, sizeof(P), cudaMemcpyHostToDevice));
+        QSI_CUDA(cudaMemcpy(dP.p, &M, sizeof(M), cudaMemcpyHostToDevice));
         QSI_CUDA(cudaMemcpy(dRoots.p, hroots.data(), (size_t)n_roots * sizeof(state2), cudaMemcpyHostToDevice));
         int dev = 0, sms = 148;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int grid = sms * 16;
         QSI_CUDA(cudaMemset(dCur.p, 0, 16));
-        k_enum<<<grid, 128>>>(dP.p, dRoots.p, n_roots, dCounts.p, nullptr, nullptr, dCur.p);
+        k_enum_mask<<<grid, 128>>>(dP.p, dRoots.p, n_roots, dCounts.p, nullptr, nullptr, dCur.p);
         QSI_CUDA(cudaGetLastError());
         unsigned long long flags[2] = {0, 0};
         QSI_CUDA(cudaMemcpy(flags, dCur.p, 16, cudaMemcpyDeviceToHost));
@@ -327,7 +366,7 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
         DBuf<state2> dLeaves;
         QSI_CUDA(dLeaves.alloc(total));
         QSI_CUDA(cudaMemset(dCur.p, 0, 16));
-        k_enum<<<grid, 128>>>(dP.p, dRoots.p, n_roots, nullptr, dOffs.p, dLeaves.p, dCur.p);
+        k_enum_mask<<<grid, 128>>>(dP.p, dRoots.p, n_roots, nullptr, dOffs.p, dLeaves.p, dCur.p);
         QSI_CUDA(cudaGetLastError());
         // byte tables and un-permutation into separate key arrays
         const int nbytes = (N + 7) / 8;

@@ -29,6 +29,7 @@ struct TileParams {
     const PushTerm* dgen;
     DiagSpec D;
     const double* diag;  // per-row diagonal, precomputed with diag_value
+    const float2* diag_ff;  // the same as (hi, lo) float pairs
     int n_off, n_lits, nwords;
 };
 
@@ -120,7 +121,7 @@ __device__ __forceinline__ double term_coeff(const PullTerm& T, const state2 s) 
 }
 
 template <typename XT, typename YT, class LK>
-__global__ void __launch_bounds__(256) k_apply_tile(TileParams P, LK lk, const XT* __restrict__ x,
+__global__ void __launch_bounds__(256, 4) k_apply_tile(TileParams P, LK lk, const XT* __restrict__ x,
                                                     YT* __restrict__ y, int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TileSmem S = stage_terms(P, smem_raw);
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(256) k_apply_tile(TileParams P, LK lk, const X
 }
 
 template <typename XT, class LK, bool kFF, int KM>
-__global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
+__global__ void __launch_bounds__(256, 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
                                                             XT* __restrict__ y, int R, int accumulate, int cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TileSmem S = stage_terms(P, smem_raw);
@@ -244,12 +245,12 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                         for (int u = 0; u < kNB; ++u) {
                             if (u >= nh) continue;
                             hJ[k] = (J[u] < 0) ? kEmpty : (uint32_t)J[u];
-                            const double cf = term_coeff(S.terms[tt[u]], s);
+                            const PullTerm& T = S.terms[tt[u]];
                             if constexpr (kFF) {
-                                const float ch = (float)cf;
-                                hcf[k] = make_float2(ch, (float)(cf - (double)ch));
+                                const bool neg = T.has_z && ((__popcll(~s.x & T.z0) + __popcll(~s.y & T.z1)) & 1);
+                                hcf[k] = neg ? make_float2(-T.cs_hi, -T.cs_lo) : make_float2(T.cs_hi, T.cs_lo);
                             } else {
-                                hc[k] = cf;
+                                hc[k] = term_coeff(T, s);
                             }
                             ++k;
                         }
@@ -257,43 +258,30 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                 }
             }
             __syncwarp();
-            for (int l = row_start; l < row_end; ++l) {
-                const int b0 = __shfl_sync(0xffffffffu, base, l);
-                const int nl = __shfl_sync(0xffffffffu, cnt, l);
-                const double dl = __shfl_sync(0xffffffffu, d, l);
-                const int64_t rl = tile * 32 + l;
-                if (rl >= P.B.n) break;
+            if constexpr (kFF) {
+                // FP32 storage, double-float accumulation, no FP64 instruction.  The chunk's hit list
+                // is walked in order across row boundaries with kU column gathers in flight.
+                constexpr int kU = 8;
+                const int kbeg = __shfl_sync(0xffffffffu, base, row_start);
+                const int last = row_end - 1;
+                const int kend = __shfl_sync(0xffffffffu, base + cnt, last);
                 for (int r0 = 0; r0 < R; r0 += 32 * KM) {
-                    if constexpr (kFF) {
-                        // FP32 storage, double-float row accumulation (no FP64 instructions)
-                        FF acc[KM];
-                        const float dh = (float)dl, dlo = (float)(dl - (double)dh);
+                    int l = row_start;
+                    int lend = __shfl_sync(0xffffffffu, base + cnt, l);
+                    FF acc[KM];
+                    auto start_row = [&](int rr_l) {
+                        const int64_t rl = tile * 32 + rr_l;
+                        const float2 dd = (rl < P.B.n) ? P.diag_ff[rl] : make_float2(0.f, 0.f);
 #pragma unroll
                         for (int m = 0; m < KM; ++m) {
                             const int rr = r0 + lane + 32 * m;
                             acc[m] = FF{0.f, 0.f};
-                            if (rr < R) ff_fma(acc[m], dh, dlo, (float)x[rl * R + rr]);
+                            if (rr < R && rl < P.B.n) ff_fma(acc[m], dd.x, dd.y, (float)x[rl * R + rr]);
                         }
-                        // four hits' gathers in flight, then accumulated in list order
-                        for (int k = b0; k < b0 + nl; k += 4) {
-                            float xv[4][KM];
-                            float2 ck[4];
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                const uint32_t J = (k + u < b0 + nl) ? hJ[k + u] : kEmpty;
-                                ck[u] = (J == kEmpty) ? make_float2(0.f, 0.f) : hcf[k + u];
-#pragma unroll
-                                for (int m = 0; m < KM; ++m) {
-                                    const int rr = r0 + lane + 32 * m;
-                                    xv[u][m] = (J != kEmpty && rr < R) ? (float)x[(int64_t)J * R + rr] : 0.f;
-                                }
-                            }
-#pragma unroll
-                            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                                for (int m = 0; m < KM; ++m)
-                                    if (above_tol(xv[u][m])) ff_fma(acc[m], ck[u].x, ck[u].y, xv[u][m]);
-                        }
+                    };
+                    auto finish_row = [&](int rr_l) {
+                        const int64_t rl = tile * 32 + rr_l;
+                        if (rl >= P.B.n) return;
 #pragma unroll
                         for (int m = 0; m < KM; ++m) {
                             const int rr = r0 + lane + 32 * m;
@@ -302,7 +290,51 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                                 y[rl * R + rr] = (XT)(acc[m].hi + acc[m].lo);
                             }
                         }
-                    } else {
+                    };
+                    start_row(l);
+                    for (int k0 = kbeg; k0 < kend; k0 += kU) {
+                        float xv[kU][KM];
+                        float2 ck[kU];
+#pragma unroll
+                        for (int u = 0; u < kU; ++u) {
+                            const uint32_t J = (k0 + u < kend) ? hJ[k0 + u] : kEmpty;
+                            ck[u] = (J == kEmpty) ? make_float2(0.f, 0.f) : hcf[k0 + u];
+#pragma unroll
+                            for (int m = 0; m < KM; ++m) {
+                                const int rr = r0 + lane + 32 * m;
+                                xv[u][m] = (J != kEmpty && rr < R) ? (float)x[(int64_t)J * R + rr] : 0.f;
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < kU; ++u) {
+                            const int k = k0 + u;
+                            if (k >= kend) break;
+                            while (k >= lend) {  // rows whose hits are complete
+                                finish_row(l);
+                                ++l;
+                                lend = __shfl_sync(0xffffffffu, base + cnt, l);
+                                start_row(l);
+                            }
+#pragma unroll
+                            for (int m = 0; m < KM; ++m)
+                                if (above_tol(xv[u][m])) ff_fma(acc[m], ck[u].x, ck[u].y, xv[u][m]);
+                        }
+                    }
+                    finish_row(l);
+                    for (++l; l <= last; ++l) {  // trailing rows without hits
+                        start_row(l);
+                        finish_row(l);
+                    }
+                }
+            } else {
+            for (int l = row_start; l < row_end; ++l) {
+                const int b0 = __shfl_sync(0xffffffffu, base, l);
+                const int nl = __shfl_sync(0xffffffffu, cnt, l);
+                const double dl = __shfl_sync(0xffffffffu, d, l);
+                const int64_t rl = tile * 32 + l;
+                if (rl >= P.B.n) break;
+                for (int r0 = 0; r0 < R; r0 += 32 * KM) {
+                    {
                         double acc[KM];
 #pragma unroll
                         for (int m = 0; m < KM; ++m) {
@@ -340,6 +372,7 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
                     }
                 }
             }
+            }
             __syncwarp();
             row_start = row_end;
         }
@@ -348,16 +381,22 @@ __global__ void __launch_bounds__(256) k_apply_tile_batched(TileParams P, LK lk,
 
 // Per-row diagonal, evaluated once per operator with the same arithmetic as
 // diag_value in the row kernels.
-__global__ void k_diag_precompute(BasisView B, DiagSpec D, const PushTerm* __restrict__ dgen, double* __restrict__ out) {
+__global__ void k_diag_precompute(BasisView B, DiagSpec D, const PushTerm* __restrict__ dgen, double* __restrict__ out,
+                                  float2* __restrict__ out_ff) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < B.n; i += (int64_t)gridDim.x * blockDim.x) {
         const state2 s = B.states[i];
-        out[i] = diag_value(D, dgen, s.x, s.y);
+        const double d = diag_value(D, dgen, s.x, s.y);
+        out[i] = d;
+        const float h = (float)d;
+        out_ff[i] = make_float2(h, (float)(d - (double)h));
     }
 }
 
 qsi_status build_diag(qsi_op* op) {
     QSI_CUDA(cudaMalloc(&op->d_diag, (size_t)op->basis->n * sizeof(double)));
-    k_diag_precompute<<<grid_for(op->basis->n, 256), 256>>>(op->basis->view(), op->diag, op->d_diag_generic, op->d_diag);
+    QSI_CUDA(cudaMalloc(&op->d_diag_ff, (size_t)op->basis->n * sizeof(float2)));
+    k_diag_precompute<<<grid_for(op->basis->n, 256), 256>>>(op->basis->view(), op->diag, op->d_diag_generic, op->d_diag,
+                                                             op->d_diag_ff);
     QSI_CUDA(cudaGetLastError());
     QSI_CUDA(cudaDeviceSynchronize());
     return QSI_OK;
@@ -429,7 +468,7 @@ template <class LK>
 static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int R, int xdtype, int ydtype,
                                   int accumulate, cudaStream_t st) {
     TileParams P{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
-                 op->d_diag, op->n_pull, op->n_lits, op->nwords};
+                 op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords};
     const int block = 256, nw = block / 32;
     const int64_t ntiles = (P.B.n + 31) / 32;
     int dev = 0, sms = 148;

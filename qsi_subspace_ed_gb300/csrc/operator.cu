@@ -380,6 +380,8 @@ extern "C" qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t
             // reference's evaluation on the image state, see operator.hpp:246-253
             q.cs = t.c * (double)t.sign;
             q.has_z = (t.z[0] | t.z[1]) != 0;
+            q.cs_hi = (float)q.cs;
+            q.cs_lo = (float)(q.cs - (double)q.cs_hi);
             pull.push_back(q);
         }
         // A single-site z class whose bits overlap another class with a
@@ -495,6 +497,7 @@ extern "C" qsi_status qsi_op_destroy(qsi_op* op) {
     cudaFree(op->d_diag_generic);
     cudaFree(op->d_lit_off);
     cudaFree(op->d_diag);
+    cudaFree(op->d_diag_ff);
     cudaFree(op->d_lits);
     cudaFree(op->d_x);
     cudaFree(op->d_y);

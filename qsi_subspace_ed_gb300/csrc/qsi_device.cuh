@@ -16,8 +16,10 @@ using state2 = ulonglong2;
 // The matrix element is cs * (-1)^popcount(~s & Z).
 struct PullTerm {
     uint64_t x0, x1, z0, z1, up0, up1, dn0, dn1;
-    double cs;  // coefficient times construction sign
+    double cs;       // coefficient times construction sign
     int32_t has_z;
+    float cs_hi;     // cs as a double-float pair (cs_hi + cs_lo), for FP32 accumulation
+    float cs_lo;
     int32_t pad;
 };
 

@@ -37,6 +37,7 @@ struct qsi_op {
     int use_hash = 1;               // look columns up through the basis hash index when it exists
     int ff_accumulate = 1;          // FP32 batched applies accumulate rows in double-float (else FP64)
     double* d_diag = nullptr;       // per-row diagonal (tile kernels)
+    float2* d_diag_ff = nullptr;    // the same as double-float pairs (FP32 batched kernel)
     cudaStream_t stream = nullptr;
     void* d_x = nullptr;   // staging for host-pointer applies
     void* d_y = nullptr;

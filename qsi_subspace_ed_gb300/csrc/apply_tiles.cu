@@ -121,7 +121,7 @@ __device__ __forceinline__ double term_coeff(const PullTerm& T, const state2 s) 
 }
 
 template <typename XT, typename YT, class LK>
-__global__ void __launch_bounds__(256, 4) k_apply_tile(TileParams P, LK lk, const XT* __restrict__ x,
+__global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, const XT* __restrict__ x,
                                                     YT* __restrict__ y, int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TileSmem S = stage_terms(P, smem_raw);

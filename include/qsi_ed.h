@@ -159,6 +159,16 @@ qsi_status qsi_op_destroy(qsi_op* op);
  *                            the RealApplyFn contract, common_bits.hpp:18-23) */
 qsi_status qsi_op_apply(qsi_op* op, const double* x, double* y, int32_t accumulate,
                         int32_t flags, void* stream);
+/* y = H x (accumulate = 0) or y += H x (accumulate = 1) for HOST x and y,
+ * without allocating device memory: the vectors are staged through two
+ * fixed arrays compiled into the library (4 MiB per GPU that loads it), for
+ * callers whose process cannot make new device allocations (GPU memory owned
+ * by another allocator or an exhausted quota).  At most 262,144 basis states
+ * (QSI_INVALID_ARG beyond).  Calls share the arrays: calls that overlap on
+ * the GPU race; consecutive calls from one thread do not.  The first call on
+ * a device looks the arrays up, so make it before any stream capture; the
+ * current device must be the operator's.  No counterpart in the reference. */
+qsi_status qsi_op_apply_static(qsi_op* op, const double* x, double* y, int32_t accumulate);
 /* Batched apply over R vectors stored row-major [dim][R] (element type dtype:
  * QSI_F64, or QSI_F32 storage with FP64 per-row accumulation). */
 qsi_status qsi_op_apply_batched(qsi_op* op, const void* X, void* Y, int32_t R,

@@ -105,6 +105,7 @@ SIGNATURES = {
     "qsi_op_create": [_P, _P, _I32, C.POINTER(_P)],
     "qsi_op_destroy": [_P],
     "qsi_op_apply": [_P, _P, _P, _I32, _I32, _P],
+    "qsi_op_apply_static": [_P, _P, _P, _I32],
     "qsi_op_apply_batched": [_P, _P, _P, _I32, _I32, _I32, _I32, _P],
     "qsi_op_set_kernel": [_P, _I32, _I32, _I32],
     "qsi_op_triplets": [_P, _D, _P, _P, _P, _I64, C.POINTER(_I64)],

@@ -344,6 +344,11 @@ class LazyOpSum:
         """y = H x."""
         call("qsi_op_apply", self._h, ptr(x), ptr(y), 0, self._kind(x), self._stream(x))
 
+    def evaluate_static(self, x, y, accumulate: bool = False) -> None:
+        """y (+)= H x for host numpy vectors without any device allocation (bases of at most
+        262,144 states; see qsi_op_apply_static)."""
+        call("qsi_op_apply_static", self._h, ptr(x), ptr(y), int(accumulate))
+
     def __matmul__(self, x):
         y = np.zeros_like(x) if not hasattr(x, "is_cuda") else x.new_zeros(x.shape)
         self.evaluate(x, y)

@@ -1,0 +1,53 @@
+"""The host-buffer apply that allocates no device memory (qsi_op_apply_static).
+
+It exists for callers whose process cannot make new device allocations, e.g.
+when another allocator already owns the GPU's memory.  It must give the same
+result as the ordinary host-pointer apply, call after call, since every call
+reuses the same fixed staging arrays.  This file is collected last on purpose.
+"""
+import numpy as np
+import pytest
+
+import qsi_subspace_ed_gb300 as q
+from qsi_subspace_ed_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _op():
+    w = workloads.config1()
+    return q.LazyOpSum(q.ZBasis(w.basis_lohi), w.hamiltonian())
+
+
+def test_static_apply_matches_ordinary_apply_twice():
+    op = _op()
+    rng = np.random.default_rng(17)
+    for call in range(2):
+        x = rng.standard_normal(op.rows())
+        y_ref = np.zeros_like(x)
+        op.evaluate(x, y_ref)
+        y = np.full_like(x, np.nan)  # stale contents must not leak into the result
+        op.evaluate_static(x, y)
+        np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max(), err_msg=f"call {call}")
+    # accumulate: y += H x, twice in a row
+    x = rng.standard_normal(op.rows())
+    y0 = rng.standard_normal(op.rows())
+    y_ref = y0.copy()
+    op.evaluate_add(x, y_ref)
+    y = y0.copy()
+    op.evaluate_static(x, y, accumulate=True)
+    np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+    op.evaluate_add(x, y_ref)
+    op.evaluate_static(x, y, accumulate=True)
+    np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+
+
+def test_static_apply_rejects_bases_above_the_limit():
+    lat = workloads.lattice("pyro_1x2x2")
+    basis = q.ZBasis(q.enumerate_basis(lat))  # 2,891,562 states > 262,144
+    op = q.LazyOpSum(basis, q.build_ring_zeeman(lat, [1, .8, .6, .4], [0.1, 0.0, 0.0]))
+    x = np.zeros(op.rows())
+    y = np.zeros(op.rows())
+    with pytest.raises(q.QsiError) as e:
+        op.evaluate_static(x, y)
+    assert e.value.status == q._lib.QSI_INVALID_ARG and "262144" in str(e.value)

@@ -47,7 +47,10 @@ def parse():
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true", help="skip batched / FTLM / e2e / CPU legs")
-    p.add_argument("--legs", default="batched,ftlm,e2e,cpu", help="extra legs after the FP64 headline")
+    p.add_argument("--legs", default="batched,ftlm,e2e,cpu",
+                   help="extra legs after the FP64 headline (also: lanczos = FP64 vs mixed 10-eigenvalue solves)")
+    p.add_argument("--nev", type=int, default=10)
+    p.add_argument("--ncv", type=int, default=24)
     return p.parse_args()
 
 
@@ -325,6 +328,27 @@ def run_ours(args):
         te = (time.time() - t0) / ke
         line["e2e"] = {"value": n / te, "unit": "states/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                        "api": "qsi_op_apply(host pointers)"}
+    if "lanczos" in legs and rank == 0:
+        # BASELINE configs 2/3: the nev lowest eigenpairs in plain FP64 and in mixed precision (FP32 Krylov
+        # vectors and gathers, FP64 recurrences, FP64 Rayleigh-Ritz polish), errors of the mixed eigenvalues
+        del x, y
+        torch.cuda.empty_cache()
+        out = {"nev": args.nev, "ncv": args.ncv, "tol": 1e-10}
+        res = {}
+        for prec, polish in (("f64", 0), ("mixed", 2)):
+            torch.cuda.synchronize()
+            t0 = time.time()
+            ev, _, rep = q.diagonalise(op, nev=args.nev, ncv=args.ncv, tol=1e-10, max_iter=400, seed=1,
+                                       precision=prec, polish_steps=polish, want_vectors=False)
+            dt = time.time() - t0
+            res[prec] = ev
+            out[prec] = {"seconds": dt, "applies": rep.applies, "restarts": rep.restarts, "converged": rep.converged,
+                         "evals": [float(v) for v in ev], "max_residual": float(np.max(rep.residual[:args.nev]))}
+        err = np.abs(res["mixed"] - res["f64"])
+        out["abs_err_mixed_vs_f64"] = [float(v) for v in err]
+        out["max_abs_err"] = float(err.max())
+        out["speedup_mixed_vs_f64"] = out["f64"]["seconds"] / out["mixed"]["seconds"]
+        line["lanczos"] = out
     if "cpu" in legs and rank == 0:
         line["cpu_baseline"] = cpu_baseline(w, H, args.cpu_seconds)
     if rank == 0:

@@ -50,6 +50,9 @@ def parse():
     p.add_argument("--legs", default="batched,ftlm,e2e,cpu",
                    help="extra legs after the FP64 headline (also: lanczos = FP64 vs mixed 10-eigenvalue solves)")
     p.add_argument("--nev", type=int, default=10)
+    p.add_argument("--serve-n", type=int, default=240)
+    p.add_argument("--serve-rate", type=float, default=40.0)
+    p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--ncv", type=int, default=24)
     return p.parse_args()
 
@@ -170,6 +173,31 @@ def cpu_baseline(w, H, seconds: float):
     return {"value": rows / dt, "unit": "states/s", "cores": threads, "kind": "port",
             "sample": f"push-form apply (per-term OpenMP pass, atomic scatter, binary search) over source rows "
                       f"[0,{rows}) of {n} of {w.name}; {dt:.1f}s"}
+
+
+def serve_leg(args):
+    """Config-5 style request loop: Poisson phase-diagram points over three resident sectors, served with
+    `slots` concurrent solves, against the same requests solved one after another."""
+    import qsi_subspace_ed_gb300 as q
+    from qsi_subspace_ed_gb300 import serve, workloads
+
+    l32, l64 = workloads.lattice("pyro_1x2x1"), workloads.lattice("pyro_1x2x2")
+    sectors = {"pyro_1x2x1.Q0": serve.Sector("pyro_1x2x1.Q0", l32, q.enumerate_basis(l32)),
+               "pyro_1x2x2.s8.8.8.8": serve.Sector("pyro_1x2x2.s8.8.8.8", l64, q.enumerate_basis_gpu(l64, [8, 8, 8, 8])),
+               "pyro_1x2x2.Q0": serve.Sector("pyro_1x2x2.Q0", l64, q.enumerate_basis_gpu(l64))}
+    weights = {"pyro_1x2x1.Q0": 0.5, "pyro_1x2x2.s8.8.8.8": 0.35, "pyro_1x2x2.Q0": 0.15}
+    out = {"requests": args.serve_n, "rate_per_s": args.serve_rate, "nev": 5, "tol": 1e-9, "slots": args.serve_slots,
+           "sectors": {k: v.dim for k, v in sectors.items()}, "weights": weights,
+           "note": "the 96-spin sector of the request mix is replaced by the 64-spin Q=0 basis"}
+    for name, slots in (("serial", 1), ("continuous", args.serve_slots)):
+        loop = serve.RequestLoop(sectors, slots=slots)
+        try:
+            arr = serve.poisson_requests(args.serve_n, args.serve_rate if slots > 1 else 1e9, weights, seed=7)
+            out[name] = serve.run_arrivals(loop, arr)
+        finally:
+            loop.close()
+    out["throughput_ratio"] = out["continuous"]["solves_per_s"] / out["serial"]["solves_per_s"]
+    return out
 
 
 def run_reference(args):
@@ -344,11 +372,19 @@ def run_ours(args):
             res[prec] = ev
             out[prec] = {"seconds": dt, "applies": rep.applies, "restarts": rep.restarts, "converged": rep.converged,
                          "evals": [float(v) for v in ev], "max_residual": float(np.max(rep.residual[:args.nev]))}
-        err = np.abs(res["mixed"] - res["f64"])
+        # Single-vector Krylov methods pick up copies of a degenerate level only through rounding, so the two
+        # runs may list a degenerate level a different number of times: each mixed eigenvalue is compared
+        # with the nearest FP64 eigenvalue, over the levels both runs reached (below the larger of their
+        # highest values, the lists are complete in both).
+        top = min(res["mixed"].max(), res["f64"].max())
+        err = np.array([np.abs(res["f64"] - v).min() for v in res["mixed"] if v <= top + 1e-8])
         out["abs_err_mixed_vs_f64"] = [float(v) for v in err]
         out["max_abs_err"] = float(err.max())
+        out["levels_compared"] = int(len(err))
         out["speedup_mixed_vs_f64"] = out["f64"]["seconds"] / out["mixed"]["seconds"]
         line["lanczos"] = out
+    if "serve" in legs and rank == 0:
+        line["serve"] = serve_leg(args)
     if "cpu" in legs and rank == 0:
         line["cpu_baseline"] = cpu_baseline(w, H, args.cpu_seconds)
     if rank == 0:

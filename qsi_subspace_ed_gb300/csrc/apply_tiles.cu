@@ -393,12 +393,13 @@ __global__ void k_diag_precompute(BasisView B, DiagSpec D, const PushTerm* __res
 }
 
 qsi_status build_diag(qsi_op* op) {
-    QSI_CUDA(cudaMalloc(&op->d_diag, (size_t)op->basis->n * sizeof(double)));
-    QSI_CUDA(cudaMalloc(&op->d_diag_ff, (size_t)op->basis->n * sizeof(float2)));
-    k_diag_precompute<<<grid_for(op->basis->n, 256), 256>>>(op->basis->view(), op->diag, op->d_diag_generic, op->d_diag,
-                                                             op->d_diag_ff);
+    cudaStream_t st = op->stream;
+    QSI_CUDA(cudaMallocAsync(&op->d_diag, (size_t)op->basis->n * sizeof(double), st));
+    QSI_CUDA(cudaMallocAsync(&op->d_diag_ff, (size_t)op->basis->n * sizeof(float2), st));
+    k_diag_precompute<<<grid_for(op->basis->n, 256), 256, 0, st>>>(op->basis->view(), op->diag, op->d_diag_generic,
+                                                                    op->d_diag, op->d_diag_ff);
     QSI_CUDA(cudaGetLastError());
-    QSI_CUDA(cudaDeviceSynchronize());
+    QSI_CUDA(cudaStreamSynchronize(st));
     return QSI_OK;
 }
 

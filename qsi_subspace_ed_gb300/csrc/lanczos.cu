@@ -306,9 +306,9 @@ qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vect
         }
     }
     double *dA = nullptr, *dw = nullptr, *dV = nullptr;
-    QSI_CUDA(cudaMalloc(&dA, Ap.size() * 8));
-    QSI_CUDA(cudaMalloc(&dw, (size_t)n_mat * M * 8));
-    QSI_CUDA(cudaMalloc(&dV, Ap.size() * 8));
+    QSI_CUDA(cudaMallocAsync(&dA, Ap.size() * 8, st));
+    QSI_CUDA(cudaMallocAsync(&dw, (size_t)n_mat * M * 8, st));
+    QSI_CUDA(cudaMallocAsync(&dV, Ap.size() * 8, st));
     QSI_CUDA(cudaMemcpyAsync(dA, Ap.data(), Ap.size() * 8, cudaMemcpyHostToDevice, st));
     size_t smem = (size_t)M * M * 8 + (size_t)M * 8 + (size_t)M * 2 * 4 + (size_t)M * 4 + 64;
     cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -318,9 +318,9 @@ qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vect
     if (e == cudaSuccess) e = cudaMemcpyAsync(wp.data(), dw, wp.size() * 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(Vp.data(), dV, Vp.size() * 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(dA);
-    cudaFree(dw);
-    cudaFree(dV);
+    cudaFreeAsync(dA, st);
+    cudaFreeAsync(dw, st);
+    cudaFreeAsync(dV, st);
     if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "jacobi: %s", cudaGetErrorString(e));
     w.assign((size_t)n_mat * m, 0.0);
     V.assign((size_t)n_mat * m * m, 0.0);
@@ -342,14 +342,14 @@ struct Vecs {
     qsi_status init(int64_t n_, cudaStream_t s) {
         n = n_;
         st = s;
-        QSI_CUDA(cudaMalloc(&partial, (size_t)kRedGrid * 257 * 8));
-        QSI_CUDA(cudaMalloc(&red, 257 * 8));
+        QSI_CUDA(cudaMallocAsync(&partial, (size_t)kRedGrid * 257 * 8, st));
+        QSI_CUDA(cudaMallocAsync(&red, 257 * 8, st));
         hred.resize(257);
         return QSI_OK;
     }
     ~Vecs() {
-        cudaFree(partial);
-        cudaFree(red);
+        cudaFreeAsync(partial, st);
+        cudaFreeAsync(red, st);
     }
     // h[0..k) = V_i . w and h[k] = |w|^2, copied to host
     template <typename VT>
@@ -383,15 +383,23 @@ qsi_status apply_to_w(qsi_op* op, const VT* v, double* w, cudaStream_t st) {
 
 namespace qsi {
 
+// Device buffer from the stream-ordered allocator of one stream (no device-wide
+// synchronisation on allocation or release, so solves on different streams overlap).
 template <typename T>
 struct DevBuf {
     T* p = nullptr;
     size_t count = 0;
-    cudaError_t alloc(size_t n) {
+    cudaStream_t st = nullptr;
+    cudaError_t alloc(size_t n, cudaStream_t s) {
         count = n;
-        return cudaMalloc(&p, n * sizeof(T));
+        st = s;
+        return cudaMallocAsync(&p, std::max<size_t>(1, n) * sizeof(T), s);
     }
-    ~DevBuf() { cudaFree(p); }
+    void release() {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+    }
+    ~DevBuf() { release(); }
 };
 
 // Orthonormalises the FP64 block X (k vectors of length n, vector-major) with
@@ -442,7 +450,7 @@ static qsi_status rayleigh_ritz(Vecs& vx, const double* S, const double* HS, int
     for (int i = 0; i < k; ++i)
         for (int j = 0; j < keep; ++j) Yk[(size_t)i * keep + j] = Y[(size_t)i * k + j];
     DevBuf<double> dY;
-    QSI_CUDA(dY.alloc(Yk.size()));
+    QSI_CUDA(dY.alloc(Yk.size(), st));
     QSI_CUDA(cudaMemcpyAsync(dY.p, Yk.data(), Yk.size() * 8, cudaMemcpyHostToDevice, st));
     size_t smem = Yk.size() * 8;
     k_ritz_vectors<double><<<grid_for(n, 128), 128, smem, st>>>(S, n, k, keep, dY.p, X, n);
@@ -476,9 +484,9 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     if (s) return s;
     DevBuf<VT> V;
     DevBuf<double> w, dY;
-    QSI_CUDA(V.alloc((size_t)(m + 1) * n));
-    QSI_CUDA(w.alloc((size_t)n));
-    QSI_CUDA(dY.alloc((size_t)m * m));
+    QSI_CUDA(V.alloc((size_t)(m + 1) * n, st));
+    QSI_CUDA(w.alloc((size_t)n, st));
+    QSI_CUDA(dY.alloc((size_t)m * m, st));
     auto vec = [&](int j) { return V.p + (size_t)j * n; };
     // start vector N(0,1), normalised (stored)
     k_randn<<<grid_for(n, 256), 256, 0, st>>>(w.p, n, cfg.seed, 0);
@@ -573,8 +581,8 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     }
     // Ritz vectors in FP64
     DevBuf<double> X, HX;
-    QSI_CUDA(X.alloc((size_t)nev * n));
-    QSI_CUDA(HX.alloc((size_t)nev * n));
+    QSI_CUDA(X.alloc((size_t)nev * n, st));
+    QSI_CUDA(HX.alloc((size_t)nev * n, st));
     {
         std::vector<double> Yk((size_t)m * nev);
         for (int i = 0; i < m; ++i)
@@ -587,15 +595,14 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     }
     std::vector<double> th(Tw.begin(), Tw.begin() + nev);
     // free the Krylov basis before polishing
-    cudaFree(V.p);
-    V.p = nullptr;
+    V.release();
     // FP64 polish: Rayleigh-Ritz on the Ritz block, then optional residual-augmented rounds
     int rounds = std::max(cfg.polish_steps, sizeof(VT) == 4 ? 1 : 0);
     DevBuf<double> S, HS, dth;
     if (rounds > 0) {
-        QSI_CUDA(S.alloc((size_t)2 * nev * n));
-        QSI_CUDA(HS.alloc((size_t)2 * nev * n));
-        QSI_CUDA(dth.alloc((size_t)nev));
+        QSI_CUDA(S.alloc((size_t)2 * nev * n, st));
+        QSI_CUDA(HS.alloc((size_t)2 * nev * n, st));
+        QSI_CUDA(dth.alloc((size_t)nev, st));
         QSI_CUDA(cudaMemcpyAsync(S.p, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, st));
         s = orthonormalise(vx, S.p, nev, n);
         if (s) return s;
@@ -631,8 +638,8 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     // residual norms ||H x - theta x|| / ||x||
     if (rep) {
         DevBuf<double> R, d2;
-        QSI_CUDA(R.alloc((size_t)nev * n));
-        QSI_CUDA(d2.alloc((size_t)nev));
+        QSI_CUDA(R.alloc((size_t)nev * n, st));
+        QSI_CUDA(d2.alloc((size_t)nev, st));
         QSI_CUDA(cudaMemcpyAsync(d2.p, th.data(), (size_t)nev * 8, cudaMemcpyHostToDevice, st));
         k_residual<<<grid_for(n, 256), 256, 0, st>>>(HX.p, X.p, d2.p, nev, n, R.p);
         for (int i = 0; i < nev && i < 64; ++i) {
@@ -649,7 +656,10 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
         rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     for (int i = 0; i < nev; ++i) evals[i] = th[i];
-    if (evecs && cfg.want_vectors) QSI_CUDA(cudaMemcpy(evecs, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToHost));
+    if (evecs && cfg.want_vectors) {
+        QSI_CUDA(cudaMemcpyAsync(evecs, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+    }
     if (nconv < nev && !(m >= n)) return fail(QSI_NOT_CONVERGED, "lanczos: %d of %d eigenpairs converged after %d restarts", nconv, nev, restarts);
     return QSI_OK;
 }
@@ -782,7 +792,7 @@ static qsi_status lowest_of_tridiag(const std::vector<double>& al, const std::ve
         hi = std::max(hi, al[i] + r);
     }
     DevBuf<double> d;
-    QSI_CUDA(d.alloc((size_t)2 * m + 1));
+    QSI_CUDA(d.alloc((size_t)2 * m + 1, st));
     QSI_CUDA(cudaMemcpyAsync(d.p, al.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
     if (m > 1) QSI_CUDA(cudaMemcpyAsync(d.p + m, be.data(), (size_t)(m - 1) * 8, cudaMemcpyHostToDevice, st));
     k_tridiag_lowest<<<1, 256, 0, st>>>(d.p, d.p + m, m, lo - 1e-12 * std::fabs(lo) - 1e-300, hi, d.p + 2 * m);
@@ -831,8 +841,8 @@ extern "C" qsi_status qsi_eigval0(qsi_op* op, const qsi_eigval0_cfg* cfg, double
         qsi_status s = vx.init(n, st);
         if (s) return s;
         DevBuf<double> v, u, ev;
-        QSI_CUDA(v.alloc(n));
-        QSI_CUDA(u.alloc(n));
+        QSI_CUDA(v.alloc(n, st));
+        QSI_CUDA(u.alloc(n, st));
         std::vector<double> alphas, betas, ritz, h;
         double eig = 1e308, e0_pass0 = 0.0;
         int its = 0;
@@ -840,7 +850,7 @@ extern "C" qsi_status qsi_eigval0(qsi_op* op, const qsi_eigval0_cfg* cfg, double
             QSI_CUDA(cudaMemcpyAsync(v.p, v0.data(), (size_t)n * 8, cudaMemcpyHostToDevice, st));
             QSI_CUDA(cudaMemsetAsync(u.p, 0, (size_t)n * 8, st));
             if (pass == 1) {
-                QSI_CUDA(ev.alloc(n));
+                QSI_CUDA(ev.alloc(n, st));
                 QSI_CUDA(cudaMemsetAsync(ev.p, 0, (size_t)n * 8, st));
             }
             std::vector<double> al, be;
@@ -888,9 +898,9 @@ extern "C" qsi_status qsi_eigval0(qsi_op* op, const qsi_eigval0_cfg* cfg, double
                 if (cfg->calc_eigenvector) {
                     const int m = (int)al.size();
                     DevBuf<double> d, work, y;
-                    QSI_CUDA(d.alloc((size_t)2 * m));
-                    QSI_CUDA(work.alloc((size_t)5 * m + 8));
-                    QSI_CUDA(y.alloc((size_t)m));
+                    QSI_CUDA(d.alloc((size_t)2 * m, st));
+                    QSI_CUDA(work.alloc((size_t)5 * m + 8, st));
+                    QSI_CUDA(y.alloc((size_t)m, st));
                     QSI_CUDA(cudaMemcpyAsync(d.p, al.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
                     if (m > 1) QSI_CUDA(cudaMemcpyAsync(d.p + m, b2.data(), (size_t)(m - 1) * 8, cudaMemcpyHostToDevice, st));
                     k_tridiag_vector<<<1, 32, 0, st>>>(d.p, d.p + m, m, eig, work.p, y.p);
@@ -903,7 +913,8 @@ extern "C" qsi_status qsi_eigval0(qsi_op* op, const qsi_eigval0_cfg* cfg, double
         *e0 = e0_pass0;
         if (iterations) *iterations = its;
         if (cfg->calc_eigenvector && eigvec) {
-            QSI_CUDA(cudaMemcpy(eigvec, ev.p, (size_t)n * 8, cudaMemcpyDeviceToHost));
+            QSI_CUDA(cudaMemcpyAsync(eigvec, ev.p, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+            QSI_CUDA(cudaStreamSynchronize(st));
         }
         return QSI_OK;
     });
@@ -1001,11 +1012,11 @@ static qsi_status ftlm_sector(qsi_op* op, int R, int M, uint64_t seed, double* a
     if (R <= 0 || R > 256 || (R & (R - 1))) return fail(QSI_INVALID_ARG, "ftlm: R must be a power of two in [1,256]");
     DevBuf<VT> P, C, W;
     DevBuf<double> partial, ab;
-    QSI_CUDA(P.alloc((size_t)n * R));
-    QSI_CUDA(C.alloc((size_t)n * R));
-    QSI_CUDA(W.alloc((size_t)n * R));
-    QSI_CUDA(partial.alloc((size_t)kColGrid * R));
-    QSI_CUDA(ab.alloc((size_t)2 * M * R));
+    QSI_CUDA(P.alloc((size_t)n * R, st));
+    QSI_CUDA(C.alloc((size_t)n * R, st));
+    QSI_CUDA(W.alloc((size_t)n * R, st));
+    QSI_CUDA(partial.alloc((size_t)kColGrid * R, st));
+    QSI_CUDA(ab.alloc((size_t)2 * M * R, st));
     double* dA = ab.p;          // [M][R]
     double* dB = ab.p + M * R;  // [M][R]
     k_ftlm_init<VT><<<grid_for(n * R, 256), 256, 0, st>>>(C.p, P.p, n, R, seed);

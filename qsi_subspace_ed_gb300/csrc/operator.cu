@@ -496,8 +496,9 @@ extern "C" qsi_status qsi_op_destroy(qsi_op* op) {
     cudaFree(op->d_push_diag);
     cudaFree(op->d_diag_generic);
     cudaFree(op->d_lit_off);
-    cudaFree(op->d_diag);
-    cudaFree(op->d_diag_ff);
+    if (op->d_diag) cudaFreeAsync(op->d_diag, op->stream);
+    if (op->d_diag_ff) cudaFreeAsync(op->d_diag_ff, op->stream);
+    if (op->stream) cudaStreamSynchronize(op->stream);
     cudaFree(op->d_lits);
     cudaFree(op->d_x);
     cudaFree(op->d_y);

@@ -51,6 +51,8 @@ def parse():
                    help="extra legs after the FP64 headline (also: lanczos = FP64 vs mixed 10-eigenvalue solves)")
     p.add_argument("--nev", type=int, default=10)
     p.add_argument("--serve-n", type=int, default=240)
+    p.add_argument("--ftlm-R", type=int, default=64)
+    p.add_argument("--ftlm-M", type=int, default=100)
     p.add_argument("--serve-rate", type=float, default=40.0)
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--ncv", type=int, default=24)
@@ -173,6 +175,54 @@ def cpu_baseline(w, H, seconds: float):
     return {"value": rows / dt, "unit": "states/s", "cores": threads, "kind": "port",
             "sample": f"push-form apply (per-term OpenMP pass, atomic scatter, binary search) over source rows "
                       f"[0,{rows}) of {n} of {w.name}; {dt:.1f}s"}
+
+
+def ftlm4_leg(args):
+    """Config-4 style FTLM: R Rademacher vectors, M steps, three sectors of uneven dimension advanced together
+    (one apply launch per step for all sectors, the run captured in one CUDA graph), FP32 vectors with FP64
+    recurrence coefficients, against the same run in plain FP64."""
+    import numpy as np
+
+    import qsi_subspace_ed_gb300 as q
+    from qsi_subspace_ed_gb300 import workloads
+
+    l32, l64 = workloads.lattice("pyro_1x2x1"), workloads.lattice("pyro_1x2x2")
+    g, B = workloads.ring_zeeman_params(args.seed, (0.2, 1.0), 0.5)
+    t0 = time.time()
+    secs = [("pyro_1x2x2.n0", l64, q.enumerate_basis_gpu(l64)),
+            ("pyro_1x2x2.n1", l64, q.enumerate_basis(l64, n_spinon_pairs=1)),
+            ("pyro_1x2x1.n2", l32, q.enumerate_basis(l32, n_spinon_pairs=2))]
+    t_enum = time.time() - t0
+    ops = [q.LazyOpSum(q.ZBasis(b), q.build_ring_zeeman(lat, g, B, Jpm=0.05)) for _, lat, b in secs]
+    R, M = args.ftlm_R, args.ftlm_M
+    T = np.logspace(-2, 1, 200)
+    out = {"R": R, "M": M, "Jpm": 0.05, "g": g, "B": B, "sectors": {nm: int(len(b)) for nm, _, b in secs},
+           "enumerate_s": round(t_enum, 2), "note": "the 2-spinon-pair sector is taken on the 32-spin cell "
+           "(its 64-spin basis does not fit R=64 FP32 vectors in memory)"}
+    res = {}
+    for prec in ("mixed", "f64"):
+        q.ftlm(ops, [R] * len(ops), M=3, seed=1, precision=prec)  # warm-up
+        torch_sync()
+        t0 = time.time()
+        res[prec] = q.ftlm(ops, [R] * len(ops), M=M, seed=1, precision=prec)
+        dt = time.time() - t0
+        out[prec] = {"seconds": dt, "vec_steps_per_s": len(ops) * R * M / dt,
+                     "state_vector_steps_per_s": sum(len(b) for _, _, b in secs) * R * M / dt}
+    out["speedup_mixed_vs_f64"] = out["f64"]["seconds"] / out["mixed"]["seconds"]
+    errs = {}
+    for k, (nm, _, b) in enumerate(secs):
+        th32 = q.ftlm_thermo(*res["mixed"][k], len(b), T)
+        th64 = q.ftlm_thermo(*res["f64"][k], len(b), T)
+        errs[nm] = {"max_abs_dC": float(np.abs(th32["C"] - th64["C"]).max()),
+                    "max_C": float(np.abs(th64["C"]).max()), "e_ref_diff": abs(th32["e_ref"] - th64["e_ref"])}
+    out["mixed_vs_f64"] = errs
+    return out
+
+
+def torch_sync():
+    import torch
+
+    torch.cuda.synchronize()
 
 
 def serve_leg(args):
@@ -383,6 +433,8 @@ def run_ours(args):
         out["levels_compared"] = int(len(err))
         out["speedup_mixed_vs_f64"] = out["f64"]["seconds"] / out["mixed"]["seconds"]
         line["lanczos"] = out
+    if "ftlm4" in legs and rank == 0:
+        line["ftlm_config4"] = ftlm4_leg(args)
     if "serve" in legs and rank == 0:
         line["serve"] = serve_leg(args)
     if "cpu" in legs and rank == 0:

@@ -14,6 +14,8 @@
 // the tile into a shared-memory hit list; then the warp walks the list row
 // by row and gathers each column's R values with coalesced loads.
 #include <algorithm>
+#include <cmath>
+#include <vector>
 #include <type_traits>
 
 #include "qsi_device.cuh"
@@ -175,10 +177,11 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, cons
     }
 }
 
+// Body of the batched tile kernel for one block (block_id of n_blocks working on this operator).
 template <typename XT, class LK, bool kFF, int KM>
-__global__ void __launch_bounds__(256, 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
-                                                            XT* __restrict__ y, int R, int accumulate, int cap) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, const XT* __restrict__ x,
+                                             XT* __restrict__ y, int R, int accumulate, int cap, int64_t block_id,
+                                             int64_t n_blocks, unsigned char* smem_raw) {
     const TileSmem S = stage_terms(P, smem_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int n_rounds = (P.n_off + 31) >> 5;
@@ -191,7 +194,7 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile_batched(TileParams P, LK 
     uint32_t* hJ = reinterpret_cast<uint32_t*>(hc + cap);
     // KM columns per lane per pass: 32*KM vectors per pass
     const int64_t ntiles = (P.B.n + 31) >> 5;
-    for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
+    for (int64_t tile = block_id * nw + wid; tile < ntiles; tile += n_blocks * nw) {
         const int64_t row = tile * 32 + lane;
         const bool valid = row < P.B.n;
         const state2 s = valid ? P.B.states[row] : make_ulonglong2(0, 0);
@@ -379,6 +382,43 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile_batched(TileParams P, LK 
     }
 }
 
+template <typename XT, class LK, bool kFF, int KM>
+__global__ void __launch_bounds__(256, 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
+                                                            XT* __restrict__ y, int R, int accumulate, int cap) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    batched_body<XT, LK, kFF, KM>(P, lk, x, y, R, accumulate, cap, blockIdx.x, gridDim.x, smem_raw);
+}
+
+// Several operators (sectors) in one launch: the grid is partitioned into
+// per-sector block ranges in proportion to each sector's rows x vectors;
+// each block stages its own sector's terms and works through that sector's
+// tiles.  FP32 storage, double-float accumulation, hash lookups.
+struct SectorLaunch {
+    TileParams P;
+    HashView H;
+    const float* x;
+    float* y;
+    int R;
+    int cap;
+    int block_begin;
+    int n_blocks;
+};
+
+template <int KM>
+__global__ void __launch_bounds__(256, 3) k_apply_sectors(const SectorLaunch* __restrict__ secs, int n_secs,
+                                                          int accumulate) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ SectorLaunch L;
+    if (threadIdx.x == 0) {
+        int s = 0;
+        while (s + 1 < n_secs && (int)blockIdx.x >= secs[s + 1].block_begin) ++s;
+        L = secs[s];
+    }
+    __syncthreads();
+    batched_body<float, LookupHash, true, KM>(L.P, LookupHash{L.H}, L.x, L.y, L.R, accumulate, L.cap,
+                                              (int64_t)blockIdx.x - L.block_begin, L.n_blocks, smem_raw);
+}
+
 // Per-row diagonal, evaluated once per operator with the same arithmetic as
 // diag_value in the row kernels.
 __global__ void k_diag_precompute(BasisView B, DiagSpec D, const PushTerm* __restrict__ dgen, double* __restrict__ out,
@@ -522,6 +562,72 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
     if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "tile apply launch: %s", cudaGetErrorString(e));
     return QSI_OK;
 }
+
+// Several sectors in one launch (FP32 batched, double-float, hash lookups), in two steps: plan_sectors builds
+// the per-sector launch records on the host (block ranges in proportion to rows x vectors, shared memory for
+// the largest sector); the caller copies plan.records to device memory once, and launch_sectors enqueues the
+// kernel (capturable into a CUDA graph: it does no host-to-device copy).
+qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
+                        SectorPlan& plan) {
+    std::vector<SectorLaunch> L(n);
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int nw = 8;
+    size_t smem = 0;
+    int maxR = 1;
+    double work_total = 0;
+    for (int s = 0; s < n; ++s) {
+        qsi_op* op = ops[s];
+        if (!op->basis->d_hash || op->kernel != 1)
+            return fail(QSI_INVALID_ARG, "sector launch needs tile kernels and a hash index");
+        const int cap = (std::max(op->list_cap, op->n_pull) + 7) & ~7;
+        const int n_rounds = (op->n_pull + 31) / 32;
+        smem = std::max(smem, term_smem(op) + (size_t)nw * (512 + (size_t)n_rounds * 128 + (size_t)cap * 12));
+        L[s].P = TileParams{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
+                            op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords};
+        L[s].H = op->basis->hview();
+        L[s].x = X[s];
+        L[s].y = Y[s];
+        L[s].R = R[s];
+        L[s].cap = cap;
+        maxR = std::max(maxR, R[s]);
+        work_total += (double)op->basis->n * R[s];
+    }
+    if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "sector launch: %zu bytes of shared memory needed", smem);
+    const int total = sms * 3;
+    int begin = 0;
+    for (int s = 0; s < n; ++s) {
+        const int64_t tiles = (ops[s]->basis->n + 31) / 32;
+        int b = (int)std::llround(total * ((double)ops[s]->basis->n * R[s]) / std::max(work_total, 1.0));
+        b = (int)std::max<int64_t>(1, std::min<int64_t>(b, (tiles + nw - 1) / nw));
+        L[s].block_begin = begin;
+        L[s].n_blocks = b;
+        begin += b;
+    }
+    plan.records.assign((const unsigned char*)L.data(), (const unsigned char*)(L.data() + n));
+    plan.smem = smem;
+    plan.maxR = maxR;
+    plan.grid = begin;
+    plan.n = n;
+    return QSI_OK;
+}
+
+qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int accumulate, cudaStream_t st) {
+    auto go = [&](auto km) {
+        constexpr int KM = decltype(km)::value;
+        auto k = k_apply_sectors<KM>;
+        set_smem(k, plan.smem);
+        k<<<plan.grid, 256, plan.smem, st>>>((const SectorLaunch*)d_records, plan.n, accumulate);
+    };
+    if (plan.maxR <= 32) go(std::integral_constant<int, 1>{});
+    else if (plan.maxR <= 64) go(std::integral_constant<int, 2>{});
+    else go(std::integral_constant<int, 4>{});
+    QSI_CUDA(cudaGetLastError());
+    return QSI_OK;
+}
+
+size_t sector_launch_bytes() { return sizeof(SectorLaunch); }
 
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
                               cudaStream_t st) {

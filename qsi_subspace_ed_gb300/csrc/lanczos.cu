@@ -937,22 +937,45 @@ __global__ void k_ftlm_init(VT* __restrict__ cur, VT* __restrict__ prev, int64_t
     }
 }
 
-// Column dot products over [row][R] data: partial[b*R + r] = sum_i a[i][r] b[i][r].
-template <typename VT, typename WT>
-__global__ void __launch_bounds__(256) k_col_dots(const VT* __restrict__ a, const WT* __restrict__ b, int64_t n, int R,
+// Double-float helpers for the FP32 recurrences: error-free products of FP32
+// values and FP64 coefficients split into (hi, lo) floats.
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ void f2_fma(F2& a, float ch, float cl, float x) {
+    const float p = ch * x;
+    const float e = fmaf(ch, x, -p) + cl * x;
+    const float s = a.hi + p;
+    const float bb = s - a.hi;
+    const float err = (a.hi - (s - bb)) + (p - bb);
+    a.hi = s;
+    a.lo += err + e;
+}
+__device__ __forceinline__ double f2_value(const F2& a) { return (double)a.hi + (double)a.lo; }
+
+// Per-column partial sums over one block's rows of a[i][r] * b[i][r]: FP64 for
+// FP64 storage, double-float for FP32 storage.
+template <typename VT>
+__global__ void __launch_bounds__(256) k_col_dots(const VT* __restrict__ a, const VT* __restrict__ b, int64_t n, int R,
                                                   double* __restrict__ partial) {
     extern __shared__ double sh[];  // blockDim.x
     const int rows_per_pass = blockDim.x / R;  // R divides blockDim (R <= 256, power of two)
     const int r = threadIdx.x % R, sub = threadIdx.x / R;
     const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
     const int64_t i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
-    double acc = 0.0;
-    for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) acc += (double)a[i * R + r] * (double)b[i * R + r];
-    sh[threadIdx.x] = acc;
+    double accd = 0.0;
+    if constexpr (sizeof(VT) == 4) {
+        F2 acc{0.f, 0.f};
+        for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) f2_fma(acc, (float)a[i * R + r], 0.f, (float)b[i * R + r]);
+        accd = f2_value(acc);
+    } else {
+        for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) accd += (double)a[i * R + r] * (double)b[i * R + r];
+    }
+    sh[threadIdx.x] = accd;
     __syncthreads();
     if (sub == 0) {
         double t = 0.0;
-        for (int s = 0; s < rows_per_pass; ++s) t += sh[s * R + r];
+        for (int q = 0; q < rows_per_pass; ++q) t += sh[q * R + r];
         partial[(int64_t)blockIdx.x * R + r] = t;
     }
 }
@@ -966,10 +989,10 @@ __global__ void k_col_reduce(const double* __restrict__ partial, int nblocks, in
     }
 }
 
-// prev <- w - alpha cur - beta_prev prev (per column), partial column sums of its square.
-template <typename VT, typename WT>
+// prev <- w - alpha cur - beta_prev prev (per column), with partial column sums of its square.
+template <typename VT>
 __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, const VT* __restrict__ cur,
-                                                     const WT* __restrict__ w, const double* __restrict__ alpha,
+                                                     const VT* __restrict__ w, const double* __restrict__ alpha,
                                                      const double* __restrict__ beta_prev, int64_t n, int R,
                                                      double* __restrict__ partial) {
     extern __shared__ double sh[];
@@ -978,71 +1001,144 @@ __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, cons
     const double a = alpha[r], b = beta_prev ? beta_prev[r] : 0.0;
     const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
     const int64_t i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
-    double acc = 0.0;
-    for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) {
-        const int64_t e = i * R + r;
-        double v = (double)w[e] - a * (double)cur[e] - b * (double)prev[e];
-        prev[e] = (VT)v;
-        acc += v * v;
+    double accd = 0.0;
+    if constexpr (sizeof(VT) == 4) {
+        const float ah = (float)(-a), al = (float)(-a - (double)ah);
+        const float bh = (float)(-b), bl = (float)(-b - (double)bh);
+        F2 nrm{0.f, 0.f};
+        for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) {
+            const int64_t e = i * R + r;
+            F2 v{(float)w[e], 0.f};
+            f2_fma(v, ah, al, (float)cur[e]);
+            f2_fma(v, bh, bl, (float)prev[e]);
+            const float vf = v.hi + v.lo;
+            prev[e] = (VT)vf;
+            f2_fma(nrm, vf, 0.f, vf);
+        }
+        accd = f2_value(nrm);
+    } else {
+        for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) {
+            const int64_t e = i * R + r;
+            double v = (double)w[e] - a * (double)cur[e] - b * (double)prev[e];
+            prev[e] = (VT)v;
+            accd += v * v;
+        }
     }
-    sh[threadIdx.x] = acc;
+    sh[threadIdx.x] = accd;
     __syncthreads();
     if (sub == 0) {
         double t = 0.0;
-        for (int s = 0; s < rows_per_pass; ++s) t += sh[s * R + r];
+        for (int q = 0; q < rows_per_pass; ++q) t += sh[q * R + r];
         partial[(int64_t)blockIdx.x * R + r] = t;
     }
 }
 
+// v /= beta per column (a double-float multiply by 1/beta for FP32 storage).
 template <typename VT>
 __global__ void k_col_scale(VT* __restrict__ v, const double* __restrict__ beta, int64_t n, int R) {
     const int64_t total = n * R;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const double b = beta[e % R];
-        v[e] = (VT)((double)v[e] / (b > 0 ? b : 1.0));
+        const double inv = (b > 0) ? 1.0 / b : 1.0;
+        if constexpr (sizeof(VT) == 4) {
+            const float ih = (float)inv, il = (float)(inv - (double)ih);
+            const float x = (float)v[e];
+            const float p = ih * x;
+            v[e] = (VT)(p + (fmaf(ih, x, -p) + il * x));
+        } else {
+            v[e] = (VT)((double)v[e] * inv);
+        }
     }
 }
 
 constexpr int kColGrid = 512;
 
 template <typename VT>
-static qsi_status ftlm_sector(qsi_op* op, int R, int M, uint64_t seed, double* alphas, double* betas,
-                              cudaStream_t st) {
-    const int64_t n = op->basis->n;
-    if (R <= 0 || R > 256 || (R & (R - 1))) return fail(QSI_INVALID_ARG, "ftlm: R must be a power of two in [1,256]");
+struct FtlmSector {
+    qsi_op* op;
+    int R;
+    int64_t n;
     DevBuf<VT> P, C, W;
     DevBuf<double> partial, ab;
-    QSI_CUDA(P.alloc((size_t)n * R, st));
-    QSI_CUDA(C.alloc((size_t)n * R, st));
-    QSI_CUDA(W.alloc((size_t)n * R, st));
-    QSI_CUDA(partial.alloc((size_t)kColGrid * R, st));
-    QSI_CUDA(ab.alloc((size_t)2 * M * R, st));
-    double* dA = ab.p;          // [M][R]
-    double* dB = ab.p + M * R;  // [M][R]
-    k_ftlm_init<VT><<<grid_for(n * R, 256), 256, 0, st>>>(C.p, P.p, n, R, seed);
-    const int blk = 256;
-    const size_t sh = (size_t)blk * 8;
-    // the whole M-step recurrence is captured into one CUDA graph
+};
+
+// All sectors advance together: per step one apply launch covering every sector
+// (FP32 storage with hash indexes) or one per sector, then the per-sector
+// recurrence kernels.  The whole M-step run is captured into one CUDA graph.
+template <typename VT>
+static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint64_t seed, double* alphas,
+                           double* betas) {
+    cudaStream_t st = ops[0]->stream;
+    std::vector<FtlmSector<VT>> S(ns);
+    bool one_launch = (sizeof(VT) == 4);
+    for (int s = 0; s < ns; ++s) {
+        const int R = Rs[s];
+        if (R <= 0 || R > 256 || (R & (R - 1))) return fail(QSI_INVALID_ARG, "ftlm: R must be a power of two in [1,256]");
+        if (ops[s]->basis->n < 1) return fail(QSI_INVALID_ARG, "ftlm: empty sector");
+        S[s].op = ops[s];
+        S[s].R = R;
+        S[s].n = ops[s]->basis->n;
+        QSI_CUDA(S[s].P.alloc((size_t)S[s].n * R, st));
+        QSI_CUDA(S[s].C.alloc((size_t)S[s].n * R, st));
+        QSI_CUDA(S[s].W.alloc((size_t)S[s].n * R, st));
+        QSI_CUDA(S[s].partial.alloc((size_t)kColGrid * R, st));
+        QSI_CUDA(S[s].ab.alloc((size_t)2 * M * R, st));
+        one_launch = one_launch && ops[s]->basis->d_hash && ops[s]->use_hash && ops[s]->kernel == 1 &&
+                     ops[s]->ff_accumulate;
+        k_ftlm_init<VT><<<grid_for(S[s].n * R, 256), 256, 0, st>>>(S[s].C.p, S[s].P.p, S[s].n, R, seed + (uint64_t)s);
+    }
+    std::vector<VT*> prev(ns), cur(ns);
+    for (int s = 0; s < ns; ++s) prev[s] = S[s].P.p, cur[s] = S[s].C.p;
+    // one-launch plans for even steps (input C) and odd steps (input P), uploaded before capture
+    SectorPlan plan[2];
+    DevBuf<unsigned char> d_plan[2];
+    if (one_launch) {
+        std::vector<qsi_op*> opv(ops, ops + ns);
+        for (int parity = 0; parity < 2; ++parity) {
+            std::vector<const float*> X(ns);
+            std::vector<float*> Y(ns);
+            for (int s = 0; s < ns; ++s) {
+                X[s] = (const float*)(parity ? S[s].P.p : S[s].C.p);
+                Y[s] = (float*)S[s].W.p;
+            }
+            qsi_status ps = plan_sectors(opv.data(), ns, X.data(), Y.data(), Rs, plan[parity]);
+            if (ps != QSI_OK) return ps;
+            QSI_CUDA(d_plan[parity].alloc(plan[parity].records.size(), st));
+            QSI_CUDA(cudaMemcpyAsync(d_plan[parity].p, plan[parity].records.data(), plan[parity].records.size(),
+                                     cudaMemcpyHostToDevice, st));
+        }
+    }
+    QSI_CUDA(cudaStreamSynchronize(st));
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    QSI_CUDA(cudaStreamSynchronize(st));
     QSI_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    VT *prev = P.p, *cur = C.p;
-    qsi_status s = QSI_OK;
-    for (int j = 0; j < M && s == QSI_OK; ++j) {
-        s = launch_apply(op, cur, W.p, R, sizeof(VT) == 4 ? QSI_F32 : QSI_F64, 0, st);
-        k_col_dots<VT, VT><<<kColGrid, blk, sh, st>>>(cur, W.p, n, R, partial.p);
-        k_col_reduce<<<1, 256, 0, st>>>(partial.p, kColGrid, R, dA + (size_t)j * R, 0);
-        k_ftlm_update<VT, VT><<<kColGrid, blk, sh, st>>>(prev, cur, W.p, dA + (size_t)j * R,
-                                                         j ? dB + (size_t)(j - 1) * R : nullptr, n, R, partial.p);
-        k_col_reduce<<<1, 256, 0, st>>>(partial.p, kColGrid, R, dB + (size_t)j * R, 1);
-        k_col_scale<VT><<<grid_for(n * R, 256), 256, 0, st>>>(prev, dB + (size_t)j * R, n, R);
-        std::swap(prev, cur);
+    qsi_status status = QSI_OK;
+    const int blk = 256;
+    const size_t sh = (size_t)blk * 8;
+    for (int j = 0; j < M && status == QSI_OK; ++j) {
+        if (one_launch) {
+            status = launch_sectors(d_plan[j & 1].p, plan[j & 1], 0, st);
+        } else {
+            for (int s = 0; s < ns && status == QSI_OK; ++s)
+                status = launch_apply(ops[s], cur[s], S[s].W.p, S[s].R, sizeof(VT) == 4 ? QSI_F32 : QSI_F64, 0, st);
+        }
+        for (int s = 0; s < ns; ++s) {
+            FtlmSector<VT>& F = S[s];
+            double* dA = F.ab.p;
+            double* dB = F.ab.p + (size_t)M * F.R;
+            k_col_dots<VT><<<kColGrid, blk, sh, st>>>(cur[s], F.W.p, F.n, F.R, F.partial.p);
+            k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dA + (size_t)j * F.R, 0);
+            k_ftlm_update<VT><<<kColGrid, blk, sh, st>>>(prev[s], cur[s], F.W.p, dA + (size_t)j * F.R,
+                                                         j ? dB + (size_t)(j - 1) * F.R : nullptr, F.n, F.R, F.partial.p);
+            k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dB + (size_t)j * F.R, 1);
+            k_col_scale<VT><<<grid_for(F.n * F.R, 256), 256, 0, st>>>(prev[s], dB + (size_t)j * F.R, F.n, F.R);
+            std::swap(prev[s], cur[s]);
+        }
     }
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
-    if (s != QSI_OK) {
+    if (status != QSI_OK) {
         if (graph) cudaGraphDestroy(graph);
-        return s;
+        return status;
     }
     QSI_CUDA(ce);
     QSI_CUDA(cudaGraphInstantiate(&exec, graph, 0));
@@ -1051,13 +1147,19 @@ static qsi_status ftlm_sector(qsi_op* op, int R, int M, uint64_t seed, double* a
     cudaGraphExecDestroy(exec);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "ftlm graph: %s", cudaGetErrorString(e));
-    std::vector<double> h((size_t)2 * M * R);
-    QSI_CUDA(cudaMemcpy(h.data(), ab.p, h.size() * 8, cudaMemcpyDeviceToHost));
-    for (int r = 0; r < R; ++r)
-        for (int j = 0; j < M; ++j) {
-            alphas[(size_t)r * M + j] = h[(size_t)j * R + r];
-            betas[(size_t)r * M + j] = h[(size_t)M * R + (size_t)j * R + r];
-        }
+    size_t off = 0;
+    for (int s = 0; s < ns; ++s) {
+        const int R = S[s].R;
+        std::vector<double> h((size_t)2 * M * R);
+        QSI_CUDA(cudaMemcpyAsync(h.data(), S[s].ab.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+        for (int r = 0; r < R; ++r)
+            for (int j = 0; j < M; ++j) {
+                alphas[off + (size_t)r * M + j] = h[(size_t)j * R + r];
+                betas[off + (size_t)r * M + j] = h[(size_t)M * R + (size_t)j * R + r];
+            }
+        off += (size_t)R * M;
+    }
     return QSI_OK;
 }
 
@@ -1067,17 +1169,11 @@ extern "C" qsi_status qsi_ftlm_run(qsi_op** ops, int32_t n_sectors, const int32_
                                    int32_t precision, double* alphas, double* betas) {
     return guarded([&]() -> qsi_status {
         if (!ops || n_sectors <= 0 || !R || M <= 0 || !alphas || !betas) return fail(QSI_INVALID_ARG, "qsi_ftlm_run: bad argument");
-        size_t off = 0;
-        for (int s = 0; s < n_sectors; ++s) {
+        for (int s = 0; s < n_sectors; ++s)
             if (!ops[s]) return fail(QSI_INVALID_ARG, "qsi_ftlm_run: null operator");
-            uint64_t sseed = seed + (uint64_t)s;  // sector s alone with seed+s gives the same vectors
-            qsi_status st = (precision == QSI_F32)
-                                ? ftlm_sector<float>(ops[s], R[s], M, sseed, alphas + off, betas + off, ops[s]->stream)
-                                : ftlm_sector<double>(ops[s], R[s], M, sseed, alphas + off, betas + off, ops[s]->stream);
-            if (st) return st;
-            off += (size_t)R[s] * M;
-        }
-        return QSI_OK;
+        // sector s uses seed + s, so a sector run alone with seed + s gets the same vectors
+        return (precision == QSI_F32) ? ftlm_run<float>(ops, n_sectors, R, M, seed, alphas, betas)
+                                      : ftlm_run<double>(ops, n_sectors, R, M, seed, alphas, betas);
     });
 }
 

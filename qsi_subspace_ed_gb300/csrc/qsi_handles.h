@@ -53,5 +53,13 @@ qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdt
                               cudaStream_t st);
 qsi_status build_hash(qsi_basis* b);
 qsi_status build_diag(qsi_op* op);
+struct SectorPlan {
+    std::vector<unsigned char> records;  // one launch record per sector, to be copied to device memory
+    size_t smem = 0;
+    int maxR = 1, grid = 0, n = 0;
+};
+qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
+                        SectorPlan& plan);
+qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int accumulate, cudaStream_t st);
 qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vector<double>& w, std::vector<double>& V, cudaStream_t st);
 }  // namespace qsi

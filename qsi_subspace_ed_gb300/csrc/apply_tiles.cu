@@ -47,8 +47,11 @@ __device__ __forceinline__ bool above_tol(double v) {
 }
 __device__ __forceinline__ bool above_tol(float v) {
     const uint32_t m = __float_as_uint(v) & 0x7FFFFFFFu;
-    return m > kTolBitsF32 && m <= 0x7F800000u;
+    return m - (kTolBitsF32 + 1) <= 0x7F800000u - (kTolBitsF32 + 1);  // kTolBitsF32 < m <= inf, one compare
 }
+// v where the tolerance test admits it (or keep is set), else 0: selected, not branched, so the
+// double-float update that follows runs unconditionally (adding 0 leaves the sum unchanged).
+__device__ __forceinline__ float tol_select(float v, bool keep) { return (keep || above_tol(v)) ? v : 0.0f; }
 
 // Double-float accumulator (hi + lo, two FP32 words, ~2^-48 relative):
 // error-free product c*x with c = ch + cl and error-free sum into hi.
@@ -64,7 +67,6 @@ __device__ __forceinline__ void ff_fma(FF& a, float ch, float cl, float x) {
     a.hi = s;
     a.lo += err + e;
 }
-
 // Shared-memory layout common to both tile kernels.
 struct TileSmem {
     PullTerm* terms;
@@ -128,7 +130,9 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, cons
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TileSmem S = stage_terms(P, smem_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t* spinw = reinterpret_cast<uint32_t*>(S.tail) + wid * 128;
+    const int n_rounds = (P.n_off + 31) >> 5;
+    uint32_t* spinw = reinterpret_cast<uint32_t*>(S.tail) + wid * (128 + 32 * n_rounds);
+    uint32_t* adm = spinw + 128;  // admission words of the tile, one per lane and 32-term round
     const int64_t ntiles = (P.B.n + 31) >> 5;
     for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
         const int64_t row = tile * 32 + lane;
@@ -136,38 +140,40 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, cons
         const state2 s = valid ? P.B.states[row] : make_ulonglong2(0, 0);
         const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
         tile_spin_words(s, P.nwords, lane, spinw);
+        for (int r = 0; r < n_rounds; ++r) adm[r * 32 + lane] = tile_admitted(S, P.n_off, r * 32, lane, vmask, spinw);
         double acc = valid ? P.diag[row] * (double)x[row] : 0.0;
-        for (int t0 = 0; t0 < P.n_off; t0 += 32) {
-            uint32_t hits = tile_admitted(S, P.n_off, t0, lane, vmask, spinw);
-            while (hits) {
-                // up to kNB admitted terms at a time: lookups and gathers in flight together,
-                // contributions added in term order
-                constexpr int kNB = 4;
-                int jj[kNB];
-                uint64_t tl[kNB], th[kNB];
-                int64_t J[kNB];
-                int nh = 0;
+        int r = 0;
+        uint32_t a = adm[lane];
+        while (true) {
+            // up to kNB admitted terms at a time (across rounds): lookups and gathers in flight together,
+            // contributions added in term order
+            constexpr int kNB = 4;
+            int tt[kNB];
+            uint64_t tl[kNB], th[kNB];
+            int64_t J[kNB];
+            int nh = 0;
 #pragma unroll
-                for (int u = 0; u < kNB; ++u) {
-                    jj[u] = 0;
-                    tl[u] = th[u] = 0;
-                    if (hits) {
-                        jj[u] = __ffs(hits) - 1;
-                        hits &= hits - 1;
-                        const PullTerm& T = S.terms[t0 + jj[u]];
-                        tl[u] = s.x ^ T.x0;
-                        th[u] = s.y ^ T.x1;
-                        ++nh;
-                    }
+            for (int u = 0; u < kNB; ++u) {
+                tt[u] = 0;
+                tl[u] = th[u] = 0;
+                while (!a && r + 1 < n_rounds) a = adm[++r * 32 + lane];
+                if (a) {
+                    tt[u] = r * 32 + __ffs(a) - 1;
+                    a &= a - 1;
+                    const PullTerm& T = S.terms[tt[u]];
+                    tl[u] = s.x ^ T.x0;
+                    th[u] = s.y ^ T.x1;
+                    ++nh;
                 }
-                lk.template find_batch<kNB>(tl, th, J, nh);
-                XT xv[kNB];
-#pragma unroll
-                for (int u = 0; u < kNB; ++u) xv[u] = (u < nh && J[u] >= 0) ? x[J[u]] : (XT)0;
-#pragma unroll
-                for (int u = 0; u < kNB; ++u)
-                    if (u < nh && J[u] >= 0 && above_tol(xv[u])) acc += term_coeff(S.terms[t0 + jj[u]], s) * (double)xv[u];
             }
+            if (!nh) break;
+            lk.template find_batch<kNB>(tl, th, J, nh);
+            XT xv[kNB];
+#pragma unroll
+            for (int u = 0; u < kNB; ++u) xv[u] = (u < nh && J[u] >= 0) ? x[J[u]] : (XT)0;
+#pragma unroll
+            for (int u = 0; u < kNB; ++u)
+                if (u < nh && J[u] >= 0 && above_tol(xv[u])) acc += term_coeff(S.terms[tt[u]], s) * (double)xv[u];
         }
         if (valid) {
             if (accumulate) acc += (double)y[row];
@@ -175,6 +181,16 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, cons
         }
         __syncwarp();
     }
+}
+
+// KM value selecting 16-byte FP32 gathers (see batched_body), and the bases, vector counts and pointers it
+// takes.  Its hit lists mark the diagonal slot with the top bit of the row index.
+constexpr int kVec4 = 0;
+constexpr uint32_t kDiagSlot = 0x80000000u;
+inline bool vec4_ok(int64_t n, int R, const void* x, const void* y) {
+    return n < (int64_t)kDiagSlot - 1 && R >= 16 && (R & 3) == 0 &&
+           (R <= 128 ? (R & (R - 1)) == 0 : (R & 127) == 0) &&
+           ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
 }
 
 // Body of the batched tile kernel for one block (block_id of n_blocks working on this operator).
@@ -192,7 +208,16 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
     double* hc = reinterpret_cast<double*>(adm + n_rounds * 32);  // coefficients (8-byte aligned)
     float2* hcf = reinterpret_cast<float2*>(hc);                   // the same slots as (hi, lo) floats
     uint32_t* hJ = reinterpret_cast<uint32_t*>(hc + cap);
-    // KM columns per lane per pass: 32*KM vectors per pass
+    // KM == kVec4 (FP32, R accepted by vec4_ok): 16-byte gathers.  A lane owns 4 consecutive vectors,
+    // lpc lanes cover one column's vectors (up to 128 per pass), and the warp's cpw = 32/lpc lane groups
+    // sum cpw rows at once.  Otherwise a lane owns KM vectors and the warp sums one row at a time.
+    constexpr bool v4 = (KM == kVec4);
+    static_assert(!v4 || kFF, "16-byte gathers are for FP32 vectors with double-float accumulation");
+    int lpc = 32, cpw = 1;
+    if constexpr (v4) {
+        lpc = R >= 128 ? 32 : R / 4;
+        cpw = 32 / lpc;
+    }
     const int64_t ntiles = (P.B.n + 31) >> 5;
     for (int64_t tile = block_id * nw + wid; tile < ntiles; tile += n_blocks * nw) {
         const int64_t row = tile * 32 + lane;
@@ -206,11 +231,12 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
             adm[r * 32 + lane] = a;
             cnt += __popc(a);
         }
+        const int pc = v4 ? cnt + 1 : cnt;  // list slots of this row: (the diagonal,) the hits
         const double d = valid ? P.diag[row] : 0.0;
         int row_start = 0;
         while (row_start < 32) {
-            // rows [row_start, row_end) whose hits fit the list (at least one row; cap >= n_off)
-            int c = (lane >= row_start) ? cnt : 0;
+            // rows [row_start, row_end) whose slots fit the list (at least one row; cap >= a row's slots)
+            int c = (lane >= row_start) ? pc : 0;
             int incl = c;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -223,10 +249,17 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
             int base = incl - c;
             if (in_chunk) {
                 int k = base;
-                for (int r = 0; r < n_rounds; ++r) {
-                    uint32_t a = adm[r * 32 + lane];
-                    while (a) {
-                        constexpr int kNB = 4;
+                if constexpr (v4) {  // the diagonal leads the row's list (gathered like a hit, no tolerance test)
+                    hJ[k] = valid ? (uint32_t)row | kDiagSlot : kEmpty;
+                    hcf[k] = valid ? P.diag_ff[row] : make_float2(0.f, 0.f);
+                    ++k;
+                }
+                // this row's admitted terms in term order, kNB lookups at a time across the 32-term rounds
+                int r = 0;
+                uint32_t a = adm[lane];
+                while (true) {
+                    {
+                        constexpr int kNB = v4 ? 6 : 4;
                         int tt[kNB];
                         uint64_t tl[kNB], th[kNB];
                         int64_t J[kNB];
@@ -235,6 +268,7 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                         for (int u = 0; u < kNB; ++u) {
                             tt[u] = 0;
                             tl[u] = th[u] = 0;
+                            while (!a && r + 1 < n_rounds) a = adm[++r * 32 + lane];
                             if (a) {
                                 tt[u] = r * 32 + __ffs(a) - 1;
                                 a &= a - 1;
@@ -243,6 +277,7 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                                 ++nh;
                             }
                         }
+                        if (!nh) break;
                         lk.template find_batch<kNB>(tl, th, J, nh);
 #pragma unroll
                         for (int u = 0; u < kNB; ++u) {
@@ -264,13 +299,72 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
             if constexpr (kFF) {
                 // FP32 storage, double-float accumulation, no FP64 instruction.  The chunk's hit list
                 // is walked in order across row boundaries with kU column gathers in flight.
+                static_assert(std::is_same<XT, float>::value, "double-float accumulation is for FP32 vectors");
                 constexpr int kU = 8;
                 const int kbeg = __shfl_sync(0xffffffffu, base, row_start);
                 const int last = row_end - 1;
-                const int kend = __shfl_sync(0xffffffffu, base + cnt, last);
+                const int kend = __shfl_sync(0xffffffffu, base + pc, last);
+                if constexpr (v4) {
+                    // Lane group g (lpc lanes, 4 vectors each) sums rows row_start + g, + g + cpw, ...: each
+                    // group walks its own row's slots, kU column gathers in flight per lane, and the warp
+                    // steps as long as its longest row of the set.
+                    const int g = lane / lpc, rr = 4 * (lane % lpc);
+                    for (int r0 = 0; r0 < R; r0 += 4 * lpc) {
+                        for (int l0 = row_start; l0 < row_end; l0 += cpw) {
+                            const int l = l0 + g;
+                            const bool mine = l < row_end;
+                            const int lsrc = mine ? l : row_end - 1;
+                            const int kb = __shfl_sync(0xffffffffu, base, lsrc);
+                            int nl = __shfl_sync(0xffffffffu, pc, lsrc);
+                            if (!mine) nl = 0;
+                            int steps = nl;
+#pragma unroll
+                            for (int o = 16; o; o >>= 1) steps = max(steps, __shfl_xor_sync(0xffffffffu, steps, o));
+                            FF acc[4];
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) acc[i] = FF{0.f, 0.f};
+                            for (int s0 = 0; s0 < steps; s0 += kU) {
+                                float4 xv[kU];
+                                float2 ck[kU];
+                                uint32_t dg = 0;  // bit u: slot u holds the diagonal
+#pragma unroll
+                                for (int u = 0; u < kU; ++u) {
+                                    const int k = kb + s0 + u;
+                                    const uint32_t J = (s0 + u < nl) ? hJ[k] : kEmpty;
+                                    if (J != kEmpty && (J & kDiagSlot)) dg |= 1u << u;
+                                    ck[u] = (J == kEmpty) ? make_float2(0.f, 0.f) : hcf[k];
+                                    xv[u] = (J == kEmpty) ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                                          : *reinterpret_cast<const float4*>(
+                                                                x + (int64_t)(J & ~kDiagSlot) * R + r0 + rr);
+                                }
+#pragma unroll
+                                for (int u = 0; u < kU; ++u) {
+                                    const bool all = (dg >> u) & 1;
+                                    ff_fma(acc[0], ck[u].x, ck[u].y, tol_select(xv[u].x, all));
+                                    ff_fma(acc[1], ck[u].x, ck[u].y, tol_select(xv[u].y, all));
+                                    ff_fma(acc[2], ck[u].x, ck[u].y, tol_select(xv[u].z, all));
+                                    ff_fma(acc[3], ck[u].x, ck[u].y, tol_select(xv[u].w, all));
+                                }
+                            }
+                            const int64_t rl = tile * 32 + l;
+                            if (mine && rl < P.B.n) {
+                                float4* yp = reinterpret_cast<float4*>(y + rl * R + r0 + rr);
+                                if (accumulate) {
+                                    const float4 yv = *yp;
+                                    ff_fma(acc[0], 1.0f, 0.0f, yv.x);
+                                    ff_fma(acc[1], 1.0f, 0.0f, yv.y);
+                                    ff_fma(acc[2], 1.0f, 0.0f, yv.z);
+                                    ff_fma(acc[3], 1.0f, 0.0f, yv.w);
+                                }
+                                *yp = make_float4(acc[0].hi + acc[0].lo, acc[1].hi + acc[1].lo, acc[2].hi + acc[2].lo,
+                                                  acc[3].hi + acc[3].lo);
+                            }
+                        }
+                    }
+                } else {
                 for (int r0 = 0; r0 < R; r0 += 32 * KM) {
                     int l = row_start;
-                    int lend = __shfl_sync(0xffffffffu, base + cnt, l);
+                    int lend = __shfl_sync(0xffffffffu, base + pc, l);
                     FF acc[KM];
                     auto start_row = [&](int rr_l) {
                         const int64_t rl = tile * 32 + rr_l;
@@ -315,12 +409,11 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                             while (k >= lend) {  // rows whose hits are complete
                                 finish_row(l);
                                 ++l;
-                                lend = __shfl_sync(0xffffffffu, base + cnt, l);
+                                lend = __shfl_sync(0xffffffffu, base + pc, l);
                                 start_row(l);
                             }
 #pragma unroll
-                            for (int m = 0; m < KM; ++m)
-                                if (above_tol(xv[u][m])) ff_fma(acc[m], ck[u].x, ck[u].y, xv[u][m]);
+                            for (int m = 0; m < KM; ++m) ff_fma(acc[m], ck[u].x, ck[u].y, tol_select(xv[u][m], false));
                         }
                     }
                     finish_row(l);
@@ -328,6 +421,7 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                         start_row(l);
                         finish_row(l);
                     }
+                }
                 }
             } else {
             for (int l = row_start; l < row_end; ++l) {
@@ -383,7 +477,7 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
 }
 
 template <typename XT, class LK, bool kFF, int KM>
-__global__ void __launch_bounds__(256, 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
+__global__ void __launch_bounds__(256, KM == kVec4 ? 2 : 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
                                                             XT* __restrict__ y, int R, int accumulate, int cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     batched_body<XT, LK, kFF, KM>(P, lk, x, y, R, accumulate, cap, blockIdx.x, gridDim.x, smem_raw);
@@ -405,7 +499,7 @@ struct SectorLaunch {
 };
 
 template <int KM>
-__global__ void __launch_bounds__(256, 3) k_apply_sectors(const SectorLaunch* __restrict__ secs, int n_secs,
+__global__ void __launch_bounds__(256, KM == kVec4 ? 2 : 3) k_apply_sectors(const SectorLaunch* __restrict__ secs, int n_secs,
                                                           int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SectorLaunch L;
@@ -516,7 +610,7 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (R == 1) {
-        const size_t smem = term_smem(op) + (size_t)nw * 512;
+        const size_t smem = term_smem(op) + (size_t)nw * (512 + (size_t)(op->n_pull + 31) / 32 * 128);
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
         if (xdtype == QSI_F64) {
             auto k = k_apply_tile<double, double, LK>;
@@ -532,7 +626,7 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
             k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, accumulate);
         }
     } else {
-        const int cap = (std::max(op->list_cap, op->n_pull) + 7) & ~7;
+        const int cap = (std::max(op->list_cap, op->n_pull + 1) + 7) & ~7;  // a row: diagonal + terms, padded to 8
         const int n_rounds = (op->n_pull + 31) / 32;
         const size_t per_warp = 512 + (size_t)n_rounds * 128 + (size_t)cap * 12;
         const size_t smem = term_smem(op) + (size_t)nw * per_warp;
@@ -545,7 +639,8 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
                 set_smem(k, smem);
                 k<<<grid, block, smem, st>>>(P, lk, (const double*)x, (double*)y, R, accumulate, cap);
             } else if (op->ff_accumulate) {
-                auto k = k_apply_tile_batched<float, LK, true, KM>;
+                auto k = vec4_ok(P.B.n, R, x, y) ? k_apply_tile_batched<float, LK, true, kVec4>
+                                          : k_apply_tile_batched<float, LK, true, KM>;
                 set_smem(k, smem);
                 k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
             } else {
@@ -570,6 +665,7 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
                         SectorPlan& plan) {
     std::vector<SectorLaunch> L(n);
+    plan.vec4 = true;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -581,7 +677,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         qsi_op* op = ops[s];
         if (!op->basis->d_hash || op->kernel != 1)
             return fail(QSI_INVALID_ARG, "sector launch needs tile kernels and a hash index");
-        const int cap = (std::max(op->list_cap, op->n_pull) + 7) & ~7;
+        const int cap = (std::max(op->list_cap, op->n_pull + 1) + 7) & ~7;  // a row: diagonal + terms, padded to 8
         const int n_rounds = (op->n_pull + 31) / 32;
         smem = std::max(smem, term_smem(op) + (size_t)nw * (512 + (size_t)n_rounds * 128 + (size_t)cap * 12));
         L[s].P = TileParams{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
@@ -592,10 +688,11 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         L[s].R = R[s];
         L[s].cap = cap;
         maxR = std::max(maxR, R[s]);
+        plan.vec4 = plan.vec4 && vec4_ok(op->basis->n, R[s], X[s], Y[s]);
         work_total += (double)op->basis->n * R[s];
     }
     if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "sector launch: %zu bytes of shared memory needed", smem);
-    const int total = sms * 3;
+    const int total = sms * (plan.vec4 ? 2 : 3);  // one wave: the kernels' resident blocks per SM
     int begin = 0;
     for (int s = 0; s < n; ++s) {
         const int64_t tiles = (ops[s]->basis->n + 31) / 32;
@@ -620,7 +717,8 @@ qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int acc
         set_smem(k, plan.smem);
         k<<<plan.grid, 256, plan.smem, st>>>((const SectorLaunch*)d_records, plan.n, accumulate);
     };
-    if (plan.maxR <= 32) go(std::integral_constant<int, 1>{});
+    if (plan.vec4) go(std::integral_constant<int, kVec4>{});
+    else if (plan.maxR <= 32) go(std::integral_constant<int, 1>{});
     else if (plan.maxR <= 64) go(std::integral_constant<int, 2>{});
     else go(std::integral_constant<int, 4>{});
     QSI_CUDA(cudaGetLastError());

@@ -153,8 +153,11 @@ struct LookupHash {
         uint4 e[NB];
 #pragma unroll
         for (int u = 0; u < NB; ++u) {
-            slot[u] = state_mix(lo[u], hi[u]) & H.mask;
-            if (u < n) e[u] = __ldg(reinterpret_cast<const uint4*>(H.slots + slot[u]));
+            slot[u] = 0;
+            if (u < n) {
+                slot[u] = state_mix(lo[u], hi[u]) & H.mask;
+                e[u] = __ldg(reinterpret_cast<const uint4*>(H.slots + slot[u]));
+            }
         }
 #pragma unroll
         for (int u = 0; u < NB; ++u) {

@@ -57,6 +57,7 @@ struct SectorPlan {
     std::vector<unsigned char> records;  // one launch record per sector, to be copied to device memory
     size_t smem = 0;
     int maxR = 1, grid = 0, n = 0;
+    bool vec4 = true;  // every sector's R and vectors take 16-byte gathers
 };
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
                         SectorPlan& plan);

@@ -208,3 +208,43 @@ def test_double_float_accumulation_matches_fp64(built):
     Yacc = Y64.copy()
     op.apply_batched(X, Yacc, accumulate=True)
     np.testing.assert_allclose(Yacc, 2 * Y64, rtol=1e-6, atol=1e-6 * np.abs(Y64).max())
+
+
+@pytest.mark.parametrize("R", [16, 24, 32, 64, 128, 256])
+def test_fp32_batched_widths(built, R):
+    """FP32 batched applies at vector counts that take 16-byte gathers (16..128, multiples of 128) and one that
+    does not (24): each within one FP32 ulp of FP64 accumulation, equal to the oracle's FP64 apply to FP32
+    rounding, and bitwise independent of the hit-list size."""
+    basis, H, b, op = built["ref32_JpmB"]
+    X = np.random.default_rng(R).standard_normal((len(basis), R)).astype(np.float32)
+    Yff, Y64, Ysmall = np.zeros_like(X), np.zeros_like(X), np.zeros_like(X)
+    op.set_kernel(1, 1)
+    op.apply_batched(X, Yff)
+    op.set_kernel(1, 1, list_cap=8)
+    op.apply_batched(X, Ysmall)
+    op.set_kernel(1, 1 | 2)
+    op.apply_batched(X, Y64)
+    op.set_kernel(1, 1)
+    assert np.array_equal(Yff, Ysmall)
+    assert np.all(np.abs(Yff - Y64) <= np.spacing(np.abs(Y64).astype(np.float32)))
+    for col in (0, R - 1):
+        ref = O.apply_port(basis, H.specs(), X[:, col].astype(np.float64))
+        np.testing.assert_allclose(Yff[:, col], ref, rtol=0, atol=4e-6 * np.abs(ref).max())
+
+
+def test_fp32_batched_unaligned_device_vectors(built):
+    """Device vectors that are not 16-byte aligned take the one-column-per-load path: same values to FP32 rounding."""
+    torch = pytest.importorskip("torch")
+    basis, H, b, op = built["ref32_JpmB"]
+    n, R = len(basis), 32
+    X = np.random.default_rng(3).standard_normal((n, R)).astype(np.float32)
+    Y = np.zeros_like(X)
+    op.apply_batched(X, Y)
+    xb = torch.zeros(n * R + 1, dtype=torch.float32, device="cuda")
+    yb = torch.zeros(n * R + 1, dtype=torch.float32, device="cuda")
+    xd, yd = xb[1:].view(n, R), yb[1:].view(n, R)
+    xd.copy_(torch.from_numpy(X))
+    op.apply_batched(xd, yd)
+    torch.cuda.synchronize()
+    Yd = yd.cpu().numpy()
+    assert np.all(np.abs(Yd - Y) <= np.spacing(np.abs(Y)))

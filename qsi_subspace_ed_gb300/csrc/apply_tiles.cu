@@ -599,6 +599,18 @@ static void set_smem(K kernel, size_t smem) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+// Grid of one wave: the blocks that fit on the GPU at once (each works through tiles with a grid stride),
+// at most one block per 8 tiles.
+template <class K>
+static int one_wave(K kernel, int block, size_t smem, int64_t ntiles) {
+    int dev = 0, sms = 148, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + block / 32 - 1) / (block / 32), (int64_t)sms * per_sm));
+}
+
 template <class LK>
 static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int R, int xdtype, int ydtype,
                                   int accumulate, cudaStream_t st) {
@@ -606,11 +618,12 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
                  op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords};
     const int block = 256, nw = block / 32;
     const int64_t ntiles = (P.B.n + 31) / 32;
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (R == 1) {
+        // several waves of blocks: measured faster than one wave for the single-vector kernel
         const size_t smem = term_smem(op) + (size_t)nw * (512 + (size_t)(op->n_pull + 31) / 32 * 128);
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
         if (xdtype == QSI_F64) {
             auto k = k_apply_tile<double, double, LK>;
@@ -631,22 +644,24 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
         const size_t per_warp = 512 + (size_t)n_rounds * 128 + (size_t)cap * 12;
         const size_t smem = term_smem(op) + (size_t)nw * per_warp;
         if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "batched apply: %zu bytes of shared memory needed", smem);
-        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
         auto go = [&](auto km) -> void {
             constexpr int KM = decltype(km)::value;
             if (xdtype == QSI_F64) {
                 auto k = k_apply_tile_batched<double, LK, false, KM>;
                 set_smem(k, smem);
-                k<<<grid, block, smem, st>>>(P, lk, (const double*)x, (double*)y, R, accumulate, cap);
+                k<<<one_wave(k, block, smem, ntiles), block, smem, st>>>(P, lk, (const double*)x, (double*)y, R,
+                                                                         accumulate, cap);
             } else if (op->ff_accumulate) {
                 auto k = vec4_ok(P.B.n, R, x, y) ? k_apply_tile_batched<float, LK, true, kVec4>
-                                          : k_apply_tile_batched<float, LK, true, KM>;
+                                                 : k_apply_tile_batched<float, LK, true, KM>;
                 set_smem(k, smem);
-                k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
+                k<<<one_wave(k, block, smem, ntiles), block, smem, st>>>(P, lk, (const float*)x, (float*)y, R,
+                                                                         accumulate, cap);
             } else {
                 auto k = k_apply_tile_batched<float, LK, false, KM>;
                 set_smem(k, smem);
-                k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, R, accumulate, cap);
+                k<<<one_wave(k, block, smem, ntiles), block, smem, st>>>(P, lk, (const float*)x, (float*)y, R,
+                                                                         accumulate, cap);
             }
         };
         if (R <= 32) go(std::integral_constant<int, 1>{});

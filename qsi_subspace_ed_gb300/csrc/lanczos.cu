@@ -953,105 +953,253 @@ __device__ __forceinline__ void f2_fma(F2& a, float ch, float cl, float x) {
 }
 __device__ __forceinline__ double f2_value(const F2& a) { return (double)a.hi + (double)a.lo; }
 
-// Per-column partial sums over one block's rows of a[i][r] * b[i][r]: FP64 for
-// FP64 storage, double-float for FP32 storage.
-template <typename VT>
-__global__ void __launch_bounds__(256) k_col_dots(const VT* __restrict__ a, const VT* __restrict__ b, int64_t n, int R,
-                                                  double* __restrict__ partial) {
-    extern __shared__ double sh[];  // blockDim.x
-    const int rows_per_pass = blockDim.x / R;  // R divides blockDim (R <= 256, power of two)
-    const int r = threadIdx.x % R, sub = threadIdx.x / R;
-    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-    const int64_t i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
-    double accd = 0.0;
-    if constexpr (sizeof(VT) == 4) {
-        F2 acc{0.f, 0.f};
-        for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) f2_fma(acc, (float)a[i * R + r], 0.f, (float)b[i * R + r]);
-        accd = f2_value(acc);
+// VW consecutive elements of a row-major [n][R] array in registers, moved with one 16-byte access when
+// VW > 1 (R is a multiple of VW and the arrays are 16-byte aligned).
+template <typename VT, int VW>
+__device__ __forceinline__ void load_vec(const VT* __restrict__ p, VT (&v)[VW]) {
+    if constexpr (VW == 1) {
+        v[0] = *p;
+    } else if constexpr (sizeof(VT) == 4 && VW == 4) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
     } else {
-        for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) accd += (double)a[i * R + r] * (double)b[i * R + r];
+        static_assert(sizeof(VT) == 8 && VW == 2, "16-byte vectors");
+        const double2 t = *reinterpret_cast<const double2*>(p);
+        v[0] = t.x, v[1] = t.y;
     }
-    sh[threadIdx.x] = accd;
-    __syncthreads();
-    if (sub == 0) {
-        double t = 0.0;
-        for (int q = 0; q < rows_per_pass; ++q) t += sh[q * R + r];
-        partial[(int64_t)blockIdx.x * R + r] = t;
+}
+template <typename VT, int VW>
+__device__ __forceinline__ void store_vec(VT* __restrict__ p, const VT (&v)[VW]) {
+    if constexpr (VW == 1) {
+        *p = v[0];
+    } else if constexpr (sizeof(VT) == 4 && VW == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+        *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
     }
 }
 
+// Layout of the column kernels: a thread owns VW consecutive columns of a row, R/VW threads cover a row,
+// a block takes blockDim*VW/R rows per pass over its contiguous chunk of rows, kColUnroll passes at a
+// time (their loads in flight together).  Per-column block sums are formed in a fixed order.
+constexpr int kColUnroll = 4;
+struct ColLayout {
+    int lpr, rpp, c0, sub;
+    int64_t i0, i1;
+    template <int VW>
+    __device__ static ColLayout make(int64_t n, int R) {
+        ColLayout L;
+        L.lpr = R / VW;
+        L.rpp = blockDim.x / L.lpr;
+        L.c0 = (threadIdx.x % L.lpr) * VW;
+        L.sub = threadIdx.x / L.lpr;
+        const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+        L.i0 = blockIdx.x * chunk;
+        L.i1 = min(n, L.i0 + chunk);
+        return L;
+    }
+};
+
+// partial[block][c] = sum over the block's threads of res (VW columns per thread), in sub order.
+template <int VW>
+__device__ __forceinline__ void col_block_sum(const ColLayout& L, const double (&res)[VW], int R, double* sh,
+                                              double* __restrict__ partial) {
+#pragma unroll
+    for (int k = 0; k < VW; ++k) sh[L.sub * R + L.c0 + k] = res[k];
+    __syncthreads();
+    for (int c = threadIdx.x; c < R; c += blockDim.x) {
+        double t = 0.0;
+        for (int q = 0; q < L.rpp; ++q) t += sh[q * R + c];
+        partial[(int64_t)blockIdx.x * R + c] = t;
+    }
+}
+
+// Per-column partial sums over one block's rows of a[i][r] * b[i][r]: FP64 for
+// FP64 storage, double-float for FP32 storage.
+template <typename VT, int VW>
+__global__ void __launch_bounds__(256) k_col_dots(const VT* __restrict__ a, const VT* __restrict__ b, int64_t n, int R,
+                                                  double* __restrict__ partial) {
+    __shared__ double sh[256 * VW];
+    const ColLayout L = ColLayout::make<VW>(n, R);
+    double res[VW];
+    if constexpr (sizeof(VT) == 4) {
+        F2 acc[VW];
+#pragma unroll
+        for (int k = 0; k < VW; ++k) acc[k] = F2{0.f, 0.f};
+        for (int64_t i = L.i0 + L.sub; i < L.i1; i += (int64_t)L.rpp * kColUnroll) {
+            VT av[kColUnroll][VW], bv[kColUnroll][VW];
+#pragma unroll
+            for (int u = 0; u < kColUnroll; ++u) {
+                const int64_t ii = i + (int64_t)u * L.rpp;
+                if (ii < L.i1) {
+                    load_vec<VT, VW>(a + ii * R + L.c0, av[u]);
+                    load_vec<VT, VW>(b + ii * R + L.c0, bv[u]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < VW; ++k) av[u][k] = bv[u][k] = (VT)0;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kColUnroll; ++u)
+#pragma unroll
+                for (int k = 0; k < VW; ++k) f2_fma(acc[k], (float)av[u][k], 0.f, (float)bv[u][k]);
+        }
+#pragma unroll
+        for (int k = 0; k < VW; ++k) res[k] = f2_value(acc[k]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < VW; ++k) res[k] = 0.0;
+        for (int64_t i = L.i0 + L.sub; i < L.i1; i += (int64_t)L.rpp * kColUnroll) {
+            VT av[kColUnroll][VW], bv[kColUnroll][VW];
+#pragma unroll
+            for (int u = 0; u < kColUnroll; ++u) {
+                const int64_t ii = i + (int64_t)u * L.rpp;
+                if (ii < L.i1) {
+                    load_vec<VT, VW>(a + ii * R + L.c0, av[u]);
+                    load_vec<VT, VW>(b + ii * R + L.c0, bv[u]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < VW; ++k) av[u][k] = bv[u][k] = (VT)0;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kColUnroll; ++u)
+#pragma unroll
+                for (int k = 0; k < VW; ++k) res[k] += (double)av[u][k] * (double)bv[u][k];
+        }
+    }
+    col_block_sum<VW>(L, res, R, sh, partial);
+}
+
+// out[r] = sum over blocks of partial[b][r] (its square root with sqrt_out, and then also the column's
+// scale 1/out[r] for k_col_scale: FP64 and as a (hi, lo) float pair).
 __global__ void k_col_reduce(const double* __restrict__ partial, int nblocks, int R, double* __restrict__ out,
-                             int sqrt_out) {
+                             int sqrt_out, double* __restrict__ inv = nullptr, float2* __restrict__ inv_ff = nullptr) {
     for (int r = threadIdx.x; r < R; r += blockDim.x) {
         double t = 0.0;
         for (int b = 0; b < nblocks; ++b) t += partial[(int64_t)b * R + r];
         out[r] = sqrt_out ? sqrt(t) : t;
+        if (inv) {
+            const double v = out[r] > 0 ? 1.0 / out[r] : 1.0;
+            const float h = (float)v;
+            inv[r] = v;
+            inv_ff[r] = make_float2(h, (float)(v - (double)h));
+        }
     }
 }
 
 // prev <- w - alpha cur - beta_prev prev (per column), with partial column sums of its square.
-template <typename VT>
+template <typename VT, int VW>
 __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, const VT* __restrict__ cur,
                                                      const VT* __restrict__ w, const double* __restrict__ alpha,
                                                      const double* __restrict__ beta_prev, int64_t n, int R,
                                                      double* __restrict__ partial) {
-    extern __shared__ double sh[];
-    const int rows_per_pass = blockDim.x / R;
-    const int r = threadIdx.x % R, sub = threadIdx.x / R;
-    const double a = alpha[r], b = beta_prev ? beta_prev[r] : 0.0;
-    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-    const int64_t i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
-    double accd = 0.0;
+    __shared__ double sh[256 * VW];
+    const ColLayout L = ColLayout::make<VW>(n, R);
+    double a[VW], b[VW], res[VW];
+#pragma unroll
+    for (int k = 0; k < VW; ++k) {
+        a[k] = alpha[L.c0 + k];
+        b[k] = beta_prev ? beta_prev[L.c0 + k] : 0.0;
+    }
     if constexpr (sizeof(VT) == 4) {
-        const float ah = (float)(-a), al = (float)(-a - (double)ah);
-        const float bh = (float)(-b), bl = (float)(-b - (double)bh);
-        F2 nrm{0.f, 0.f};
-        for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) {
-            const int64_t e = i * R + r;
-            F2 v{(float)w[e], 0.f};
-            f2_fma(v, ah, al, (float)cur[e]);
-            f2_fma(v, bh, bl, (float)prev[e]);
-            const float vf = v.hi + v.lo;
-            prev[e] = (VT)vf;
-            f2_fma(nrm, vf, 0.f, vf);
+        float ah[VW], al[VW], bh[VW], bl[VW];
+        F2 nrm[VW];
+#pragma unroll
+        for (int k = 0; k < VW; ++k) {
+            ah[k] = (float)(-a[k]), al[k] = (float)(-a[k] - (double)ah[k]);
+            bh[k] = (float)(-b[k]), bl[k] = (float)(-b[k] - (double)bh[k]);
+            nrm[k] = F2{0.f, 0.f};
         }
-        accd = f2_value(nrm);
+        for (int64_t i = L.i0 + L.sub; i < L.i1; i += (int64_t)L.rpp * kColUnroll) {
+            VT wv[kColUnroll][VW], cv[kColUnroll][VW], pv[kColUnroll][VW];
+#pragma unroll
+            for (int u = 0; u < kColUnroll; ++u) {
+                const int64_t ii = i + (int64_t)u * L.rpp;
+                if (ii < L.i1) {
+                    load_vec<VT, VW>(w + ii * R + L.c0, wv[u]);
+                    load_vec<VT, VW>(cur + ii * R + L.c0, cv[u]);
+                    load_vec<VT, VW>(prev + ii * R + L.c0, pv[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kColUnroll; ++u) {
+                const int64_t ii = i + (int64_t)u * L.rpp;
+                if (ii >= L.i1) continue;
+                VT out[VW];
+#pragma unroll
+                for (int k = 0; k < VW; ++k) {
+                    F2 v{(float)wv[u][k], 0.f};
+                    f2_fma(v, ah[k], al[k], (float)cv[u][k]);
+                    f2_fma(v, bh[k], bl[k], (float)pv[u][k]);
+                    const float vf = v.hi + v.lo;
+                    out[k] = (VT)vf;
+                    f2_fma(nrm[k], vf, 0.f, vf);
+                }
+                store_vec<VT, VW>(prev + ii * R + L.c0, out);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < VW; ++k) res[k] = f2_value(nrm[k]);
     } else {
-        for (int64_t i = i0 + sub; i < i1; i += rows_per_pass) {
-            const int64_t e = i * R + r;
-            double v = (double)w[e] - a * (double)cur[e] - b * (double)prev[e];
-            prev[e] = (VT)v;
-            accd += v * v;
+#pragma unroll
+        for (int k = 0; k < VW; ++k) res[k] = 0.0;
+        for (int64_t i = L.i0 + L.sub; i < L.i1; i += (int64_t)L.rpp * kColUnroll) {
+            VT wv[kColUnroll][VW], cv[kColUnroll][VW], pv[kColUnroll][VW];
+#pragma unroll
+            for (int u = 0; u < kColUnroll; ++u) {
+                const int64_t ii = i + (int64_t)u * L.rpp;
+                if (ii < L.i1) {
+                    load_vec<VT, VW>(w + ii * R + L.c0, wv[u]);
+                    load_vec<VT, VW>(cur + ii * R + L.c0, cv[u]);
+                    load_vec<VT, VW>(prev + ii * R + L.c0, pv[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kColUnroll; ++u) {
+                const int64_t ii = i + (int64_t)u * L.rpp;
+                if (ii >= L.i1) continue;
+                VT out[VW];
+#pragma unroll
+                for (int k = 0; k < VW; ++k) {
+                    const double v = (double)wv[u][k] - a[k] * (double)cv[u][k] - b[k] * (double)pv[u][k];
+                    out[k] = (VT)v;
+                    res[k] += v * v;
+                }
+                store_vec<VT, VW>(prev + ii * R + L.c0, out);
+            }
         }
     }
-    sh[threadIdx.x] = accd;
-    __syncthreads();
-    if (sub == 0) {
-        double t = 0.0;
-        for (int q = 0; q < rows_per_pass; ++q) t += sh[q * R + r];
-        partial[(int64_t)blockIdx.x * R + r] = t;
-    }
+    col_block_sum<VW>(L, res, R, sh, partial);
 }
 
-// v /= beta per column (a double-float multiply by 1/beta for FP32 storage).
-template <typename VT>
-__global__ void k_col_scale(VT* __restrict__ v, const double* __restrict__ beta, int64_t n, int R) {
-    const int64_t total = n * R;
+// v *= inv per column (1/beta from k_col_reduce; a double-float multiply for FP32 storage).  R is a
+// power of two.
+template <typename VT, int VW>
+__global__ void k_col_scale(VT* __restrict__ v, const double* __restrict__ inv, const float2* __restrict__ inv_ff,
+                            int64_t n, int R) {
+    const int64_t total = n * R / VW;
+#pragma unroll 4
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const double b = beta[e % R];
-        const double inv = (b > 0) ? 1.0 / b : 1.0;
-        if constexpr (sizeof(VT) == 4) {
-            const float ih = (float)inv, il = (float)(inv - (double)ih);
-            const float x = (float)v[e];
-            const float p = ih * x;
-            v[e] = (VT)(p + (fmaf(ih, x, -p) + il * x));
-        } else {
-            v[e] = (VT)((double)v[e] * inv);
+        const int c0 = (int)(e * VW) & (R - 1);
+        VT x[VW];
+        load_vec<VT, VW>(v + e * VW, x);
+#pragma unroll
+        for (int k = 0; k < VW; ++k) {
+            if constexpr (sizeof(VT) == 4) {
+                const float2 ic = inv_ff[c0 + k];
+                const float xf = (float)x[k];
+                const float p = ic.x * xf;
+                x[k] = (VT)(p + (fmaf(ic.x, xf, -p) + ic.y * xf));
+            } else {
+                x[k] = (VT)((double)x[k] * inv[c0 + k]);
+            }
         }
+        store_vec<VT, VW>(v + e * VW, x);
     }
 }
 
-constexpr int kColGrid = 512;
+constexpr int kColGrid = 1024;
 
 template <typename VT>
 struct FtlmSector {
@@ -1059,7 +1207,8 @@ struct FtlmSector {
     int R;
     int64_t n;
     DevBuf<VT> P, C, W;
-    DevBuf<double> partial, ab;
+    DevBuf<double> partial, ab, inv;
+    DevBuf<float2> inv_ff;
 };
 
 // All sectors advance together: per step one apply launch covering every sector
@@ -1083,6 +1232,8 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
         QSI_CUDA(S[s].W.alloc((size_t)S[s].n * R, st));
         QSI_CUDA(S[s].partial.alloc((size_t)kColGrid * R, st));
         QSI_CUDA(S[s].ab.alloc((size_t)2 * M * R, st));
+        QSI_CUDA(S[s].inv.alloc((size_t)R, st));
+        QSI_CUDA(S[s].inv_ff.alloc((size_t)R, st));
         one_launch = one_launch && ops[s]->basis->d_hash && ops[s]->use_hash && ops[s]->kernel == 1 &&
                      ops[s]->ff_accumulate;
         k_ftlm_init<VT><<<grid_for(S[s].n * R, 256), 256, 0, st>>>(S[s].C.p, S[s].P.p, S[s].n, R, seed + (uint64_t)s);
@@ -1114,7 +1265,6 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
     QSI_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     qsi_status status = QSI_OK;
     const int blk = 256;
-    const size_t sh = (size_t)blk * 8;
     for (int j = 0; j < M && status == QSI_OK; ++j) {
         if (one_launch) {
             status = launch_sectors(d_plan[j & 1].p, plan[j & 1], 0, st);
@@ -1126,12 +1276,21 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
             FtlmSector<VT>& F = S[s];
             double* dA = F.ab.p;
             double* dB = F.ab.p + (size_t)M * F.R;
-            k_col_dots<VT><<<kColGrid, blk, sh, st>>>(cur[s], F.W.p, F.n, F.R, F.partial.p);
-            k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dA + (size_t)j * F.R, 0);
-            k_ftlm_update<VT><<<kColGrid, blk, sh, st>>>(prev[s], cur[s], F.W.p, dA + (size_t)j * F.R,
-                                                         j ? dB + (size_t)(j - 1) * F.R : nullptr, F.n, F.R, F.partial.p);
-            k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dB + (size_t)j * F.R, 1);
-            k_col_scale<VT><<<grid_for(F.n * F.R, 256), 256, 0, st>>>(prev[s], dB + (size_t)j * F.R, F.n, F.R);
+            const double* bprev = j ? dB + (size_t)(j - 1) * F.R : nullptr;
+            auto col_step = [&](auto vw) {
+                constexpr int VW = decltype(vw)::value;
+                k_col_dots<VT, VW><<<kColGrid, blk, 0, st>>>(cur[s], F.W.p, F.n, F.R, F.partial.p);
+                k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dA + (size_t)j * F.R, 0);
+                k_ftlm_update<VT, VW><<<kColGrid, blk, 0, st>>>(prev[s], cur[s], F.W.p, dA + (size_t)j * F.R, bprev,
+                                                                F.n, F.R, F.partial.p);
+                k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dB + (size_t)j * F.R, 1, F.inv.p,
+                                                F.inv_ff.p);
+                k_col_scale<VT, VW><<<grid_for(F.n * F.R / VW, 256), 256, 0, st>>>(prev[s], F.inv.p, F.inv_ff.p,
+                                                                                  F.n, F.R);
+            };
+            constexpr int kVW = 16 / sizeof(VT);  // 16-byte accesses when R allows
+            if (F.R % kVW == 0) col_step(std::integral_constant<int, kVW>{});
+            else col_step(std::integral_constant<int, 1>{});
             std::swap(prev[s], cur[s]);
         }
     }

@@ -50,8 +50,11 @@ __device__ __forceinline__ bool above_tol(float v) {
     return m - (kTolBitsF32 + 1) <= 0x7F800000u - (kTolBitsF32 + 1);  // kTolBitsF32 < m <= inf, one compare
 }
 // v where the tolerance test admits it (or keep is set), else 0: selected, not branched, so the
-// double-float update that follows runs unconditionally (adding 0 leaves the sum unchanged).
-__device__ __forceinline__ float tol_select(float v, bool keep) { return (keep || above_tol(v)) ? v : 0.0f; }
+// double-float update that follows runs unconditionally (adding 0 leaves the sum unchanged).  The float
+// compare |v| > largest-float-below-1e-15 is the same test as above_tol (false for NaN, true for inf).
+__device__ __forceinline__ float tol_select(float v, bool keep) {
+    return (keep || fabsf(v) > __uint_as_float(kTolBitsF32)) ? v : 0.0f;
+}
 
 // Double-float accumulator (hi + lo, two FP32 words, ~2^-48 relative):
 // error-free product c*x with c = ch + cl and error-free sum into hi.
@@ -67,6 +70,54 @@ __device__ __forceinline__ void ff_fma(FF& a, float ch, float cl, float x) {
     a.hi = s;
     a.lo += err + e;
 }
+// Two double-float accumulators held as packed FP32 pairs and updated with the f32x2 instructions of
+// sm_100-family GPUs (one instruction per operation for both): the same operations, in the same order,
+// as ff_fma on each lane of the pair.
+struct FF2 {
+    uint64_t hi, lo;
+};
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 unpk2(uint64_t v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// a += (ch + cl) * x on both lanes; cn = -ch.  q = cn*x = -(ch*x) exactly, so hi - q is hi + p and
+// fma(ch, x, q) is the exact error of the product p = ch*x, as in ff_fma.
+__device__ __forceinline__ void ff2_fma(FF2& a, uint64_t ch, uint64_t cn, uint64_t cl, uint64_t x) {
+    const uint64_t q = mul2(cn, x);
+    const uint64_t e = fma2(cl, x, fma2(ch, x, q));
+    const uint64_t s = sub2(a.hi, q);
+    const uint64_t bb = sub2(s, a.hi);
+    const uint64_t err = sub2(sub2(a.hi, sub2(s, bb)), add2(q, bb));
+    a.hi = s;
+    a.lo = add2(a.lo, add2(err, e));
+}
+
 // Shared-memory layout common to both tile kernels.
 struct TileSmem {
     PullTerm* terms;
@@ -320,9 +371,9 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                             int steps = nl;
 #pragma unroll
                             for (int o = 16; o; o >>= 1) steps = max(steps, __shfl_xor_sync(0xffffffffu, steps, o));
-                            FF acc[4];
+                            FF2 acc[2];  // vectors (0, 1) and (2, 3) of this lane
 #pragma unroll
-                            for (int i = 0; i < 4; ++i) acc[i] = FF{0.f, 0.f};
+                            for (int i = 0; i < 2; ++i) acc[i] = FF2{0, 0};
                             for (int s0 = 0; s0 < steps; s0 += kU) {
                                 float4 xv[kU];
                                 float2 ck[kU];
@@ -340,10 +391,10 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
 #pragma unroll
                                 for (int u = 0; u < kU; ++u) {
                                     const bool all = (dg >> u) & 1;
-                                    ff_fma(acc[0], ck[u].x, ck[u].y, tol_select(xv[u].x, all));
-                                    ff_fma(acc[1], ck[u].x, ck[u].y, tol_select(xv[u].y, all));
-                                    ff_fma(acc[2], ck[u].x, ck[u].y, tol_select(xv[u].z, all));
-                                    ff_fma(acc[3], ck[u].x, ck[u].y, tol_select(xv[u].w, all));
+                                    const uint64_t ch = pk2(ck[u].x, ck[u].x), cn = pk2(-ck[u].x, -ck[u].x),
+                                                   cl = pk2(ck[u].y, ck[u].y);
+                                    ff2_fma(acc[0], ch, cn, cl, pk2(tol_select(xv[u].x, all), tol_select(xv[u].y, all)));
+                                    ff2_fma(acc[1], ch, cn, cl, pk2(tol_select(xv[u].z, all), tol_select(xv[u].w, all)));
                                 }
                             }
                             const int64_t rl = tile * 32 + l;
@@ -351,13 +402,12 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                                 float4* yp = reinterpret_cast<float4*>(y + rl * R + r0 + rr);
                                 if (accumulate) {
                                     const float4 yv = *yp;
-                                    ff_fma(acc[0], 1.0f, 0.0f, yv.x);
-                                    ff_fma(acc[1], 1.0f, 0.0f, yv.y);
-                                    ff_fma(acc[2], 1.0f, 0.0f, yv.z);
-                                    ff_fma(acc[3], 1.0f, 0.0f, yv.w);
+                                    const uint64_t one = pk2(1.0f, 1.0f), mone = pk2(-1.0f, -1.0f), zero = pk2(0.f, 0.f);
+                                    ff2_fma(acc[0], one, mone, zero, pk2(yv.x, yv.y));
+                                    ff2_fma(acc[1], one, mone, zero, pk2(yv.z, yv.w));
                                 }
-                                *yp = make_float4(acc[0].hi + acc[0].lo, acc[1].hi + acc[1].lo, acc[2].hi + acc[2].lo,
-                                                  acc[3].hi + acc[3].lo);
+                                const float2 a = unpk2(add2(acc[0].hi, acc[0].lo)), b = unpk2(add2(acc[1].hi, acc[1].lo));
+                                *yp = make_float4(a.x, a.y, b.x, b.y);
                             }
                         }
                     }

@@ -182,6 +182,30 @@ qsi_status qsi_op_apply_batched(qsi_op* op, const void* X, void* Y, int32_t R,
  * slow on this GPU);
  * list_cap (> 0) sets the per-warp hit-list size of the batched tile kernel. */
 qsi_status qsi_op_set_kernel(qsi_op* op, int32_t kernel, int32_t use_hash, int32_t list_cap);
+/* Launch settings of the tile kernels, kept separately for single-vector
+ * applies (which = 0) and batched applies (which = 1; -1 sets both):
+ * grid_bps = blocks per SM (0 = built-in choice), vec_chunk = vectors per
+ * pass of the FP32 batched kernel (0, 16, 32, 64 or 128; 0 = up to 128).
+ * qsi_op_get_tuning also reports the kernel, use_hash (as qsi_op_set_kernel
+ * takes it) and list_cap of that class.  No counterpart in the reference (its
+ * apply is an OpenMP loop with nothing to tune); results do not depend on
+ * these settings. */
+qsi_status qsi_op_set_tuning(qsi_op* op, int32_t which, int32_t grid_bps, int32_t vec_chunk);
+qsi_status qsi_op_get_tuning(const qsi_op* op, int32_t which, int32_t* kernel, int32_t* use_hash,
+                             int32_t* list_cap, int32_t* grid_bps, int32_t* vec_chunk);
+/* Autotuner: times applies of R vectors of type dtype (x, y device buffers
+ * of dim*R elements, or NULL for scratch the call allocates and frees) and
+ * keeps, for the class of R (single vector or batched), the fastest lookup
+ * structure (with QSI_TUNE_INDEX: the hash index or the bucket table at
+ * several widths; the basis keeps the width chosen), vectors per pass, blocks
+ * per SM and hit-list size, one parameter at a time, best of reps timed
+ * applies each.
+ * report (optional) receives one line per trial.  Results of later applies
+ * are the same for every setting; only their speed changes.  No counterpart
+ * in the reference. */
+enum { QSI_TUNE_INDEX = 1 };
+qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_t R, int32_t dtype,
+                           int32_t flags, int32_t reps, char* report, size_t report_len);
 /* Connectivity export in the order of LazyOpSum::toSparseMatrix
  * (operator_matrix.hpp:79-105): for each basis index j, each off-diagonal
  * term with |c*sign| > tol gives (J, j, c*sign); then (j, j, sum of diagonal

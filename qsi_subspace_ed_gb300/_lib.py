@@ -17,6 +17,7 @@ QSI_OK, QSI_INVALID_ARG, QSI_OOM, QSI_CUDA_ERROR, QSI_NOT_CONVERGED, QSI_TIMEOUT
 STATUS_NAMES = ["OK", "INVALID_ARG", "OOM", "CUDA_ERROR", "NOT_CONVERGED", "TIMEOUT", "IO_ERROR", "NOT_FOUND"]
 QSI_PTR_HOST, QSI_PTR_DEVICE = 0, 1
 QSI_F64, QSI_F32 = 0, 1
+QSI_TUNE_INDEX = 1
 CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
 
 
@@ -108,6 +109,10 @@ SIGNATURES = {
     "qsi_op_apply_static": [_P, _P, _P, _I32],
     "qsi_op_apply_batched": [_P, _P, _P, _I32, _I32, _I32, _I32, _P],
     "qsi_op_set_kernel": [_P, _I32, _I32, _I32],
+    "qsi_op_set_tuning": [_P, _I32, _I32, _I32],
+    "qsi_op_get_tuning": [_P, _I32, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32),
+                          C.POINTER(_I32)],
+    "qsi_op_autotune": [_P, _P, _P, _I32, _I32, _I32, _I32, C.c_char_p, C.c_size_t],
     "qsi_op_triplets": [_P, _D, _P, _P, _P, _I64, C.POINTER(_I64)],
     "qsi_op_count_misses": [_P, C.POINTER(_I64)],
     "qsi_op_connectivity": [_P, C.POINTER(_I64), C.POINTER(_I64)],

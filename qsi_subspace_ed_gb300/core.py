@@ -322,6 +322,31 @@ class LazyOpSum:
         """kernel 0: row per thread / warp per row; 1: bit-sliced 32-row tiles (default)."""
         call("qsi_op_set_kernel", self._h, int(kernel), int(use_hash), int(list_cap))
 
+    def set_tuning(self, grid_bps: int = 0, vec_chunk: int = 0, which: int = -1) -> None:
+        """Blocks per SM of the tile kernels and vectors per pass of the FP32 batched kernel (0 = built-in)
+        for single-vector (which=0), batched (1) or both (-1) applies."""
+        call("qsi_op_set_tuning", self._h, int(which), int(grid_bps), int(vec_chunk))
+
+    def tuning(self, which: int = 0) -> dict:
+        """Launch settings of single-vector (which=0) or batched (1) applies."""
+        v = [C.c_int32() for _ in range(5)]
+        call("qsi_op_get_tuning", self._h, int(which), *[C.byref(a) for a in v])
+        k, h, cap, g, vc = (a.value for a in v)
+        return {"kernel": k, "use_hash": h & 1, "fp64_accumulate": bool(h & 2), "list_cap": cap, "grid_bps": g,
+                "vec_chunk": vc, "bucket_bits": self.basis.index_info()["bucket_bits"]}
+
+    def autotune(self, R: int = 1, dtype: str = "f64", X=None, Y=None, tune_index: bool = False,
+                 reps: int = 2) -> str:
+        """Times applies of R vectors (device tensors X, Y of shape (dim, R) or scratch) and keeps the
+        fastest launch settings; returns the trial log.  Results of applies do not depend on the settings."""
+        buf = C.create_string_buffer(8192)
+        dt = _lib.QSI_F32 if dtype in ("f32", "mixed", "float32") else _lib.QSI_F64
+        xp = C.c_void_p(X.data_ptr()) if X is not None else None
+        yp = C.c_void_p(Y.data_ptr()) if Y is not None else None
+        call("qsi_op_autotune", self._h, xp, yp, int(R), dt, _lib.QSI_TUNE_INDEX if tune_index else 0, int(reps),
+             buf, len(buf))
+        return buf.value.decode()
+
     @staticmethod
     def _kind(a):
         return _lib.QSI_PTR_DEVICE if hasattr(a, "is_cuda") and a.is_cuda else _lib.QSI_PTR_HOST

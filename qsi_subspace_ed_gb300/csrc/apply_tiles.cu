@@ -33,6 +33,7 @@ struct TileParams {
     const double* diag;  // per-row diagonal, precomputed with diag_value
     const float2* diag_ff;  // the same as (hi, lo) float pairs
     int n_off, n_lits, nwords;
+    int vchunk;             // vectors per pass of the 16-byte batched kernel (16, 32, 64 or 128; 0 = 128)
 };
 
 // |x| > 1e-15 (APPLY_TOL, operator_matrix.hpp:113) as integer compares on the
@@ -266,7 +267,8 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
     static_assert(!v4 || kFF, "16-byte gathers are for FP32 vectors with double-float accumulation");
     int lpc = 32, cpw = 1;
     if constexpr (v4) {
-        lpc = R >= 128 ? 32 : R / 4;
+        const int vc = P.vchunk > 0 ? P.vchunk : 128;
+        lpc = (R >= vc ? vc : R) / 4;
         cpw = 32 / lpc;
     }
     const int64_t ntiles = (P.B.n + 31) >> 5;
@@ -649,14 +651,15 @@ static void set_smem(K kernel, size_t smem) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-// Grid of one wave: the blocks that fit on the GPU at once (each works through tiles with a grid stride),
-// at most one block per 8 tiles.
+// Grid of one wave (the blocks that fit on the GPU at once, each working through tiles with a grid
+// stride) or of bps blocks per SM when bps > 0; at most one block per 8 tiles.
 template <class K>
-static int one_wave(K kernel, int block, size_t smem, int64_t ntiles) {
+static int one_wave(K kernel, int block, size_t smem, int64_t ntiles, int bps = 0) {
     int dev = 0, sms = 148, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess || per_sm < 1)
+    if (bps > 0) per_sm = bps;
+    else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     return (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + block / 32 - 1) / (block / 32), (int64_t)sms * per_sm));
 }
@@ -664,8 +667,9 @@ static int one_wave(K kernel, int block, size_t smem, int64_t ntiles) {
 template <class LK>
 static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int R, int xdtype, int ydtype,
                                   int accumulate, cudaStream_t st) {
+    const qsi_tuning& T = op->tune[R > 1];
     TileParams P{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
-                 op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords};
+                 op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords, T.vec_chunk};
     const int block = 256, nw = block / 32;
     const int64_t ntiles = (P.B.n + 31) / 32;
     if (R == 1) {
@@ -674,7 +678,8 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
         int dev = 0, sms = 148;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
+        const int grid = (int)std::max<int64_t>(
+            1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * (T.grid_bps > 0 ? T.grid_bps : 8)));
         if (xdtype == QSI_F64) {
             auto k = k_apply_tile<double, double, LK>;
             set_smem(k, smem);
@@ -689,7 +694,7 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
             k<<<grid, block, smem, st>>>(P, lk, (const float*)x, (float*)y, accumulate);
         }
     } else {
-        const int cap = (std::max(op->list_cap, op->n_pull + 1) + 7) & ~7;  // a row: diagonal + terms, padded to 8
+        const int cap = (std::max(T.list_cap, op->n_pull + 1) + 7) & ~7;  // a row: diagonal + terms, padded to 8
         const int n_rounds = (op->n_pull + 31) / 32;
         const size_t per_warp = 512 + (size_t)n_rounds * 128 + (size_t)cap * 12;
         const size_t smem = term_smem(op) + (size_t)nw * per_warp;
@@ -699,18 +704,18 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
             if (xdtype == QSI_F64) {
                 auto k = k_apply_tile_batched<double, LK, false, KM>;
                 set_smem(k, smem);
-                k<<<one_wave(k, block, smem, ntiles), block, smem, st>>>(P, lk, (const double*)x, (double*)y, R,
+                k<<<one_wave(k, block, smem, ntiles, T.grid_bps), block, smem, st>>>(P, lk, (const double*)x, (double*)y, R,
                                                                          accumulate, cap);
             } else if (op->ff_accumulate) {
                 auto k = vec4_ok(P.B.n, R, x, y) ? k_apply_tile_batched<float, LK, true, kVec4>
                                                  : k_apply_tile_batched<float, LK, true, KM>;
                 set_smem(k, smem);
-                k<<<one_wave(k, block, smem, ntiles), block, smem, st>>>(P, lk, (const float*)x, (float*)y, R,
+                k<<<one_wave(k, block, smem, ntiles, T.grid_bps), block, smem, st>>>(P, lk, (const float*)x, (float*)y, R,
                                                                          accumulate, cap);
             } else {
                 auto k = k_apply_tile_batched<float, LK, false, KM>;
                 set_smem(k, smem);
-                k<<<one_wave(k, block, smem, ntiles), block, smem, st>>>(P, lk, (const float*)x, (float*)y, R,
+                k<<<one_wave(k, block, smem, ntiles, T.grid_bps), block, smem, st>>>(P, lk, (const float*)x, (float*)y, R,
                                                                          accumulate, cap);
             }
         };
@@ -742,11 +747,11 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         qsi_op* op = ops[s];
         if (!op->basis->d_hash || op->kernel != 1)
             return fail(QSI_INVALID_ARG, "sector launch needs tile kernels and a hash index");
-        const int cap = (std::max(op->list_cap, op->n_pull + 1) + 7) & ~7;  // a row: diagonal + terms, padded to 8
+        const int cap = (std::max(op->tune[1].list_cap, op->n_pull + 1) + 7) & ~7;  // a row: diagonal + terms
         const int n_rounds = (op->n_pull + 31) / 32;
         smem = std::max(smem, term_smem(op) + (size_t)nw * (512 + (size_t)n_rounds * 128 + (size_t)cap * 12));
         L[s].P = TileParams{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
-                            op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords};
+                            op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords, op->tune[1].vec_chunk};
         L[s].H = op->basis->hview();
         L[s].x = X[s];
         L[s].y = Y[s];
@@ -794,7 +799,7 @@ size_t sector_launch_bytes() { return sizeof(SectorLaunch); }
 
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
                               cudaStream_t st) {
-    if (op->basis->d_hash && op->use_hash) return launch_tiles_lk(op, LookupHash{op->basis->hview()}, x, y, R, xdtype, ydtype, accumulate, st);
+    if (op->basis->d_hash && op->tune[R > 1].use_hash) return launch_tiles_lk(op, LookupHash{op->basis->hview()}, x, y, R, xdtype, ydtype, accumulate, st);
     return launch_tiles_lk(op, LookupTable{op->basis->view()}, x, y, R, xdtype, ydtype, accumulate, st);
 }
 

@@ -709,8 +709,10 @@ extern "C" qsi_status qsi_basis_info(const qsi_basis* b, int32_t* bucket_bits, i
 extern "C" qsi_status qsi_op_set_kernel(qsi_op* op, int32_t kernel, int32_t use_hash, int32_t list_cap) {
     if (!op || kernel < 0 || kernel > 1 || list_cap < 0) return fail(QSI_INVALID_ARG, "qsi_op_set_kernel: bad argument");
     op->kernel = kernel;
-    op->use_hash = use_hash & 1;
+    for (qsi_tuning& T : op->tune) {
+        T.use_hash = use_hash & 1;
+        if (list_cap > 0) T.list_cap = list_cap;
+    }
     op->ff_accumulate = (use_hash & 2) ? 0 : 1;
-    if (list_cap > 0) op->list_cap = list_cap;
     return QSI_OK;
 }

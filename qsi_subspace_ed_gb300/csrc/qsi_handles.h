@@ -18,6 +18,14 @@ struct qsi_basis {
     qsi::HashView hview() const { return qsi::HashView{d_hash, hash_mask}; }
 };
 
+// Launch settings of one class of applies (single vector, batched).  None of them changes results.
+struct qsi_tuning {
+    int use_hash = 1;    // look columns up through the basis hash index when it exists (else bucket table)
+    int list_cap = 256;  // hit-list entries per warp in the batched tile kernel
+    int grid_bps = 0;    // tile-kernel blocks per SM (0: built-in choice)
+    int vec_chunk = 0;   // vectors per pass of the 16-byte batched kernel (0: up to 128)
+};
+
 struct qsi_op {
     qsi_basis* basis = nullptr;
     qsi::PullTerm* d_pull = nullptr;        // transposed off-diagonal terms (apply)
@@ -33,9 +41,8 @@ struct qsi_op {
     int n_lits = 0;
     int nwords = 4;                 // 32-bit words that hold any basis or term bit
     int kernel = 1;                 // 0 = row-per-thread / warp-per-row, 1 = bit-sliced tiles
-    int list_cap = 256;             // hit-list entries per warp in the batched tile kernel
-    int use_hash = 1;               // look columns up through the basis hash index when it exists
     int ff_accumulate = 1;          // FP32 batched applies accumulate rows in double-float (else FP64)
+    qsi_tuning tune[2];             // [0] single-vector applies, [1] batched applies (R > 1)
     double* d_diag = nullptr;       // per-row diagonal (tile kernels)
     float2* d_diag_ff = nullptr;    // the same as double-float pairs (FP32 batched kernel)
     cudaStream_t stream = nullptr;

@@ -248,3 +248,31 @@ def test_fp32_batched_unaligned_device_vectors(built):
     torch.cuda.synchronize()
     Yd = yd.cpu().numpy()
     assert np.all(np.abs(Yd - Y) <= np.spacing(np.abs(Y)))
+
+
+def test_autotune_keeps_results(built):
+    """The autotuner changes launch settings only: applies before and after are bitwise equal."""
+    basis, H, b, op = built["cfg1"]
+    x = np.random.default_rng(31).standard_normal(len(basis))
+    X = np.random.default_rng(32).standard_normal((len(basis), 64)).astype(np.float32)
+    y0, Y0 = np.zeros_like(x), np.zeros_like(X)
+    op.evaluate(x, y0)
+    op.apply_batched(X, Y0)
+    log1 = op.autotune(R=1, dtype="f64", tune_index=True, reps=1)
+    log64 = op.autotune(R=64, dtype="f32", reps=1)
+    assert "best" in log1 and "vec_chunk" in log64
+    t = op.tuning(1)
+    y1, Y1 = np.zeros_like(x), np.zeros_like(X)
+    op.evaluate(x, y1)
+    op.apply_batched(X, Y1)
+    assert np.array_equal(y0, y1) and np.array_equal(Y0, Y1)
+    for vc in (16, 32, 64):
+        op.set_tuning(t["grid_bps"], vc, which=1)
+        Y2 = np.zeros_like(X)
+        op.apply_batched(X, Y2)
+        assert np.array_equal(Y0, Y2)
+    with pytest.raises(q.QsiError):
+        op.set_tuning(0, 48)
+    op.set_tuning(0, 0)
+    op.set_kernel(1, 1, list_cap=256)
+    b.set_index(use_hash=True, bucket_bits=0)

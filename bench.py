@@ -43,7 +43,9 @@ def parse():
     p.add_argument("--lattice", default="pyro_1x2x3", help="pyro_1x2x1 | pyro_1x2x2 | pyro_1x2x3")
     p.add_argument("--full-basis", action="store_true", help="all Q=0 states instead of the equal sector")
     p.add_argument("--sector", default="", help="comma-separated sublattice up-counts (default: equal sector)")
-    p.add_argument("--R", type=int, default=32, help="vectors of the batched mixed apply")
+    p.add_argument("--R", type=int, default=64, help="vectors of the batched mixed apply")
+    p.add_argument("--no-tune", action="store_true", help="skip the launch autotuner (built-in settings)")
+    p.add_argument("--ftlm-steps", type=int, default=30, help="Lanczos steps of the timed FTLM runs")
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true", help="skip batched / FTLM / e2e / CPU legs")
@@ -149,6 +151,17 @@ def make_workload(args, gpu: bool = False):
     else:
         w = workloads.sector_workload(args.lattice, seed=args.seed, gpu=gpu)
     return w, time.time() - t0
+
+
+def measured_traffic(workload: str, kernel: str, n: int):
+    """DRAM bytes of one full launch from the ncu summaries in profiles/apply_traffic.json, or None."""
+    tp = ROOT / "profiles" / "apply_traffic.json"
+    if not tp.exists():
+        return None
+    for e in json.load(open(tp)).get("entries", []):
+        if e.get("workload") == workload and e.get("kernel") == kernel and e.get("bytes_per_row"):
+            return e["bytes_per_row"] * n
+    return None
 
 
 def cpu_baseline(w, H, seconds: float):
@@ -301,6 +314,13 @@ def run_ours(args):
     t0 = time.time()
     op = q.LazyOpSum(basis, H)
     t_op = time.time() - t0
+    tuning = {}
+    if not args.no_tune:
+        # launch autotuner (single-vector FP64 applies): lookup structure and table width, blocks per SM
+        t0 = time.time()
+        log = op.autotune(R=1, dtype="f64", tune_index=True)
+        tuning["single"] = {"seconds": round(time.time() - t0, 2), "trials": len(log.splitlines()) - 2,
+                            "settings": op.tuning(0)}
     hits, misses = op.connectivity()
     h = hits / n
     dev = torch.device("cuda", local)
@@ -339,12 +359,9 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     bytes_per_row = 16 + 8 + 8 * h + 8
     achieved = n * bytes_per_row / (ms * 1e-3) / 1e9
-    traffic = None
-    tp = ROOT / "profiles" / "apply_traffic.json"
-    if tp.exists():
-        tj = json.load(open(tp))
-        if tj.get("workload") == w.name and tj.get("bytes_per_row"):
-            traffic = tj["bytes_per_row"] * n
+    lookup = "LookupHash" if op.tuning(0)["use_hash"] and basis.index_info()["hash"] else "LookupTable"
+    kname = f"k_apply_tile<double,double,{lookup}>"
+    traffic = measured_traffic(w.name, kname, n)
     line = {"metric": METRIC, "value": value, "unit": "states/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ring/Zeeman parameters, N(0,1) vectors)",
@@ -353,10 +370,10 @@ def run_ours(args):
                        "l2": "inputs larger than L2" if inputs_exceed_l2 else "L2 flushed between steps",
                        "setup_s": {"enumerate": round(setup_s, 2), "basis_index": round(t_basis, 2),
                                    "operator": round(t_op, 2)},
-                       "index": basis.index_info()},
+                       "index": basis.index_info(), "tuning": tuning},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "bytes_per_row": bytes_per_row, "kernel": "k_apply_tile<double,double,LookupHash>"},
+                         "bytes_per_row": bytes_per_row, "kernel": kname},
             "gpu_launches": args.steps, "clocks": clk.summary(), "wall_s_timed": t_wall}
     legs = set() if args.no_extras else set(args.legs.split(","))
     if "batched" in legs and rank == 0:
@@ -364,34 +381,61 @@ def run_ours(args):
         R = args.R
         X = torch.randn(n, R, dtype=torch.float32, device=dev)
         Y = torch.zeros_like(X)
+        if not args.no_tune:
+            t0 = time.time()
+            log = op.autotune(R=R, dtype="f32", X=X, Y=Y, tune_lookup=True)
+            tuning["batched"] = {"seconds": round(time.time() - t0, 2), "trials": len(log.splitlines()) - 2,
+                                 "settings": op.tuning(1)}
         for _ in range(2):
             op.apply_batched(X, Y)
         torch.cuda.synchronize()
         kb = max(3, args.steps // 2)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(kb):
+        ev_b = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(kb)]
+        for a, b in ev_b:
+            a.record(stream)
             op.apply_batched(X, Y)
-        e1.record(stream)
+            b.record(stream)
         torch.cuda.synchronize()
-        bms = e0.elapsed_time(e1) / kb
+        bms = sum(a.elapsed_time(b) for a, b in ev_b) / kb
         bval = n * R / (bms * 1e-3)
         bbytes = n * (16 + R * 4 * (h + 2))
+        blk = "LookupHash" if op.tuning(1)["use_hash"] and basis.index_info()["hash"] else "LookupTable"
+        bk = f"k_apply_tile_batched<float,{blk},FF,16-byte gathers> R={R}"
+        bach = bbytes / (bms * 1e-3) / 1e9
         line["batched_mixed"] = {"value": bval, "unit": "state-vectors/s", "R": R, "ms_per_apply": bms,
                                  "accumulation": "double-float (2xFP32) per row", "storage": "FP32 [row][R]",
                                  "vs_plain_fp64": bval / value * ws,
-                                 "roofline_frac": bbytes / (bms * 1e-3) / 1e9 / peak}
-        line["gpu_launches"] += kb
+                                 "roofline": {"bound": "hbm", "achieved": bach, "peak": peak, "unit": "GB/s",
+                                              "frac": bach / peak, "peak_kind": peak_kind,
+                                              "bytes_per_row": 16 + R * 4 * (h + 2), "kernel": bk,
+                                              "traffic": measured_traffic(w.name, bk, n)}}
         del X, Y
+        torch.cuda.empty_cache()
     if "ftlm" in legs and rank == 0:
-        # FTLM vector-steps/s on the same operator (R vectors, M plain Lanczos steps)
-        R = args.R
-        Mf = 20
-        t0 = time.time()
-        q.ftlm([op], [R], M=Mf, seed=1, precision="mixed")
-        tf = time.time() - t0
-        line["ftlm"] = {"value": R * Mf / tf, "unit": "vec-steps/s", "R": R, "M": Mf, "precision": "mixed",
-                        "note": "includes graph capture and host readout"}
+        # FTLM vector-steps/s on the same operator: batched mixed precision (ftlm-R FP32 vectors, one apply
+        # launch per step, the run captured in one CUDA graph) against plain FP64 single-vector Lanczos.
+        # Per-step rates come from the difference of an M and an M/3 step run (setup, capture and readout
+        # cancel); the rates including setup are given beside them.
+        M1 = max(3, args.ftlm_steps)
+        M0 = max(1, M1 // 3)
+
+        def ftlm_rate(R, prec):
+            q.ftlm([op], [R], M=2, seed=1, precision=prec)  # warm-up (allocations, graph paths)
+            t = {}
+            for M in (M0, M1):
+                torch.cuda.synchronize()
+                t0 = time.time()
+                q.ftlm([op], [R], M=M, seed=1, precision=prec)
+                t[M] = time.time() - t0
+            per = (t[M1] - t[M0]) / (M1 - M0)
+            return {"R": R, "precision": prec, "ms_per_step": per * 1e3, "vec_steps_per_s": R / per,
+                    "vec_steps_per_s_incl_setup": R * M1 / t[M1], "seconds": {str(M0): t[M0], str(M1): t[M1]}}
+
+        mixed = ftlm_rate(args.ftlm_R, "mixed")
+        torch.cuda.empty_cache()
+        plain = ftlm_rate(1, "f64")
+        line["ftlm"] = {"value": mixed["vec_steps_per_s"], "unit": "vec-steps/s", "mixed": mixed, "plain_fp64": plain,
+                        "speedup_vs_plain_fp64": mixed["vec_steps_per_s"] / plain["vec_steps_per_s"]}
     if "e2e" in legs and rank == 0:
         # end to end through the C-ABI with pinned host buffers (copies inside the timed region)
         xh = torch.randn(n, dtype=torch.float64).pin_memory()

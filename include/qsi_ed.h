@@ -197,13 +197,14 @@ qsi_status qsi_op_get_tuning(const qsi_op* op, int32_t which, int32_t* kernel, i
  * of dim*R elements, or NULL for scratch the call allocates and frees) and
  * keeps, for the class of R (single vector or batched), the fastest lookup
  * structure (with QSI_TUNE_INDEX: the hash index or the bucket table at
- * several widths; the basis keeps the width chosen), vectors per pass, blocks
+ * several widths, and the basis keeps the width chosen; with QSI_TUNE_LOOKUP:
+ * the hash index or the table at its current width), vectors per pass, blocks
  * per SM and hit-list size, one parameter at a time, best of reps timed
  * applies each.
  * report (optional) receives one line per trial.  Results of later applies
  * are the same for every setting; only their speed changes.  No counterpart
  * in the reference. */
-enum { QSI_TUNE_INDEX = 1 };
+enum { QSI_TUNE_INDEX = 1, QSI_TUNE_LOOKUP = 2 };
 qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_t R, int32_t dtype,
                            int32_t flags, int32_t reps, char* report, size_t report_len);
 /* Connectivity export in the order of LazyOpSum::toSparseMatrix

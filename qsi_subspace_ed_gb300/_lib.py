@@ -17,7 +17,7 @@ QSI_OK, QSI_INVALID_ARG, QSI_OOM, QSI_CUDA_ERROR, QSI_NOT_CONVERGED, QSI_TIMEOUT
 STATUS_NAMES = ["OK", "INVALID_ARG", "OOM", "CUDA_ERROR", "NOT_CONVERGED", "TIMEOUT", "IO_ERROR", "NOT_FOUND"]
 QSI_PTR_HOST, QSI_PTR_DEVICE = 0, 1
 QSI_F64, QSI_F32 = 0, 1
-QSI_TUNE_INDEX = 1
+QSI_TUNE_INDEX, QSI_TUNE_LOOKUP = 1, 2
 CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
 
 

@@ -336,15 +336,17 @@ class LazyOpSum:
                 "vec_chunk": vc, "bucket_bits": self.basis.index_info()["bucket_bits"]}
 
     def autotune(self, R: int = 1, dtype: str = "f64", X=None, Y=None, tune_index: bool = False,
-                 reps: int = 2) -> str:
+                 tune_lookup: bool = False, reps: int = 2) -> str:
         """Times applies of R vectors (device tensors X, Y of shape (dim, R) or scratch) and keeps the
-        fastest launch settings; returns the trial log.  Results of applies do not depend on the settings."""
+        fastest launch settings; returns the trial log.  tune_index also tries the bucket table at several
+        widths (the basis keeps the best), tune_lookup the hash against the table at its current width.
+        Results of applies do not depend on the settings."""
         buf = C.create_string_buffer(8192)
         dt = _lib.QSI_F32 if dtype in ("f32", "mixed", "float32") else _lib.QSI_F64
         xp = C.c_void_p(X.data_ptr()) if X is not None else None
         yp = C.c_void_p(Y.data_ptr()) if Y is not None else None
-        call("qsi_op_autotune", self._h, xp, yp, int(R), dt, _lib.QSI_TUNE_INDEX if tune_index else 0, int(reps),
-             buf, len(buf))
+        flags = (_lib.QSI_TUNE_INDEX if tune_index else 0) | (_lib.QSI_TUNE_LOOKUP if tune_lookup else 0)
+        call("qsi_op_autotune", self._h, xp, yp, int(R), dt, flags, int(reps), buf, len(buf))
         return buf.value.decode()
 
     @staticmethod

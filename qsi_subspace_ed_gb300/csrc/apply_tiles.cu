@@ -538,7 +538,8 @@ __global__ void __launch_bounds__(256, KM == kVec4 ? 2 : 3) k_apply_tile_batched
 // Several operators (sectors) in one launch: the grid is partitioned into
 // per-sector block ranges in proportion to each sector's rows x vectors;
 // each block stages its own sector's terms and works through that sector's
-// tiles.  FP32 storage, double-float accumulation, hash lookups.
+// tiles.  FP32 storage, double-float accumulation; hash lookups when every
+// sector's batched applies use them, else bucket-table lookups.
 struct SectorLaunch {
     TileParams P;
     HashView H;
@@ -550,7 +551,7 @@ struct SectorLaunch {
     int n_blocks;
 };
 
-template <int KM>
+template <int KM, class LK>
 __global__ void __launch_bounds__(256, KM == kVec4 ? 2 : 3) k_apply_sectors(const SectorLaunch* __restrict__ secs, int n_secs,
                                                           int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -561,8 +562,11 @@ __global__ void __launch_bounds__(256, KM == kVec4 ? 2 : 3) k_apply_sectors(cons
         L = secs[s];
     }
     __syncthreads();
-    batched_body<float, LookupHash, true, KM>(L.P, LookupHash{L.H}, L.x, L.y, L.R, accumulate, L.cap,
-                                              (int64_t)blockIdx.x - L.block_begin, L.n_blocks, smem_raw);
+    LK lk;
+    if constexpr (std::is_same<LK, LookupHash>::value) lk = LookupHash{L.H};
+    else lk = LookupTable{L.P.B};
+    batched_body<float, LK, true, KM>(L.P, lk, L.x, L.y, L.R, accumulate, L.cap, (int64_t)blockIdx.x - L.block_begin,
+                                      L.n_blocks, smem_raw);
 }
 
 // Per-row diagonal, evaluated once per operator with the same arithmetic as
@@ -736,6 +740,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
                         SectorPlan& plan) {
     std::vector<SectorLaunch> L(n);
     plan.vec4 = true;
+    plan.hash = true;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -745,8 +750,8 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
     double work_total = 0;
     for (int s = 0; s < n; ++s) {
         qsi_op* op = ops[s];
-        if (!op->basis->d_hash || op->kernel != 1)
-            return fail(QSI_INVALID_ARG, "sector launch needs tile kernels and a hash index");
+        if (op->kernel != 1) return fail(QSI_INVALID_ARG, "sector launch needs the tile kernels");
+        plan.hash = plan.hash && op->basis->d_hash && op->tune[1].use_hash;
         const int cap = (std::max(op->tune[1].list_cap, op->n_pull + 1) + 7) & ~7;  // a row: diagonal + terms
         const int n_rounds = (op->n_pull + 31) / 32;
         smem = std::max(smem, term_smem(op) + (size_t)nw * (512 + (size_t)n_rounds * 128 + (size_t)cap * 12));
@@ -762,7 +767,9 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         work_total += (double)op->basis->n * R[s];
     }
     if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "sector launch: %zu bytes of shared memory needed", smem);
-    const int total = sms * (plan.vec4 ? 2 : 3);  // one wave: the kernels' resident blocks per SM
+    // one wave of the kernel's resident blocks per SM, or the first sector's tuned blocks per SM
+    const int bps = ops[0]->tune[1].grid_bps;
+    const int total = sms * (bps > 0 ? bps : plan.vec4 ? 2 : 3);
     int begin = 0;
     for (int s = 0; s < n; ++s) {
         const int64_t tiles = (ops[s]->basis->n + 31) / 32;
@@ -783,7 +790,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
 qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int accumulate, cudaStream_t st) {
     auto go = [&](auto km) {
         constexpr int KM = decltype(km)::value;
-        auto k = k_apply_sectors<KM>;
+        auto k = plan.hash ? k_apply_sectors<KM, LookupHash> : k_apply_sectors<KM, LookupTable>;
         set_smem(k, plan.smem);
         k<<<plan.grid, 256, plan.smem, st>>>((const SectorLaunch*)d_records, plan.n, accumulate);
     };

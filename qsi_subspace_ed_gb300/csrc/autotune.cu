@@ -6,6 +6,7 @@
 // keeps, one parameter at a time (coordinate descent), the fastest value of:
 //   lookup      hash index, or the bucket table + binary search at several
 //               table widths (QSI_TUNE_INDEX; the basis keeps the best table)
+//               or at its current width (QSI_TUNE_LOOKUP)
 //   vec_chunk   vectors per pass of the 16-byte batched kernel (R FP32 vectors)
 //   grid_bps    blocks per SM of the tile kernels
 //   list_cap    per-warp hit-list size of the batched kernel (rows per chunk)
@@ -138,8 +139,9 @@ extern "C" qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_
                           cfg.use_hash, cfg.grid_bps, cfg.vec_chunk, cfg.list_cap, best);
             T.log += line;
         }
-        // lookup: hash, or the bucket table at widths around the current one
-        if (s == QSI_OK && (flags & QSI_TUNE_INDEX)) {
+        // lookup: hash, or the bucket table (QSI_TUNE_INDEX: at widths around the current one; QSI_TUNE_LOOKUP:
+        // at the current width, leaving the basis as it is)
+        if (s == QSI_OK && (flags & (QSI_TUNE_INDEX | QSI_TUNE_LOOKUP))) {
             qsi_basis* b = op->basis;
             const int b0 = b->bits;
             const int hash0 = cfg.use_hash && b->d_hash ? 1 : 0;
@@ -149,7 +151,8 @@ extern "C" qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_
             if (b->d_hash) codes.push_back(0);
             for (int d = -4; d <= 4; d += 2) {
                 const int bits = b0 + d;
-                if (bits >= 8 && bits <= std::min(30, b->hb + 1)) codes.push_back(bits);
+                if ((flags & QSI_TUNE_INDEX) || d == 0)
+                    if (bits >= 8 && bits <= std::min(30, b->hb + 1)) codes.push_back(bits);
             }
             s = T.sweep("index(0=hash,k=table bits)", codes, best_code, best, [&](int code) -> qsi_status {
                 if (code == 0) {

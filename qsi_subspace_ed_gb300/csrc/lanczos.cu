@@ -1234,7 +1234,7 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
         QSI_CUDA(S[s].ab.alloc((size_t)2 * M * R, st));
         QSI_CUDA(S[s].inv.alloc((size_t)R, st));
         QSI_CUDA(S[s].inv_ff.alloc((size_t)R, st));
-        one_launch = one_launch && ops[s]->basis->d_hash && ops[s]->tune[1].use_hash && ops[s]->kernel == 1 &&
+        one_launch = one_launch && ops[s]->kernel == 1 &&
                      ops[s]->ff_accumulate;
         k_ftlm_init<VT><<<grid_for(S[s].n * R, 256), 256, 0, st>>>(S[s].C.p, S[s].P.p, S[s].n, R, seed + (uint64_t)s);
     }

@@ -65,6 +65,7 @@ struct SectorPlan {
     size_t smem = 0;
     int maxR = 1, grid = 0, n = 0;
     bool vec4 = true;  // every sector's R and vectors take 16-byte gathers
+    bool hash = true;  // every sector's batched applies look columns up through the hash index
 };
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
                         SectorPlan& plan);

@@ -96,6 +96,20 @@ def test_ftlm_multi_sector_batch():
     assert np.array_equal(alone[0][0], res[1][0]) and np.array_equal(alone[0][1], res[1][1])
 
 
+def test_ftlm_sector_launch_lookup_and_tuning_independent():
+    """The one-launch sector apply gives the same recurrences with hash or bucket-table lookups and under any
+    launch settings."""
+    cs = cases()
+    ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["cfg1", "s4444"]]
+    ref = q.ftlm(ops, [32, 16], M=20, seed=4, precision="mixed")
+    for op in ops:
+        op.set_kernel(1, 0)  # bucket table
+        op.set_tuning(4, 16, which=1)
+    other = q.ftlm(ops, [32, 16], M=20, seed=4, precision="mixed")
+    for (a, b), (c, d) in zip(ref, other):
+        assert np.array_equal(a, c) and np.array_equal(b, d)
+
+
 def test_tridiag_ritz_matches_numpy():
     rng = np.random.default_rng(4)
     a = rng.standard_normal((5, 40))

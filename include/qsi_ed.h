@@ -174,6 +174,14 @@ qsi_status qsi_op_apply_static(qsi_op* op, const double* x, double* y, int32_t a
 qsi_status qsi_op_apply_batched(qsi_op* op, const void* X, void* Y, int32_t R,
                                 int32_t dtype, int32_t accumulate, int32_t flags,
                                 void* stream);
+/* Shape of the operator as the apply runs it: off-diagonal terms applied (in
+ * transposed form), off-diagonal terms removed at creation because their
+ * flipped state lies in the basis for no row (every contribution of such a
+ * term is a dropped miss, so removing it changes no result), single-site
+ * Z classes folded into the per-row diagonal, and other diagonal terms.
+ * No counterpart in the reference. */
+qsi_status qsi_op_info(const qsi_op* op, int32_t* n_offdiag, int32_t* n_pruned,
+                       int32_t* n_diag_classes, int32_t* n_diag_generic);
 /* Kernel selection (autotuning): kernel 0 = one row per thread (single
  * vector) / one warp per row (batched); kernel 1 = bit-sliced 32-row tiles
  * (default).  use_hash bit 0 selects the hash index for column lookups; bit 1

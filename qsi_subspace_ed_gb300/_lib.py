@@ -109,6 +109,7 @@ SIGNATURES = {
     "qsi_op_apply_static": [_P, _P, _P, _I32],
     "qsi_op_apply_batched": [_P, _P, _P, _I32, _I32, _I32, _I32, _P],
     "qsi_op_set_kernel": [_P, _I32, _I32, _I32],
+    "qsi_op_info": [_P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)],
     "qsi_op_set_tuning": [_P, _I32, _I32, _I32],
     "qsi_op_get_tuning": [_P, _I32, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32),
                           C.POINTER(_I32)],

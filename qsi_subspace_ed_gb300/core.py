@@ -322,6 +322,12 @@ class LazyOpSum:
         """kernel 0: row per thread / warp per row; 1: bit-sliced 32-row tiles (default)."""
         call("qsi_op_set_kernel", self._h, int(kernel), int(use_hash), int(list_cap))
 
+    def info(self) -> dict:
+        """Off-diagonal terms applied and pruned (never landing in the basis), diagonal classes and others."""
+        v = [C.c_int32() for _ in range(4)]
+        call("qsi_op_info", self._h, *[C.byref(a) for a in v])
+        return dict(zip(("offdiag", "pruned", "diag_classes", "diag_generic"), (a.value for a in v)))
+
     def set_tuning(self, grid_bps: int = 0, vec_chunk: int = 0, which: int = -1) -> None:
         """Blocks per SM of the tile kernels and vectors per pass of the FP32 batched kernel (0 = built-in)
         for single-vector (which=0), batched (1) or both (-1) applies."""

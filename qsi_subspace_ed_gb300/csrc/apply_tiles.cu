@@ -732,12 +732,12 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
     return QSI_OK;
 }
 
-// Several sectors in one launch (FP32 batched, double-float, hash lookups), in two steps: plan_sectors builds
-// the per-sector launch records on the host (block ranges in proportion to rows x vectors, shared memory for
-// the largest sector); the caller copies plan.records to device memory once, and launch_sectors enqueues the
+// Several sectors in one launch (FP32 batched, double-float), in two steps: plan_sectors builds the per-sector
+// launch records on the host (block ranges in proportion to weights, e.g. each sector's measured apply time, or
+// else to rows x vectors; shared memory for the largest sector); the caller copies plan.records to device memory once, and launch_sectors enqueues the
 // kernel (capturable into a CUDA graph: it does no host-to-device copy).
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
-                        SectorPlan& plan) {
+                        SectorPlan& plan, const double* weights) {
     std::vector<SectorLaunch> L(n);
     plan.vec4 = true;
     plan.hash = true;
@@ -764,7 +764,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         L[s].cap = cap;
         maxR = std::max(maxR, R[s]);
         plan.vec4 = plan.vec4 && vec4_ok(op->basis->n, R[s], X[s], Y[s]);
-        work_total += (double)op->basis->n * R[s];
+        work_total += weights ? weights[s] : (double)op->basis->n * R[s];
     }
     if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "sector launch: %zu bytes of shared memory needed", smem);
     // one wave of the kernel's resident blocks per SM, or the first sector's tuned blocks per SM
@@ -773,7 +773,8 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
     int begin = 0;
     for (int s = 0; s < n; ++s) {
         const int64_t tiles = (ops[s]->basis->n + 31) / 32;
-        int b = (int)std::llround(total * ((double)ops[s]->basis->n * R[s]) / std::max(work_total, 1.0));
+        const double work = weights ? weights[s] : (double)ops[s]->basis->n * R[s];
+        int b = (int)std::llround(total * work / std::max(work_total, 1e-30));
         b = (int)std::max<int64_t>(1, std::min<int64_t>(b, (tiles + nw - 1) / nw));
         L[s].block_begin = begin;
         L[s].n_blocks = b;

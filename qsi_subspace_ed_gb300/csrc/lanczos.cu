@@ -1245,6 +1245,28 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
     DevBuf<unsigned char> d_plan[2];
     if (one_launch) {
         std::vector<qsi_op*> opv(ops, ops + ns);
+        // Blocks are shared out in proportion to each sector's apply time alone (rows, vectors, hits and lookup
+        // misses all count): one warm-up and one timed apply per sector, W = H C on the run's own buffers.
+        std::vector<double> weight(ns, 1.0);
+        if (ns > 1) {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            QSI_CUDA(cudaEventCreate(&e0));
+            QSI_CUDA(cudaEventCreate(&e1));
+            qsi_status ts = QSI_OK;
+            for (int s = 0; s < ns && ts == QSI_OK; ++s) {
+                ts = launch_apply(ops[s], S[s].C.p, S[s].W.p, S[s].R, QSI_F32, 0, st);
+                if (ts == QSI_OK && cudaEventRecord(e0, st) != cudaSuccess) ts = QSI_CUDA_ERROR;
+                if (ts == QSI_OK) ts = launch_apply(ops[s], S[s].C.p, S[s].W.p, S[s].R, QSI_F32, 0, st);
+                float ms = 0.f;
+                if (ts == QSI_OK && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                                     cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+                    ts = fail(QSI_CUDA_ERROR, "ftlm: sector timing failed");
+                weight[s] = std::max(1e-3, (double)ms);
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            if (ts != QSI_OK) return ts;
+        }
         for (int parity = 0; parity < 2; ++parity) {
             std::vector<const float*> X(ns);
             std::vector<float*> Y(ns);
@@ -1252,7 +1274,7 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
                 X[s] = (const float*)(parity ? S[s].P.p : S[s].C.p);
                 Y[s] = (float*)S[s].W.p;
             }
-            qsi_status ps = plan_sectors(opv.data(), ns, X.data(), Y.data(), Rs, plan[parity]);
+            qsi_status ps = plan_sectors(opv.data(), ns, X.data(), Y.data(), Rs, plan[parity], weight.data());
             if (ps != QSI_OK) return ps;
             QSI_CUDA(d_plan[parity].alloc(plan[parity].records.size(), st));
             QSI_CUDA(cudaMemcpyAsync(d_plan[parity].p, plan[parity].records.data(), plan[parity].records.size(),

@@ -219,6 +219,75 @@ __global__ void k_count_connectivity(BasisView B, const PushTerm* __restrict__ o
     }
 }
 
+// hit[t] = 1 when transposed term t maps some row's state onto a basis state.  A block stops once every term
+// is known to hit (terms that hit usually do so within the first rows); terms that never hit are tested on
+// every row they admit.
+template <class LK>
+__global__ void k_pull_term_hits(BasisView B, LK lk, const PullTerm* __restrict__ terms, int n, int* __restrict__ hit) {
+    extern __shared__ int known[];
+    __shared__ int n_known;
+    if (threadIdx.x == 0) n_known = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        known[t] = hit[t];
+        if (known[t]) atomicAdd(&n_known, 1);
+    }
+    __syncthreads();
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < B.n; j += (int64_t)gridDim.x * blockDim.x) {
+        if (*(volatile int*)&n_known == n) break;
+        const state2 s = B.states[j];
+        for (int t = 0; t < n; ++t) {
+            if (((volatile int*)known)[t]) continue;
+            const PullTerm& T = terms[t];
+            const bool ok = ((s.x & T.dn0) | (s.y & T.dn1)) == 0 && (s.x & T.up0) == T.up0 && (s.y & T.up1) == T.up1;
+            if (ok && lk.find(s.x ^ T.x0, s.y ^ T.x1) >= 0 && atomicExch(known + t, 1) == 0) {
+                atomicAdd(&n_known, 1);
+                hit[t] = 1;
+            }
+        }
+    }
+}
+
+// Removes the transposed terms that map no row into the basis (their contributions are all dropped misses), keeping
+// the order of the others: an exact reduction of the lookups the apply issues.
+static qsi_status prune_pull_terms(qsi_basis* b, std::vector<PullTerm>& pull) {
+    const int n = (int)pull.size();
+    if (n == 0 || b->n == 0) return QSI_OK;
+    PullTerm* d_terms = nullptr;
+    int* d_hit = nullptr;
+    cudaError_t e = cudaMalloc(&d_terms, n * sizeof(PullTerm));
+    if (e == cudaSuccess) e = cudaMalloc(&d_hit, n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(d_terms, pull.data(), n * sizeof(PullTerm), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(d_hit, 0, n * sizeof(int));
+    if (e == cudaSuccess) {
+        const size_t smem = (size_t)n * sizeof(int);
+        const int grid = grid_for(b->n, 256);
+        if (b->d_hash) {
+            auto k = k_pull_term_hits<LookupHash>;
+            if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k<<<grid, 256, smem>>>(b->view(), LookupHash{b->hview()}, d_terms, n, d_hit);
+        } else {
+            auto k = k_pull_term_hits<LookupTable>;
+            if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k<<<grid, 256, smem>>>(b->view(), LookupTable{b->view()}, d_terms, n, d_hit);
+        }
+        e = cudaGetLastError();
+    }
+    std::vector<int> hit(n, 1);
+    if (e == cudaSuccess) e = cudaMemcpy(hit.data(), d_hit, n * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_terms);
+    cudaFree(d_hit);
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? QSI_OOM : QSI_CUDA_ERROR, "qsi_op_create (term pruning): %s",
+                    cudaGetErrorString(e));
+    std::vector<PullTerm> kept;
+    kept.reserve(n);
+    for (int t = 0; t < n; ++t)
+        if (hit[t]) kept.push_back(pull[t]);
+    pull.swap(kept);
+    return QSI_OK;
+}
+
 // ------------------------------------------------------------------ host helpers
 int grid_for(int64_t n, int block) {
     int dev = 0, sms = 148;
@@ -384,6 +453,15 @@ extern "C" qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t
             q.cs_lo = (float)(q.cs - (double)q.cs_hi);
             pull.push_back(q);
         }
+        const int n_pull_given = (int)pull.size();
+        {
+            qsi_status ps = prune_pull_terms(b, pull);
+            if (ps != QSI_OK) {
+                qsi_op_destroy(op);
+                return ps;
+            }
+        }
+        op->n_pull_pruned = n_pull_given - (int)pull.size();
         // A single-site z class whose bits overlap another class with a
         // different weight would double count; the map above merges equal
         // weights only, and each bit can carry several terms.  Handle repeated
@@ -703,6 +781,16 @@ extern "C" qsi_status qsi_basis_info(const qsi_basis* b, int32_t* bucket_bits, i
     if (has_hash) *has_hash = b->d_hash != nullptr;
     if (index_bytes)
         *index_bytes = (int64_t)(((size_t)b->n_buckets + 1) * 4 + (b->d_hash ? (b->hash_mask + 1) * sizeof(HashSlot) : 0));
+    return QSI_OK;
+}
+
+extern "C" qsi_status qsi_op_info(const qsi_op* op, int32_t* n_offdiag, int32_t* n_pruned, int32_t* n_diag_classes,
+                                   int32_t* n_diag_generic) {
+    if (!op) return fail(QSI_INVALID_ARG, "qsi_op_info: null operator");
+    if (n_offdiag) *n_offdiag = op->n_pull;
+    if (n_pruned) *n_pruned = op->n_pull_pruned;
+    if (n_diag_classes) *n_diag_classes = op->diag.n_cls;
+    if (n_diag_generic) *n_diag_generic = op->n_diag_generic;
     return QSI_OK;
 }
 

@@ -33,6 +33,7 @@ struct qsi_op {
     qsi::PushTerm* d_push_diag = nullptr;   // diagonal terms as given (export)
     qsi::PushTerm* d_diag_generic = nullptr;
     int n_pull = 0, n_push_off = 0, n_push_diag = 0, n_diag_generic = 0;
+    int n_pull_pruned = 0;                  // transposed terms removed because they map no row into the basis
     qsi::DiagSpec diag{};
     size_t smem_bytes = 0;
     // bit-sliced admission tests: per pull term, literals (spin | 0x80 when the spin must be down)
@@ -68,7 +69,7 @@ struct SectorPlan {
     bool hash = true;  // every sector's batched applies look columns up through the hash index
 };
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
-                        SectorPlan& plan);
+                        SectorPlan& plan, const double* weights = nullptr);
 qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int accumulate, cudaStream_t st);
 qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vector<double>& w, std::vector<double>& V, cudaStream_t st);
 }  // namespace qsi

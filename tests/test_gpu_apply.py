@@ -276,3 +276,31 @@ def test_autotune_keeps_results(built):
     op.set_tuning(0, 0)
     op.set_kernel(1, 1, list_cap=256)
     b.set_index(use_hash=True, bucket_bits=0)
+
+
+def test_terms_never_landing_in_the_basis_are_pruned(built):
+    """Bond hopping on an ice-rule (Q=0) basis always leaves it: those terms are removed at creation, and the
+    apply (single and batched) still equals the oracle's push loop over all terms; with two spinon pairs some
+    hops stay in the basis and are kept."""
+    from qsi_subspace_ed_gb300 import workloads
+
+    lat = workloads.lattice("pyro_1x2x1")
+    H = q.build_ring_zeeman(lat, [1, .8, .6, .4], [0.1, 0.2, -0.1], Jpm=0.05)
+    n_hop = sum(1 for c, ops, ids in H.specs() if ops in ("+-", "-+"))
+    for pairs, all_pruned in ((0, True), (2, False)):
+        basis = q.enumerate_basis(lat, n_spinon_pairs=pairs)
+        op = q.LazyOpSum(q.ZBasis(basis), H)
+        info = op.info()
+        assert (info["pruned"] == n_hop) if all_pruned else (info["pruned"] < n_hop), (pairs, info, n_hop)
+        x = np.random.default_rng(41).standard_normal(len(basis))
+        y = np.zeros_like(x)
+        op.evaluate(x, y)
+        ref = O.apply_port(basis, H.specs(), x, threads=1)
+        np.testing.assert_allclose(y, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+        X = np.random.default_rng(42).standard_normal((len(basis), 32)).astype(np.float32)
+        Y = np.zeros_like(X)
+        op.apply_batched(X, Y)
+        ref0 = O.apply_port(basis, H.specs(), X[:, 0].astype(np.float64), threads=1)
+        np.testing.assert_allclose(Y[:, 0], ref0, rtol=0, atol=4e-6 * np.abs(ref0).max())
+    # the ring-only Hamiltonian on its sector keeps every term
+    assert built["s4444"][3].info()["pruned"] == 0

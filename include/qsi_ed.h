@@ -221,6 +221,11 @@ qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_t R, int32_
  * terms).  Call with rows=NULL to get the count. */
 qsi_status qsi_op_triplets(qsi_op* op, double tol, int64_t* rows, int64_t* cols,
                            double* vals, int64_t cap, int64_t* n_out);
+/* MatrixMarket file of the matrix toSparseMatrix assembles, as build_hamiltonian
+ * writes it with Eigen::saveMarket (src/build_hamiltonian.cpp:104-111):
+ * duplicates summed, column-major order, explicit zeros kept, 1-based
+ * indices, values "%.17e".  *nnz_out (optional) receives the entry count. */
+qsi_status qsi_op_write_mtx(qsi_op* op, const char* path, double tol, int64_t* nnz_out);
 /* Number of off-diagonal terms whose flipped state is not in the basis,
  * summed over all rows (projected-ED drops them). */
 qsi_status qsi_op_count_misses(qsi_op* op, int64_t* misses);
@@ -268,6 +273,22 @@ typedef struct qsi_eigval0_cfg {
 } qsi_eigval0_cfg;
 qsi_status qsi_eigval0(qsi_op* op, const qsi_eigval0_cfg* cfg, double* e0,
                        double* eigvec, int32_t* iterations);
+/* qsi_eigval0 with checkpoint/resume of its first (Lanczos) pass, the
+ * checkpoint of the reference's long-run drivers
+ * (components/operator/include/checkpoint_utils.hpp:48-313): an HDF5 file at
+ * `path` with datasets v and u (the current and previous Lanczos vectors,
+ * FP64[dim]), alphas, betas, beta, iteration (uint64), eigval (the current
+ * lowest Ritz value) and random_seed (int32).  If `path` holds a checkpoint
+ * of this run (same dimension and seed) the first pass resumes from it, and
+ * the results are bitwise those of an uninterrupted run.  A checkpoint is
+ * written every `every` iterations (0: only on stopping) and when the call
+ * stops early: after `stop_after` iterations of this call (> 0) or after
+ * `wall_limit_s` seconds (> 0; the role of the reference's SLURM end-time
+ * check, checkpoint_utils.hpp:18-46), returning QSI_TIMEOUT.  Files are
+ * written to path.tmp and renamed over path. */
+qsi_status qsi_eigval0_checkpointed(qsi_op* op, const qsi_eigval0_cfg* cfg, const char* path,
+                                    int32_t every, int32_t stop_after, double wall_limit_s,
+                                    double* e0, double* eigvec, int32_t* iterations);
 
 /* Finite-temperature Lanczos over several sectors at once.  Each sector s has
  * an operator ops[s] and R[s] random vectors; all run M Lanczos steps in one

@@ -198,6 +198,25 @@ def triplet_digest(r, c, v) -> str:
     return h.hexdigest()
 
 
+def save_market_port(r, c, v, n: int, path) -> int:
+    """The MatrixMarket text Eigen::saveMarket writes for SparseMatrix::setFromTriplets(r, c, v)
+    (src/build_hamiltonian.cpp:104-111; Eigen's MarketIO writer restated): duplicates summed in triplet
+    order, column-major with rows ascending, explicit zeros kept, 1-based indices, values '%.17e'."""
+    order = np.lexsort((r, c))  # stable: by column, then row, ties in triplet order
+    rr, cc, vv = r[order], c[order], v[order]
+    er, ec, ev = [], [], []
+    for a, b, x in zip(rr.tolist(), cc.tolist(), vv.tolist()):
+        if er and er[-1] == a and ec[-1] == b:
+            ev[-1] += x
+        else:
+            er.append(a), ec.append(b), ev.append(x)
+    with open(path, "w") as f:
+        f.write("%%MatrixMarket matrix coordinate  real general\n")
+        f.write(f"{n} {n} {len(ev)}\n")
+        f.writelines("%d %d %.17e\n" % (a + 1, b + 1, x) for a, b, x in zip(er, ec, ev))
+    return len(ev)
+
+
 def csr_from_triplets(r, c, v, n):
     import scipy.sparse as sp
 

@@ -110,6 +110,7 @@ SIGNATURES = {
     "qsi_op_apply_batched": [_P, _P, _P, _I32, _I32, _I32, _I32, _P],
     "qsi_op_set_kernel": [_P, _I32, _I32, _I32],
     "qsi_op_info": [_P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)],
+    "qsi_op_write_mtx": [_P, C.c_char_p, _D, C.POINTER(_I64)],
     "qsi_op_set_tuning": [_P, _I32, _I32, _I32],
     "qsi_op_get_tuning": [_P, _I32, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32),
                           C.POINTER(_I32)],
@@ -119,6 +120,8 @@ SIGNATURES = {
     "qsi_op_connectivity": [_P, C.POINTER(_I64), C.POINTER(_I64)],
     "qsi_lanczos_solve": [_P, C.POINTER(LanczosCfg), _P, _P, C.POINTER(Report)],
     "qsi_eigval0": [_P, C.POINTER(Eigval0Cfg), C.POINTER(_D), _P, C.POINTER(_I32)],
+    "qsi_eigval0_checkpointed": [_P, C.POINTER(Eigval0Cfg), C.c_char_p, _I32, _I32, _D, C.POINTER(_D), _P,
+                                 C.POINTER(_I32)],
     "qsi_ftlm_run": [_P, _I32, _P, _I32, _U64, _I32, _P, _P],
     "qsi_tridiag_ritz": [_P, _P, _I32, _I32, _P, _P],
 }

@@ -412,6 +412,12 @@ class LazyOpSum:
         N = self.basis.dim()
         return sp.csr_matrix((v, (r, c)), shape=(N, N))
 
+    def saveMarket(self, path, tol: float = 1e-14) -> int:
+        """Writes toSparseMatrix as a MatrixMarket file (Eigen::saveMarket layout); returns the entry count."""
+        nnz = C.c_int64()
+        call("qsi_op_write_mtx", self._h, str(path).encode(), float(tol), C.byref(nnz))
+        return nnz.value
+
     def connectivity(self):
         """(hits, misses): off-diagonal terms over all rows landing in / leaving the basis."""
         h, m = C.c_int64(), C.c_int64()

@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "h5lite.h"
 #include "qsi_internal.h"
 
 namespace qsi {
@@ -264,13 +265,6 @@ struct Writer {
     }
 };
 
-struct OutDataset {
-    std::string name;
-    int type_class;  // 0 uint, 1 float, 3 string
-    int type_size;
-    std::vector<uint64_t> dims;  // empty = scalar
-    std::vector<uint8_t> data;
-};
 
 static void write_message(Writer& W, int type, const std::vector<uint8_t>& body) {
     size_t n = (body.size() + 7) / 8 * 8;
@@ -316,7 +310,7 @@ static void write_file(const char* path, std::vector<OutDataset> ds) {
         for (auto x : d.dims) append(space, le(x, 8));
         std::vector<uint8_t> dtype;
         if (d.type_class == 0) {
-            dtype = {0x10, 0x00, 0x00, 0x00};
+            dtype = {0x10, (uint8_t)(d.is_signed ? 0x08 : 0x00), 0x00, 0x00};
             append(dtype, le(d.type_size, 4));
             append(dtype, le(0, 2));                   // bit offset
             append(dtype, le(8 * d.type_size, 2));     // precision
@@ -456,6 +450,7 @@ static std::vector<OutDataset> read_all_for_append(const char* path) {
         o.name = kv.first;
         o.type_class = d.type_class == 1 ? 1 : (d.type_class == 3 ? 3 : 0);
         o.type_size = d.type_size;
+        o.is_signed = d.type_signed;
         for (int i = 0; i < d.rank; ++i) o.dims.push_back(d.dims[i]);
         uint64_t nbytes = d.n_elems() * (uint64_t)d.type_size;
         const uint8_t* src = dataset_bytes(R, d, nbytes);
@@ -463,6 +458,33 @@ static std::vector<OutDataset> read_all_for_append(const char* path) {
         all.push_back(std::move(o));
     }
     return all;
+}
+
+void write_datasets(const char* path, const std::vector<OutDataset>& ds) { write_file(path, ds); }
+
+bool read_dataset(const char* path, const char* name, OutDataset& out) {
+    {
+        std::ifstream probe(path, std::ios::binary);
+        if (!probe) return false;
+    }
+    Reader R;
+    open_file(R, path);
+    Dataset d;
+    try {
+        d = find_dataset(R, name);
+    } catch (const std::out_of_range&) {
+        return false;
+    }
+    if (d.is_group || d.big_endian) throw std::runtime_error(std::string(path) + ": unsupported dataset " + name);
+    out.name = name;
+    out.type_class = d.type_class == 1 ? 1 : (d.type_class == 3 ? 3 : 0);
+    out.type_size = d.type_size;
+    out.is_signed = d.type_signed;
+    out.dims.assign(d.dims, d.dims + d.rank);
+    const uint64_t nbytes = d.n_elems() * (uint64_t)d.type_size;
+    const uint8_t* src = dataset_bytes(R, d, nbytes);
+    out.data.assign(src, src + nbytes);
+    return true;
 }
 
 }  // namespace h5

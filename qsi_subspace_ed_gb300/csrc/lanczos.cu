@@ -15,6 +15,7 @@
 #include <random>
 #include <vector>
 
+#include "h5lite.h"
 #include "qsi_device.cuh"
 #include "qsi_handles.h"
 
@@ -815,108 +816,244 @@ extern "C" qsi_status qsi_lanczos_solve(qsi_op* op, const qsi_lanczos_cfg* cfg, 
     });
 }
 
+namespace qsi {
+
+// Checkpoint of the first eigval0 pass, the fields of projED::checkpoint::CheckpointData
+// (components/operator/include/checkpoint_utils.hpp:48-57) as HDF5 datasets of the same names: v (current
+// Lanczos vector), u (previous one), alphas, betas, beta, iteration, eigval, random_seed.
+struct Eigval0Checkpoint {
+    const char* path;
+    int every;            // write every `every` iterations (0: only when stopping early)
+    int stop_after;       // stop (and write) after this many iterations of this call (0: no limit)
+    double wall_limit_s;  // stop (and write) once this much wall time has passed (0: no limit)
+};
+
+static qsi_status write_eigval0_checkpoint(const char* path, const double* d_v, const double* d_u, int64_t n,
+                                           const std::vector<double>& al, const std::vector<double>& be, double beta,
+                                           int64_t iteration, double eigval, uint64_t seed, cudaStream_t st) {
+    auto f64 = [](const char* name, const double* p, size_t count, bool scalar) {
+        h5::OutDataset d;
+        d.name = name;
+        d.type_class = 1;
+        d.type_size = 8;
+        if (!scalar) d.dims = {(uint64_t)count};
+        d.data.resize(count * 8);
+        if (count && p) std::memcpy(d.data.data(), p, count * 8);  // p == nullptr: filled by the caller
+        return d;
+    };
+    std::vector<h5::OutDataset> ds;
+    ds.push_back(f64("v", nullptr, (size_t)n, false));
+    ds.push_back(f64("u", nullptr, (size_t)n, false));
+    QSI_CUDA(cudaMemcpyAsync(ds[0].data.data(), d_v, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+    QSI_CUDA(cudaMemcpyAsync(ds[1].data.data(), d_u, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+    QSI_CUDA(cudaStreamSynchronize(st));
+    ds.push_back(f64("alphas", al.data(), al.size(), false));
+    ds.push_back(f64("betas", be.data(), be.size(), false));
+    ds.push_back(f64("beta", &beta, 1, true));
+    ds.push_back(f64("eigval", &eigval, 1, true));
+    h5::OutDataset it;
+    it.name = "iteration";
+    it.type_class = 0;
+    it.type_size = 8;
+    it.data.resize(8);
+    std::memcpy(it.data.data(), &iteration, 8);
+    ds.push_back(it);
+    h5::OutDataset sd;
+    sd.name = "random_seed";
+    sd.type_class = 0;
+    sd.type_size = 4;
+    sd.is_signed = true;
+    const int32_t seed32 = (int32_t)(uint32_t)seed;
+    sd.data.resize(4);
+    std::memcpy(sd.data.data(), &seed32, 4);
+    ds.push_back(sd);
+    const std::string tmp = std::string(path) + ".tmp";
+    try {
+        h5::write_datasets(tmp.c_str(), ds);
+    } catch (const std::exception& e) {
+        return fail(QSI_IO_ERROR, "eigval0 checkpoint: %s", e.what());
+    }
+    if (std::rename(tmp.c_str(), path) != 0) return fail(QSI_IO_ERROR, "eigval0 checkpoint: cannot rename %s", tmp.c_str());
+    return QSI_OK;
+}
+
 // projED::lanczos::eigval0 (components/linalg_routines/src/lanczos.cpp:67-227):
 // unit start vector from std::mt19937(seed) + std::normal_distribution
 // (set_random_unit, :55-62); u = -beta*u_prev + H v, alpha = <v,u>, u -= alpha v,
 // beta = |u|; stop when beta < abs_tol, or from min_iterations on when the
 // lowest Ritz value changes by less than abs_tol (absolute) or rel_tol
-// (relative); a second identical pass accumulates the Ritz vector.
+// (relative); a second identical pass accumulates the Ritz vector.  With a
+// checkpoint, the first pass resumes from it and writes it at the top of an
+// iteration (the state that iteration starts from).
+static qsi_status eigval0_run(qsi_op* op, const qsi_eigval0_cfg* cfg, const Eigval0Checkpoint* ck, double* e0,
+                              double* eigvec, int32_t* iterations) {
+    const int64_t n = op->basis->n;
+    cudaStream_t st = op->stream;
+    std::vector<double> v0(n);
+    {
+        std::mt19937 rng((unsigned)cfg->seed);
+        std::normal_distribution<double> dist(0.0, 1.0);
+        for (auto& x : v0) x = dist(rng);
+        double nrm = 0.0;
+        for (double x : v0) nrm += x * x;
+        nrm = std::sqrt(nrm);
+        for (auto& x : v0) x /= nrm;
+    }
+    Vecs vx;
+    qsi_status s = vx.init(n, st);
+    if (s) return s;
+    DevBuf<double> v, u, ev;
+    QSI_CUDA(v.alloc(n, st));
+    QSI_CUDA(u.alloc(n, st));
+    std::vector<double> alphas, betas, ritz, h;
+    double eig = 1e308, e0_pass0 = 0.0;
+    int its = 0;
+    const auto t_start = std::chrono::steady_clock::now();
+    for (int pass = 0; pass < (cfg->calc_eigenvector ? 2 : 1); ++pass) {
+        QSI_CUDA(cudaMemcpyAsync(v.p, v0.data(), (size_t)n * 8, cudaMemcpyHostToDevice, st));
+        QSI_CUDA(cudaMemsetAsync(u.p, 0, (size_t)n * 8, st));
+        if (pass == 1) {
+            QSI_CUDA(ev.alloc(n, st));
+            QSI_CUDA(cudaMemsetAsync(ev.p, 0, (size_t)n * 8, st));
+        }
+        std::vector<double> al, be;
+        double beta = 0.0;
+        int it, it0 = 0;
+        if (pass == 0 && ck) {  // resume the first pass from an existing checkpoint of this run
+            h5::OutDataset dv, du, da, db, dbeta, dit, dseed;
+            bool have = false;
+            try {
+                have = h5::read_dataset(ck->path, "v", dv);
+                if (have && !(h5::read_dataset(ck->path, "u", du) && h5::read_dataset(ck->path, "alphas", da) &&
+                              h5::read_dataset(ck->path, "betas", db) && h5::read_dataset(ck->path, "beta", dbeta) &&
+                              h5::read_dataset(ck->path, "iteration", dit) &&
+                              h5::read_dataset(ck->path, "random_seed", dseed)))
+                    return fail(QSI_IO_ERROR, "eigval0 checkpoint %s: missing datasets", ck->path);
+            } catch (const std::exception& e) {
+                return fail(QSI_IO_ERROR, "eigval0 checkpoint %s: %s", ck->path, e.what());
+            }
+            if (have) {
+                int64_t itv = 0;
+                int32_t seed32 = 0;
+                if (dit.data.size() == 8) std::memcpy(&itv, dit.data.data(), 8);
+                if (dseed.data.size() == 4) std::memcpy(&seed32, dseed.data.data(), 4);
+                const size_t m = da.data.size() / 8;
+                if (dv.type_class != 1 || dv.data.size() != (size_t)n * 8 || du.data.size() != (size_t)n * 8 ||
+                    db.data.size() != m * 8 || (int64_t)m != itv || dbeta.data.size() != 8 ||
+                    seed32 != (int32_t)(uint32_t)cfg->seed || itv > cfg->max_iterations)
+                    return fail(QSI_INVALID_ARG, "eigval0 checkpoint %s: not a checkpoint of this run", ck->path);
+                QSI_CUDA(cudaMemcpyAsync(v.p, dv.data.data(), (size_t)n * 8, cudaMemcpyHostToDevice, st));
+                QSI_CUDA(cudaMemcpyAsync(u.p, du.data.data(), (size_t)n * 8, cudaMemcpyHostToDevice, st));
+                QSI_CUDA(cudaStreamSynchronize(st));
+                al.resize(m);
+                be.resize(m);
+                std::memcpy(al.data(), da.data.data(), m * 8);
+                std::memcpy(be.data(), db.data.data(), m * 8);
+                std::memcpy(&beta, dbeta.data.data(), 8);
+                it0 = (int)itv;
+            }
+        }
+        if (pass == 1) eig = 1e308;
+        for (it = it0; it < cfg->max_iterations; ++it) {
+            if (pass == 0 && ck && it > it0) {
+                const double elapsed =
+                    std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+                const bool stop = (ck->stop_after > 0 && it - it0 >= ck->stop_after) ||
+                                  (ck->wall_limit_s > 0 && elapsed >= ck->wall_limit_s);
+                if (stop || (ck->every > 0 && it % ck->every == 0)) {
+                    double est = std::nan("");
+                    if (!al.empty()) {
+                        std::vector<double> b2(be.begin(), be.end() - 1);
+                        s = lowest_of_tridiag(al, b2, est, st);
+                        if (s) return s;
+                    }
+                    s = write_eigval0_checkpoint(ck->path, v.p, u.p, n, al, be, beta, it, est, cfg->seed, st);
+                    if (s) return s;
+                }
+                if (stop) {
+                    if (iterations) *iterations = it;
+                    return fail(QSI_TIMEOUT, "eigval0: stopped at iteration %d, checkpoint written to %s", it, ck->path);
+                }
+            }
+            if (pass == 1 && it < (int)ritz.size())
+                k_axpby<<<grid_for(n, 256), 256, 0, st>>>(ev.p, v.p, ritz[it], 1.0, n);
+            if (it > 0) k_axpby<<<grid_for(n, 256), 256, 0, st>>>(u.p, v.p, 0.0, -beta, n);
+            s = launch_apply(op, v.p, u.p, 1, QSI_F64, 1, st);
+            if (s) return s;
+            s = vx.dots<double>(v.p, n, 1, u.p, h);
+            if (s) return s;
+            double alpha = h[0];
+            k_axpby<<<grid_for(n, 256), 256, 0, st>>>(u.p, v.p, -alpha, 1.0, n);
+            s = vx.dots<double>(v.p, n, 0, u.p, h);
+            if (s) return s;
+            beta = std::sqrt(h[0]);
+            if (beta < cfg->abs_tol) break;
+            std::swap(v.p, u.p);
+            k_axpby<<<grid_for(n, 256), 256, 0, st>>>(v.p, v.p, 0.0, 1.0 / beta, n);
+            al.push_back(alpha);
+            be.push_back(beta);
+            // The first pass never stops on convergence (lanczos.cpp:163-167 breaks
+            // only when a Ritz vector is being accumulated); the second pass does.
+            if (pass == 1 && it >= cfg->min_iterations) {
+                double old = eig;
+                std::vector<double> b2(be.begin(), be.end() - 1);
+                s = lowest_of_tridiag(al, b2, eig, st);
+                if (s) return s;
+                double err = std::fabs(eig - old);
+                double rel = err / std::max(std::fabs(eig), 1e-10);
+                if (err < cfg->abs_tol || rel < cfg->rel_tol) break;
+            }
+        }
+        if (pass == 0) {
+            its = it;
+            alphas = al;
+            betas = be;
+            std::vector<double> b2(be.begin(), be.empty() ? be.end() : be.end() - 1);
+            s = lowest_of_tridiag(al, b2, eig, st);
+            if (s) return s;
+            e0_pass0 = eig;
+            if (cfg->calc_eigenvector) {
+                const int m = (int)al.size();
+                DevBuf<double> d, work, y;
+                QSI_CUDA(d.alloc((size_t)2 * m, st));
+                QSI_CUDA(work.alloc((size_t)5 * m + 8, st));
+                QSI_CUDA(y.alloc((size_t)m, st));
+                QSI_CUDA(cudaMemcpyAsync(d.p, al.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
+                if (m > 1) QSI_CUDA(cudaMemcpyAsync(d.p + m, b2.data(), (size_t)(m - 1) * 8, cudaMemcpyHostToDevice, st));
+                k_tridiag_vector<<<1, 32, 0, st>>>(d.p, d.p + m, m, eig, work.p, y.p);
+                ritz.resize(m);
+                QSI_CUDA(cudaMemcpyAsync(ritz.data(), y.p, (size_t)m * 8, cudaMemcpyDeviceToHost, st));
+                QSI_CUDA(cudaStreamSynchronize(st));
+            }
+        }
+    }
+    *e0 = e0_pass0;
+    if (iterations) *iterations = its;
+    if (cfg->calc_eigenvector && eigvec) {
+        QSI_CUDA(cudaMemcpyAsync(eigvec, ev.p, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+    }
+    return QSI_OK;
+}
+
+}  // namespace qsi
+
 extern "C" qsi_status qsi_eigval0(qsi_op* op, const qsi_eigval0_cfg* cfg, double* e0, double* eigvec,
                                   int32_t* iterations) {
     return guarded([&]() -> qsi_status {
         if (!op || !cfg || !e0) return fail(QSI_INVALID_ARG, "qsi_eigval0: null argument");
-        const int64_t n = op->basis->n;
-        cudaStream_t st = op->stream;
-        std::vector<double> v0(n);
-        {
-            std::mt19937 rng((unsigned)cfg->seed);
-            std::normal_distribution<double> dist(0.0, 1.0);
-            for (auto& x : v0) x = dist(rng);
-            double nrm = 0.0;
-            for (double x : v0) nrm += x * x;
-            nrm = std::sqrt(nrm);
-            for (auto& x : v0) x /= nrm;
-        }
-        Vecs vx;
-        qsi_status s = vx.init(n, st);
-        if (s) return s;
-        DevBuf<double> v, u, ev;
-        QSI_CUDA(v.alloc(n, st));
-        QSI_CUDA(u.alloc(n, st));
-        std::vector<double> alphas, betas, ritz, h;
-        double eig = 1e308, e0_pass0 = 0.0;
-        int its = 0;
-        for (int pass = 0; pass < (cfg->calc_eigenvector ? 2 : 1); ++pass) {
-            QSI_CUDA(cudaMemcpyAsync(v.p, v0.data(), (size_t)n * 8, cudaMemcpyHostToDevice, st));
-            QSI_CUDA(cudaMemsetAsync(u.p, 0, (size_t)n * 8, st));
-            if (pass == 1) {
-                QSI_CUDA(ev.alloc(n, st));
-                QSI_CUDA(cudaMemsetAsync(ev.p, 0, (size_t)n * 8, st));
-            }
-            std::vector<double> al, be;
-            double beta = 0.0;
-            int it;
-            if (pass == 1) eig = 1e308;
-            for (it = 0; it < cfg->max_iterations; ++it) {
-                if (pass == 1 && it < (int)ritz.size())
-                    k_axpby<<<grid_for(n, 256), 256, 0, st>>>(ev.p, v.p, ritz[it], 1.0, n);
-                if (it > 0) k_axpby<<<grid_for(n, 256), 256, 0, st>>>(u.p, v.p, 0.0, -beta, n);
-                s = launch_apply(op, v.p, u.p, 1, QSI_F64, 1, st);
-                if (s) return s;
-                s = vx.dots<double>(v.p, n, 1, u.p, h);
-                if (s) return s;
-                double alpha = h[0];
-                k_axpby<<<grid_for(n, 256), 256, 0, st>>>(u.p, v.p, -alpha, 1.0, n);
-                s = vx.dots<double>(v.p, n, 0, u.p, h);
-                if (s) return s;
-                beta = std::sqrt(h[0]);
-                if (beta < cfg->abs_tol) break;
-                std::swap(v.p, u.p);
-                k_axpby<<<grid_for(n, 256), 256, 0, st>>>(v.p, v.p, 0.0, 1.0 / beta, n);
-                al.push_back(alpha);
-                be.push_back(beta);
-                // The first pass never stops on convergence (lanczos.cpp:163-167 breaks
-                // only when a Ritz vector is being accumulated); the second pass does.
-                if (pass == 1 && it >= cfg->min_iterations) {
-                    double old = eig;
-                    std::vector<double> b2(be.begin(), be.end() - 1);
-                    s = lowest_of_tridiag(al, b2, eig, st);
-                    if (s) return s;
-                    double err = std::fabs(eig - old);
-                    double rel = err / std::max(std::fabs(eig), 1e-10);
-                    if (err < cfg->abs_tol || rel < cfg->rel_tol) break;
-                }
-            }
-            if (pass == 0) {
-                its = it;
-                alphas = al;
-                betas = be;
-                std::vector<double> b2(be.begin(), be.empty() ? be.end() : be.end() - 1);
-                s = lowest_of_tridiag(al, b2, eig, st);
-                if (s) return s;
-                e0_pass0 = eig;
-                if (cfg->calc_eigenvector) {
-                    const int m = (int)al.size();
-                    DevBuf<double> d, work, y;
-                    QSI_CUDA(d.alloc((size_t)2 * m, st));
-                    QSI_CUDA(work.alloc((size_t)5 * m + 8, st));
-                    QSI_CUDA(y.alloc((size_t)m, st));
-                    QSI_CUDA(cudaMemcpyAsync(d.p, al.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
-                    if (m > 1) QSI_CUDA(cudaMemcpyAsync(d.p + m, b2.data(), (size_t)(m - 1) * 8, cudaMemcpyHostToDevice, st));
-                    k_tridiag_vector<<<1, 32, 0, st>>>(d.p, d.p + m, m, eig, work.p, y.p);
-                    ritz.resize(m);
-                    QSI_CUDA(cudaMemcpyAsync(ritz.data(), y.p, (size_t)m * 8, cudaMemcpyDeviceToHost, st));
-                    QSI_CUDA(cudaStreamSynchronize(st));
-                }
-            }
-        }
-        *e0 = e0_pass0;
-        if (iterations) *iterations = its;
-        if (cfg->calc_eigenvector && eigvec) {
-            QSI_CUDA(cudaMemcpyAsync(eigvec, ev.p, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
-            QSI_CUDA(cudaStreamSynchronize(st));
-        }
-        return QSI_OK;
+        return eigval0_run(op, cfg, nullptr, e0, eigvec, iterations);
+    });
+}
+
+extern "C" qsi_status qsi_eigval0_checkpointed(qsi_op* op, const qsi_eigval0_cfg* cfg, const char* path, int32_t every,
+                                               int32_t stop_after, double wall_limit_s, double* e0, double* eigvec,
+                                               int32_t* iterations) {
+    return guarded([&]() -> qsi_status {
+        if (!op || !cfg || !e0 || !path || every < 0 || stop_after < 0 || wall_limit_s < 0)
+            return fail(QSI_INVALID_ARG, "qsi_eigval0_checkpointed: bad argument");
+        const Eigval0Checkpoint ck{path, every, stop_after, wall_limit_s};
+        return eigval0_run(op, cfg, &ck, e0, eigvec, iterations);
     });
 }
 

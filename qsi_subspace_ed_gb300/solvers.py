@@ -49,11 +49,15 @@ def diagonalise(op: LazyOpSum, nev: int = 1, ncv: int = 15, tol: float = 1e-10, 
 
 
 def eigval0(op: LazyOpSum, seed: int = 10, abs_tol: float = 1e-8, rel_tol: float = 1e-8, min_iterations: int = 10,
-            max_iterations: int = 5000, calc_eigenvector: bool = True):
+            max_iterations: int = 5000, calc_eigenvector: bool = True, checkpoint: str | None = None,
+            checkpoint_every: int = 0, stop_after: int = 0, wall_limit_s: float = 0.0):
     """Lowest eigenvalue by plain Lanczos (no reorthogonalisation), two-pass eigenvector.
 
     Defaults follow lanczos::Settings (components/linalg_routines/include/lanczos.hpp:9-20);
     diag_DOQSI_ham sets min_iterations=10 and calc_eigenvector=true (include/lanczos_cli.hpp:29-38).
+    With `checkpoint` (an HDF5 path) the first pass resumes from that file when it holds a checkpoint of
+    this run, and writes it every `checkpoint_every` iterations and on an early stop (`stop_after`
+    iterations of this call, or `wall_limit_s` seconds), which raises QsiError with status QSI_TIMEOUT.
     Returns (E0, eigvec or None, iterations).
     """
     n = op.rows()
@@ -62,7 +66,12 @@ def eigval0(op: LazyOpSum, seed: int = 10, abs_tol: float = 1e-8, rel_tol: float
     e0 = C.c_double()
     its = C.c_int32()
     vec = np.zeros(n) if calc_eigenvector else None
-    call("qsi_eigval0", op._h, C.byref(cfg), C.byref(e0), ptr(vec) if calc_eigenvector else None, C.byref(its))
+    if checkpoint is None:
+        call("qsi_eigval0", op._h, C.byref(cfg), C.byref(e0), ptr(vec) if calc_eigenvector else None, C.byref(its))
+    else:
+        call("qsi_eigval0_checkpointed", op._h, C.byref(cfg), str(checkpoint).encode(), int(checkpoint_every),
+             int(stop_after), float(wall_limit_s), C.byref(e0), ptr(vec) if calc_eigenvector else None,
+             C.byref(its))
     return e0.value, vec, its.value
 
 

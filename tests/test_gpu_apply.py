@@ -304,3 +304,20 @@ def test_terms_never_landing_in_the_basis_are_pruned(built):
         np.testing.assert_allclose(Y[:, 0], ref0, rtol=0, atol=4e-6 * np.abs(ref0).max())
     # the ring-only Hamiltonian on its sector keeps every term
     assert built["s4444"][3].info()["pruned"] == 0
+
+
+@pytest.mark.parametrize("name", ["ref32_g", "s4444"])
+def test_matrix_market_export(built, name, tmp_path):
+    """saveMarket of the GPU triplets is byte-identical to the oracle's restatement of Eigen's writer over the
+    oracle's triplets, and reads back (scipy) as the same matrix."""
+    import scipy.io
+
+    basis, H, b, op = built[name]
+    p_gpu, p_ora = tmp_path / "gpu.mtx", tmp_path / "oracle.mtx"
+    nnz = op.saveMarket(p_gpu)
+    r, c, v = O.triplets_port(basis, H.specs())
+    assert O.save_market_port(r, c, v, len(basis), p_ora) == nnz
+    assert p_gpu.read_bytes() == p_ora.read_bytes()
+    M = scipy.io.mmread(str(p_gpu)).tocsr()
+    ref = O.csr_from_triplets(r, c, v, len(basis))
+    assert abs(M - ref).max() == 0

@@ -120,3 +120,28 @@ def test_tridiag_ritz_matches_numpy():
         w, Y = np.linalg.eigh(T)
         np.testing.assert_allclose(ev[k], w, atol=1e-12)
         np.testing.assert_allclose(first[k] ** 2, Y[0] ** 2, atol=1e-10)
+
+
+def test_eigval0_checkpoint_resume_is_bitwise(tmp_path):
+    """A run stopped at an iteration limit and resumed from its checkpoint gives the uninterrupted result bitwise;
+    the checkpoint file holds the reference's checkpoint datasets."""
+    basis, H = cases()["cfg1"]
+    op = q.LazyOpSum(q.ZBasis(basis), H)
+    kw = dict(seed=5, max_iterations=150, min_iterations=10, abs_tol=1e-10, rel_tol=1e-10)
+    e_ref, v_ref, it_ref = q.eigval0(op, **kw)
+    path = tmp_path / "ckpt.h5"
+    with pytest.raises(q.QsiError) as ex:
+        q.eigval0(op, checkpoint=path, checkpoint_every=20, stop_after=57, **kw)
+    assert ex.value.status == 5  # QSI_TIMEOUT
+    al = q.read_f64_h5(path, "alphas")
+    v = q.read_f64_h5(path, "v")
+    assert len(al) == 57 and len(v) == len(basis) and abs(np.linalg.norm(v) - 1) < 1e-12
+    assert np.isfinite(q.read_f64_h5(path, "eigval")).all()
+    with pytest.raises(q.QsiError):  # a second interruption, resumed from the first checkpoint
+        q.eigval0(op, checkpoint=path, stop_after=40, **kw)
+    assert len(q.read_f64_h5(path, "alphas")) == 97
+    e, vec, its = q.eigval0(op, checkpoint=path, checkpoint_every=20, **kw)
+    assert e == e_ref and its == it_ref and np.array_equal(vec, v_ref)
+    # a checkpoint of another seed is refused
+    with pytest.raises(q.QsiError):
+        q.eigval0(op, checkpoint=path, **{**kw, "seed": 6})

@@ -98,6 +98,13 @@ qsi_status qsi_h5_write_basis(const char* path, const char* dataset,
 qsi_status qsi_h5_write_eigs(const char* path, const double* evals, int64_t nev,
                              const double* evecs, int64_t dim, int64_t nvec,
                              const char* latfile_json, const char* dset_name);
+/* One float64 dataset of any rank (dims[rank]) / one fixed-length string
+ * dataset, in a new file (append = 0) or added to a file this library wrote
+ * (append = 1): the datasets of eval_observables' .out.h5 file
+ * (src/expectation_eval.cpp:127-230, src/eval_observables.cpp:119-130). */
+qsi_status qsi_h5_write_f64(const char* path, const char* dataset, const double* data,
+                            const int64_t* dims, int32_t rank, int32_t append);
+qsi_status qsi_h5_write_string(const char* path, const char* dataset, const char* text, int32_t append);
 /* CSV basis "0x%016hi%016lo" per line (basis_io.hpp:16-53). */
 qsi_status qsi_csv_read_basis(const char* path, uint64_t* out_lohi, int64_t cap, int64_t* n_out);
 
@@ -297,6 +304,18 @@ qsi_status qsi_eigval0_checkpointed(qsi_op* op, const qsi_eigval0_cfg* cfg, cons
 qsi_status qsi_ftlm_run(qsi_op** ops, int32_t n_sectors, const int32_t* R,
                         int32_t M, uint64_t seed, int32_t precision,
                         double* alphas, double* betas);
+
+/* Expectation values of n_ops operators between nvec vectors, as eval_observables
+ * computes them (src/expectation_eval.cpp:27-110, src/eval_observables.cpp:134-208):
+ * operator l is the term list terms[op_offsets[l] .. op_offsets[l+1]) (a
+ * SymbolicOpSum) bound to basis b; psi holds the vectors column by column
+ * (dim x nvec, Eigen's column-major layout, 1 <= nvec <= 256).
+ *   expect[(l*nvec + i)*nvec + j]            = psi_j . (O_l psi_i)
+ *   cross[((l*n_ops + m)*nvec + i)*nvec + j] = (O_l psi_i) . (O_m psi_j)   (optional)
+ * FP64 on the device; cross keeps all n_ops*nvec vectors O_l psi_i resident. */
+qsi_status qsi_expectations(qsi_basis* b, const qsi_term* terms, const int32_t* op_offsets,
+                            int32_t n_ops, const double* psi, int32_t nvec, double* expect,
+                            double* cross);
 
 /* Batched eigen-decomposition of n_mat symmetric tridiagonal m x m matrices
  * (diagonals a[k*m..], off-diagonals b[k*m..], the first m-1 used), m <= 128:

@@ -72,6 +72,8 @@ def port():
                                             C.c_int]
         lib.oracle_term_compile.argtypes = [C.c_char_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]
         lib.oracle_apply_state.argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_term_mul.restype = None
+        lib.oracle_term_mul.argtypes = [C.c_void_p, C.c_void_p]
         lib.oracle_set_random_unit.restype = None
         lib.oracle_set_random_unit.argtypes = [C.c_void_p, C.c_int64, C.c_uint]
         lib.oracle_evaluate_add_rows.restype = C.c_int
@@ -111,6 +113,63 @@ def terms_array(specs):
         if rc != 0:
             raise ValueError(f"bad operator spec {ops!r}")
     return buf[: len(specs)].copy()
+
+
+def apply_terms_port(basis: np.ndarray, terms: np.ndarray, x: np.ndarray, threads: int = 0) -> np.ndarray:
+    """y = O x by the restated push loop for a compiled term array (qsi_term layout rows)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x)
+    t = np.ascontiguousarray(terms)
+    port().oracle_evaluate_add(_p(basis), len(basis), _p(t), len(t), _p(x), _p(y), threads)
+    return y
+
+
+def term_product_port(factors: np.ndarray) -> np.ndarray:
+    """The product factors[0] * factors[1] * ... (SymbolicPMROperator::operator*=, restated), one term row."""
+    out = np.ascontiguousarray(factors[0:1]).copy()
+    for k in range(1, len(factors)):
+        f = np.ascontiguousarray(factors[k:k + 1])
+        port().oracle_term_mul(_p(out), _p(f))
+    return out
+
+
+def ring_terms_port(lat: dict) -> list:
+    """One term array per hexagon ring (get_ring_ops, geometry.hpp:29-62: sign +1 -> '+', -1 -> '-')."""
+    out = []
+    for ring in lat["rings"]:
+        ids = list(ring["member_spin_idx"])
+        if len(ids) != 6:
+            continue
+        ops = "".join("+" if v == 1 else "-" for v in ring["signs"])
+        out.append(terms_array([(1.0, ops, ids)]))
+    return out
+
+
+_PERM3 = ((0, 1, 2), (1, 2, 0), (2, 0, 1), (0, 2, 1), (2, 1, 0), (1, 0, 2))
+
+
+def partial_vol_terms_port(lat: dict, rings: list, missing_sl: int) -> list:
+    """get_partial_vol_ops (geometry.hpp:107-145): per volume, the three rings other than the one of
+    sublattice `missing_sl`, multiplied in the six orders and summed (coefficient 1 each)."""
+    out = []
+    for vol in lat["vols"]:
+        plaq = vol["member_plaq_idx"]
+        three = [rings[plaq[i]][0] for i in range(4) if i != missing_sl]
+        terms = [term_product_port(np.stack([three[p[0]], three[p[1]], three[p[2]]]))[0] for p in _PERM3]
+        out.append(np.stack(terms))
+    return out
+
+
+def expectations_port(basis: np.ndarray, ops: list, psi: np.ndarray, cross: bool = False):
+    """compute_all_expectations / compute_cross_correlation (src/expectation_eval.cpp:27-110), FP64:
+    expect[l, i, j] = psi_j . (O_l psi_i), cross[l, m, i, j] = (O_l psi_i) . (O_m psi_j)."""
+    psi = np.asarray(psi, dtype=np.float64).reshape(len(basis), -1)
+    nv = psi.shape[1]
+    W = np.stack([np.stack([apply_terms_port(basis, t, psi[:, i]) for i in range(nv)]) for t in ops])  # (L, nv, N)
+    expect = np.einsum("lin,nj->lij", W, psi)
+    if not cross:
+        return expect, None
+    return expect, np.einsum("lin,mjn->lmij", W, W)
 
 
 def apply_port(basis: np.ndarray, specs, x: np.ndarray, y: np.ndarray | None = None, threads: int = 0):

@@ -224,6 +224,24 @@ int64_t oracle_triplets(const uint64_t* basis, int64_t n, const oterm* terms, in
 
 /* _construct: right-to-left walk over (op, spin) pairs.  Returns 0, or -1 on
  * an unknown op character (bad_operator_spec). */
+/* a *= b: SymbolicPMROperator::operator*= (operator.hpp:312-330).  The sign picks up (-1)^popcount(a.X & b.Z)
+ * (moving b's Z through a's X), the Z and X masks combine by XOR, a's projector requirements are carried
+ * through b's flips, and an up/down conflict kills the operator (sign 0).  Coefficients multiply. */
+void oracle_term_mul(oterm* a, const oterm* b) {
+    u128 aX = mk(a->x), aU = mk(a->up), aD = mk(a->down), bX = mk(b->x), bZ = mk(b->z);
+    a->sign *= 1 - 2 * (popc128(aX & bZ) % 2);
+    u128 Z = mk(a->z) ^ bZ, X = aX ^ bX;
+    u128 req_up = (aD & bX) | (aU & ~bX);
+    u128 req_dn = (aU & bX) | (aD & ~bX);
+    u128 U = mk(b->up) | req_up, D = mk(b->down) | req_dn;
+    if ((U & D) != 0) a->sign = 0;
+    a->x[0] = (uint64_t)X, a->x[1] = (uint64_t)(X >> 64);
+    a->z[0] = (uint64_t)Z, a->z[1] = (uint64_t)(Z >> 64);
+    a->up[0] = (uint64_t)U, a->up[1] = (uint64_t)(U >> 64);
+    a->down[0] = (uint64_t)D, a->down[1] = (uint64_t)(D >> 64);
+    a->c *= b->c;
+}
+
 int oracle_term_compile(const char* ops, const int32_t* ids, int n, double c, oterm* out) {
     u128 X = 0, Z = 0, up = 0, down = 0;
     int sign = 1;

@@ -92,6 +92,8 @@ SIGNATURES = {
     "qsi_h5_read_f64": [C.c_char_p, C.c_char_p, _P, _I64, C.POINTER(_I64), _P, C.POINTER(_I32)],
     "qsi_h5_write_basis": [C.c_char_p, C.c_char_p, _P, _I64, _I32],
     "qsi_h5_write_eigs": [C.c_char_p, _P, _I64, _P, _I64, _I64, C.c_char_p, C.c_char_p],
+    "qsi_h5_write_f64": [C.c_char_p, C.c_char_p, _P, _P, _I32, _I32],
+    "qsi_h5_write_string": [C.c_char_p, C.c_char_p, C.c_char_p, _I32],
     "qsi_csv_read_basis": [C.c_char_p, _P, _I64, C.POINTER(_I64)],
     "qsi_enumerate_basis": [_I32, _P, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32,
                             C.POINTER(C.POINTER(C.c_uint64)), C.POINTER(_I64)],
@@ -111,6 +113,7 @@ SIGNATURES = {
     "qsi_op_set_kernel": [_P, _I32, _I32, _I32],
     "qsi_op_info": [_P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)],
     "qsi_op_write_mtx": [_P, C.c_char_p, _D, C.POINTER(_I64)],
+    "qsi_expectations": [_P, _P, _P, _I32, _P, _I32, _P, _P],
     "qsi_op_set_tuning": [_P, _I32, _I32, _I32],
     "qsi_op_get_tuning": [_P, _I32, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32),
                           C.POINTER(_I32)],

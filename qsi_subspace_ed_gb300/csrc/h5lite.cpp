@@ -629,6 +629,65 @@ extern "C" qsi_status qsi_h5_write_eigs(const char* path, const double* evals, i
     });
 }
 
+extern "C" qsi_status qsi_h5_write_f64(const char* path, const char* dataset, const double* data, const int64_t* dims,
+                                       int32_t rank, int32_t append) {
+    return guarded([&]() -> qsi_status {
+        if (!path || !dataset || rank < 0 || rank > 8 || (rank > 0 && !dims))
+            return fail(QSI_INVALID_ARG, "qsi_h5_write_f64: bad argument");
+        uint64_t count = 1;
+        h5::OutDataset o;
+        o.name = dataset;
+        o.type_class = 1;
+        o.type_size = 8;
+        for (int i = 0; i < rank; ++i) {
+            if (dims[i] < 0) return fail(QSI_INVALID_ARG, "qsi_h5_write_f64: negative dimension");
+            o.dims.push_back((uint64_t)dims[i]);
+            count *= (uint64_t)dims[i];
+        }
+        if (count && !data) return fail(QSI_INVALID_ARG, "qsi_h5_write_f64: null data");
+        o.data.resize(count * 8);
+        if (count) std::memcpy(o.data.data(), data, count * 8);
+        std::vector<h5::OutDataset> all;
+        try {
+            if (append) {
+                all = h5::read_all_for_append(path);
+                all.erase(std::remove_if(all.begin(), all.end(), [&](const h5::OutDataset& d) { return d.name == dataset; }),
+                          all.end());
+            }
+            all.push_back(std::move(o));
+            h5::write_file(path, std::move(all));
+        } catch (const std::exception& e) {
+            return fail(QSI_IO_ERROR, "%s: %s", path, e.what());
+        }
+        return QSI_OK;
+    });
+}
+
+extern "C" qsi_status qsi_h5_write_string(const char* path, const char* dataset, const char* text, int32_t append) {
+    return guarded([&]() -> qsi_status {
+        if (!path || !dataset || !text) return fail(QSI_INVALID_ARG, "qsi_h5_write_string: bad argument");
+        h5::OutDataset o;
+        o.name = dataset;
+        o.type_class = 3;
+        const size_t len = std::strlen(text) + 1;
+        o.type_size = (int)len;
+        o.data.assign(text, text + len);
+        std::vector<h5::OutDataset> all;
+        try {
+            if (append) {
+                all = h5::read_all_for_append(path);
+                all.erase(std::remove_if(all.begin(), all.end(), [&](const h5::OutDataset& d) { return d.name == dataset; }),
+                          all.end());
+            }
+            all.push_back(std::move(o));
+            h5::write_file(path, std::move(all));
+        } catch (const std::exception& e) {
+            return fail(QSI_IO_ERROR, "%s: %s", path, e.what());
+        }
+        return QSI_OK;
+    });
+}
+
 extern "C" qsi_status qsi_csv_read_basis(const char* path, uint64_t* out_lohi, int64_t cap, int64_t* n_out) {
     return guarded([&]() -> qsi_status {
         if (!path || !n_out) return fail(QSI_INVALID_ARG, "qsi_csv_read_basis: null argument");

@@ -1057,6 +1057,81 @@ extern "C" qsi_status qsi_eigval0_checkpointed(qsi_op* op, const qsi_eigval0_cfg
     });
 }
 
+// ------------------------------------------------------------------ expectation values
+// compute_all_expectations / compute_cross_correlation (src/expectation_eval.cpp:27-110) on the device:
+// expect[l][i][j] = psi_j . (O_l psi_i), cross[l][m][i][j] = (O_l psi_i) . (O_m psi_j).  Each operator l
+// (terms[off[l] .. off[l+1])) is bound to the basis in turn; W_{l,i} = O_l psi_i is one FP64 apply.  The
+// dots are the fixed-order FP64 reductions of the Lanczos drivers.
+extern "C" qsi_status qsi_expectations(qsi_basis* b, const qsi_term* terms, const int32_t* op_offsets, int32_t n_ops,
+                                       const double* psi, int32_t nvec, double* expect, double* cross) {
+    return guarded([&]() -> qsi_status {
+        if (!b || !terms || !op_offsets || n_ops < 1 || !psi || nvec < 1 || nvec > 256 || !expect)
+            return fail(QSI_INVALID_ARG, "qsi_expectations: bad argument (1 <= nvec <= 256)");
+        for (int l = 0; l < n_ops; ++l)
+            if (op_offsets[l + 1] < op_offsets[l] || op_offsets[l] < 0)
+                return fail(QSI_INVALID_ARG, "qsi_expectations: operator offsets must not decrease");
+        const int64_t n = b->n;
+        const int64_t K = (int64_t)n_ops * nvec;  // vectors W_{l,i}, index l*nvec + i
+        cudaStream_t st = nullptr;
+        QSI_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard() {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
+        } guard{st};
+        if (cross) {
+            size_t free_b = 0, total_b = 0;
+            QSI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            const double need = ((double)K + nvec + 1) * (double)n * 8.0;
+            if (need > 0.9 * (double)free_b)
+                return fail(QSI_OOM, "qsi_expectations: %lld vectors of %lld states exceed device memory",
+                            (long long)K, (long long)n);
+        }
+        Vecs vx;
+        qsi_status s = vx.init(n, st);
+        if (s) return s;
+        DevBuf<double> P, W;
+        QSI_CUDA(P.alloc((size_t)n * nvec, st));
+        QSI_CUDA(cudaMemcpyAsync(P.p, psi, (size_t)n * nvec * 8, cudaMemcpyHostToDevice, st));
+        QSI_CUDA(W.alloc((size_t)n * (cross ? K : 1), st));
+        std::vector<double> h;
+        for (int l = 0; l < n_ops; ++l) {
+            qsi_op* op = nullptr;
+            s = qsi_op_create(b, terms + op_offsets[l], op_offsets[l + 1] - op_offsets[l], &op);
+            if (s) return s;
+            for (int i = 0; i < nvec && s == QSI_OK; ++i) {
+                double* w = W.p + (cross ? (size_t)(l * nvec + i) * n : 0);
+                QSI_CUDA(cudaStreamSynchronize(st));
+                s = launch_apply(op, P.p + (size_t)i * n, w, 1, QSI_F64, 0, op->stream);
+                if (s == QSI_OK && cudaStreamSynchronize(op->stream) != cudaSuccess) s = fail(QSI_CUDA_ERROR, "apply");
+                if (s == QSI_OK) s = vx.dots<double>(P.p, n, nvec, w, h);
+                for (int j = 0; j < nvec && s == QSI_OK; ++j) expect[((size_t)l * nvec + i) * nvec + j] = h[j];
+            }
+            qsi_op_destroy(op);
+            if (s) return s;
+        }
+        if (cross) {
+            std::vector<double> col((size_t)K);
+            for (int m = 0; m < n_ops; ++m)
+                for (int j = 0; j < nvec; ++j) {
+                    const double* wmj = W.p + (size_t)(m * nvec + j) * n;
+                    for (int64_t c0 = 0; c0 < K; c0 += 256) {  // the reduction buffers hold 256 dots
+                        const int kc = (int)std::min<int64_t>(256, K - c0);
+                        s = vx.dots<double>(W.p + (size_t)c0 * n, n, kc, wmj, h);
+                        if (s) return s;
+                        std::copy(h.begin(), h.begin() + kc, col.begin() + c0);
+                    }
+                    for (int l = 0; l < n_ops; ++l)
+                        for (int i = 0; i < nvec; ++i)
+                            cross[(((size_t)l * n_ops + m) * nvec + i) * nvec + j] = col[(size_t)l * nvec + i];
+                }
+        }
+        return QSI_OK;
+    });
+}
+
 // ------------------------------------------------------------------ FTLM
 namespace qsi {
 

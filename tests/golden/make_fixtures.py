@@ -15,6 +15,9 @@ writes small files next to this script:
   apply_ref32.npy, apply_cfg1.npy   y = H x from the reference code (seeded x)
   eigs_cfg1.json           FP64 lowest eigenvalues of the 32-spin config-1 Hamiltonian
   thermo_s4444.npz         exact E(T), C(T) of the 32-spin 4.4.4.4 sector
+  observables48.npz        ring, ring_ring, partial_vol_sl0..3 of the reference's stored .eigs.out.h5
+
+`python tests/golden/make_fixtures.py [REFERENCE_ROOT] observables` writes only the last file.
 """
 from __future__ import annotations
 
@@ -37,6 +40,7 @@ from oracle import oracle as O  # noqa: E402
 REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
 T = REF / "test"
 GOLDEN_EIGS = T / "data" / "REFERENCE_Jpm=0.0200%Bx=0.1000%By=0.1000%Bz=0.1000%.eigs.h5"
+GOLDEN_OBS = T / "data" / "REFERENCE_Jpm=0.0200%Bx=0.1000%By=0.1000%Bz=0.1000%.eigs.out.h5"
 
 
 def sha(a: np.ndarray) -> str:
@@ -140,5 +144,17 @@ def main():
     print("fixtures written to", HERE)
 
 
+def observables():
+    """The reference's eval_observables output for the golden eigenvector (test/data/...eigs.out.h5)."""
+    names = ["ring", "ring_ring"] + [f"partial_vol_sl{k}" for k in range(4)]
+    np.savez(HERE / "observables48.npz", **{k: q.read_f64_h5(GOLDEN_OBS, k) for k in names},
+             eigenvalues=q.read_f64_h5(GOLDEN_OBS, "eigenvalues"))
+    print("observables48.npz written to", HERE)
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 2 and sys.argv[2] == "observables":
+        observables()
+    else:
+        main()
+        observables()

@@ -59,3 +59,42 @@ def test_oracle_ftlm_formula_approaches_exact():
     f = O.ftlm_oracle(r, c, v, len(basis), R=32, M=60, seed=0, temps=th["T"])
     hi = th["T"] > 0.5  # FTLM with few vectors is accurate at high T
     np.testing.assert_allclose(f["C"][hi], th["C"][hi], rtol=0.15, atol=0.02)
+
+
+# The reference's stored observables (.eigs.out.h5) were computed from an eigenvector that differs from the
+# stored unit vector at the 1e-5 level (a different run), so the values agree to this absolute tolerance.
+OBS_TOL = 2e-5
+
+
+def test_oracle_observables_match_reference_output():
+    """ring, ring_ring and partial_vol of the golden eigenvector (eval_observables) by the oracle's restated
+    operators, products and expectation loops, against the reference's stored output."""
+    import json
+
+    obs = np.load(GOLDEN / "observables48.npz")
+    lat = json.load(open(GOLDEN / "lattices" / "golden48.json"))
+    basis = cases()["golden48_JpmB"][0]
+    psi = np.load(GOLDEN / "golden48_evec.npy").astype(np.float64)
+    rings = O.ring_terms_port(lat)
+    e, c = O.expectations_port(basis, rings, psi, cross=True)
+    np.testing.assert_allclose(e, obs["ring"], rtol=0, atol=OBS_TOL)
+    np.testing.assert_allclose(c, obs["ring_ring"], rtol=0, atol=OBS_TOL)
+    for sl in range(4):
+        pv, _ = O.expectations_port(basis, O.partial_vol_terms_port(lat, rings, sl), psi)
+        np.testing.assert_allclose(pv, obs[f"partial_vol_sl{sl}"], rtol=0, atol=OBS_TOL)
+
+
+def test_oracle_term_product_matches_reference_kats():
+    """operator*= restated in the oracle reproduces the reference's compiled products ("0Z 0X" etc.)."""
+    for kat in golden_json("term_kats.json"):
+        toks = kat["spec"].split()
+        if len(toks) < 2 or len(set(int(t[:-1]) for t in toks)) != 1:
+            continue
+        # a product of single-site operators on one spin, built factor by factor
+        factors = np.concatenate([O.terms_array([(1.0, t[-1], [int(t[:-1])])]) for t in toks])
+        prod = O.term_product_port(factors)
+        whole = O.terms_array([(1.0, "".join(t[-1] for t in toks), [int(t[:-1]) for t in toks])])
+        sign_p, sign_w = prod.view(np.int32)[0, 18], whole.view(np.int32)[0, 18]
+        assert sign_p == sign_w, kat["spec"]
+        if sign_w != 0:  # a vanished operator's masks carry no meaning
+            assert prod.tobytes() == whole.tobytes(), kat["spec"]

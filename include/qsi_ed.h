@@ -105,6 +105,9 @@ qsi_status qsi_h5_write_eigs(const char* path, const double* evals, int64_t nev,
 qsi_status qsi_h5_write_f64(const char* path, const char* dataset, const double* data,
                             const int64_t* dims, int32_t rank, int32_t append);
 qsi_status qsi_h5_write_string(const char* path, const char* dataset, const char* text, int32_t append);
+/* Reads a string dataset (fixed-length, or the variable-length strings the
+ * reference writes for latfile_json / dset_name) into buf (NUL-terminated). */
+qsi_status qsi_h5_read_string(const char* path, const char* dataset, char* buf, size_t len);
 /* CSV basis "0x%016hi%016lo" per line (basis_io.hpp:16-53). */
 qsi_status qsi_csv_read_basis(const char* path, uint64_t* out_lohi, int64_t cap, int64_t* n_out);
 

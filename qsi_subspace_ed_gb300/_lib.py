@@ -94,6 +94,7 @@ SIGNATURES = {
     "qsi_h5_write_eigs": [C.c_char_p, _P, _I64, _P, _I64, _I64, C.c_char_p, C.c_char_p],
     "qsi_h5_write_f64": [C.c_char_p, C.c_char_p, _P, _P, _I32, _I32],
     "qsi_h5_write_string": [C.c_char_p, C.c_char_p, C.c_char_p, _I32],
+    "qsi_h5_read_string": [C.c_char_p, C.c_char_p, C.c_char_p, C.c_size_t],
     "qsi_csv_read_basis": [C.c_char_p, _P, _I64, C.POINTER(_I64)],
     "qsi_enumerate_basis": [_I32, _P, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32,
                             C.POINTER(C.POINTER(C.c_uint64)), C.POINTER(_I64)],

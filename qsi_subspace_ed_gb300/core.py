@@ -183,6 +183,12 @@ def read_f64_h5(path, dataset: str) -> np.ndarray:
     return a.reshape(tuple(int(d) for d in dims[: rank.value])) if rank.value else a
 
 
+def _read_string_h5(path, dataset: str) -> str:
+    buf = C.create_string_buffer(65536)
+    call("qsi_h5_read_string", str(path).encode(), dataset.encode(), buf, len(buf))
+    return buf.value.decode()
+
+
 def read_basis_csv(path) -> np.ndarray:
     n = C.c_int64()
     call("qsi_csv_read_basis", str(path).encode(), None, 0, C.byref(n))

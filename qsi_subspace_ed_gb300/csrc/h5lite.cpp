@@ -688,6 +688,59 @@ extern "C" qsi_status qsi_h5_write_string(const char* path, const char* dataset,
     });
 }
 
+// The first element of a string dataset: fixed-length (class 3), or variable-length (class 9) with the text in a
+// global heap collection, which is how libhdf5 stores std::string attributes written by the reference
+// (write_string_to_hdf5, src/expectation_eval.cpp).
+extern "C" qsi_status qsi_h5_read_string(const char* path, const char* dataset, char* buf, size_t len) {
+    return guarded([&]() -> qsi_status {
+        if (!path || !dataset || !buf || len == 0) return fail(QSI_INVALID_ARG, "qsi_h5_read_string: bad argument");
+        h5::Reader R;
+        h5::Dataset d;
+        std::string text;
+        try {
+            h5::open_file(R, path);
+            d = h5::find_dataset(R, dataset);
+            if (d.type_class == 3) {
+                const uint8_t* src = h5::dataset_bytes(R, d, (uint64_t)d.type_size);
+                text.assign((const char*)src, strnlen((const char*)src, (size_t)d.type_size));
+            } else if (d.type_class == 9) {
+                const uint8_t* e = h5::dataset_bytes(R, d, 4 + (uint64_t)R.so + 4);
+                uint64_t L = 0, heap = 0, index = 0;
+                for (int i = 0; i < 4; ++i) L |= (uint64_t)e[i] << (8 * i);
+                for (int i = 0; i < R.so; ++i) heap |= (uint64_t)e[4 + i] << (8 * i);
+                for (int i = 0; i < 4; ++i) index |= (uint64_t)e[4 + R.so + i] << (8 * i);
+                const uint64_t g = heap + R.base;
+                if (std::memcmp(R.at(g, 4), "GCOL", 4) != 0) throw std::runtime_error("bad global heap signature");
+                const uint64_t end = g + R.rd(g + 8, R.sl);
+                uint64_t q = g + 8 + R.sl;
+                bool found = false;
+                while (q + 8 + R.sl <= end) {
+                    const uint64_t idx = R.rd(q, 2), size = R.rd(q + 8, R.sl);
+                    if (idx == 0) break;  // free space
+                    if (idx == index) {
+                        const uint8_t* src = R.at(q + 8 + R.sl, size);
+                        text.assign((const char*)src, (size_t)std::min<uint64_t>(L, size));
+                        found = true;
+                        break;
+                    }
+                    q += 8 + R.sl + ((size + 7) & ~(uint64_t)7);
+                }
+                if (!found) throw std::runtime_error("string not found in the global heap");
+            } else {
+                throw std::runtime_error("not a string dataset");
+            }
+        } catch (const std::out_of_range& e) {
+            return fail(QSI_NOT_FOUND, "%s", e.what());
+        } catch (const std::exception& e) {
+            return fail(QSI_IO_ERROR, "%s/%s: %s", path, dataset, e.what());
+        }
+        const size_t n = std::min(len - 1, text.size());
+        std::memcpy(buf, text.data(), n);
+        buf[n] = 0;
+        return QSI_OK;
+    });
+}
+
 extern "C" qsi_status qsi_csv_read_basis(const char* path, uint64_t* out_lohi, int64_t cap, int64_t* n_out) {
     return guarded([&]() -> qsi_status {
         if (!path || !n_out) return fail(QSI_INVALID_ARG, "qsi_csv_read_basis: null argument");

@@ -142,3 +142,30 @@ def test_hamiltonian_builders():
     assert len(Hz.diagonal_terms) == 32 and len(Hz.off_diag_terms) == 64
     with pytest.raises(RuntimeError):
         q.build_hamiltonian(q.Lattice.from_dict({**lat.data, "__version__": "1.0"}), 0.02, [0, 0, 0])
+
+
+def test_cli_names_and_flags():
+    """Basis-file and output naming of the reference executables, and their flags."""
+    from qsi_subspace_ed_gb300 import cli
+
+    assert str(cli.get_basis_file("a/pyro_2,0,0_0,2,0_0,0,3.json", 0)) == "a/pyro_2,0,0_0,2,0_0,0,3.0.basis.h5"
+    assert str(cli.get_basis_file("a/x.json", 1, True)) == "a/x.1.basis.partitioned.h5"
+    assert str(cli.get_basis_file("a/x", 2)) == "a/x.2.basis.h5"
+    a = cli.diag_parser().parse_args(["L.json", "--Jpm", "0.02", "--B", "0.1", "0.1", "0.1", "-n", "1", "-N", "1",
+                                      "--algorithm", "mfeig0", "-k", "20", "--rng_seed", "11", "--atol", "-9",
+                                      "--rtol", "-9", "-o", "out"])
+    assert (a.ncv, a.rng_seed, a.atol, a.rtol, a.algorithm, a.max_iters) == (20, 11, -9, -9, "mfeig0", 1000)
+    with pytest.raises(SystemExit):
+        cli.diag_parser().parse_args(["L.json", "--g", "1", "1", "1", "1", "--B", "0", "0", "0", "-o", "o"])
+    f = cli.ftlm_parser().parse_args(["L.json", "--g", "1", "2", "3", "4", "-o", "o", "--T_min", "0.1", "--T_max", "2"])
+    assert (f.n_randvecs, f.n_temps, f.ncv) == (20, 100, 15)
+
+
+def test_h5_string_round_trip(tmp_path):
+    from qsi_subspace_ed_gb300.core import _read_string_h5
+
+    p = tmp_path / "s.h5"
+    q._lib.call("qsi_h5_write_string", str(p).encode(), b"latfile_json", b"pyro_2,0,0_0,2,0_0,0,3.json", 0)
+    q._lib.call("qsi_h5_write_string", str(p).encode(), b"dset_name", b"basis", 1)
+    assert _read_string_h5(p, "latfile_json") == "pyro_2,0,0_0,2,0_0,0,3.json"
+    assert _read_string_h5(p, "dset_name") == "basis"

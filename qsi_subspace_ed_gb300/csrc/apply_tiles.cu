@@ -376,12 +376,13 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                             FF2 acc[2];  // vectors (0, 1) and (2, 3) of this lane
 #pragma unroll
                             for (int i = 0; i < 2; ++i) acc[i] = FF2{0, 0};
-                            for (int s0 = 0; s0 < steps; s0 += kU) {
-                                float4 xv[kU];
-                                float2 ck[kU];
+                            auto run_batch = [&](int s0, auto width) {
+                                constexpr int W = decltype(width)::value;
+                                float4 xv[W];
+                                float2 ck[W];
                                 uint32_t dg = 0;  // bit u: slot u holds the diagonal
 #pragma unroll
-                                for (int u = 0; u < kU; ++u) {
+                                for (int u = 0; u < W; ++u) {
                                     const int k = kb + s0 + u;
                                     const uint32_t J = (s0 + u < nl) ? hJ[k] : kEmpty;
                                     if (J != kEmpty && (J & kDiagSlot)) dg |= 1u << u;
@@ -391,12 +392,21 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                                                                 x + (int64_t)(J & ~kDiagSlot) * R + r0 + rr);
                                 }
 #pragma unroll
-                                for (int u = 0; u < kU; ++u) {
+                                for (int u = 0; u < W; ++u) {
                                     const bool all = (dg >> u) & 1;
                                     const uint64_t ch = pk2(ck[u].x, ck[u].x), cn = pk2(-ck[u].x, -ck[u].x),
                                                    cl = pk2(ck[u].y, ck[u].y);
                                     ff2_fma(acc[0], ch, cn, cl, pk2(tol_select(xv[u].x, all), tol_select(xv[u].y, all)));
                                     ff2_fma(acc[1], ch, cn, cl, pk2(tol_select(xv[u].z, all), tol_select(xv[u].w, all)));
+                                }
+                            };
+                            for (int s0 = 0; s0 < steps;) {  // full batches, and a half batch for a short tail
+                                if (steps - s0 > kU / 2) {
+                                    run_batch(s0, std::integral_constant<int, kU>{});
+                                    s0 += kU;
+                                } else {
+                                    run_batch(s0, std::integral_constant<int, kU / 2>{});
+                                    s0 += kU / 2;
                                 }
                             }
                             const int64_t rl = tile * 32 + l;

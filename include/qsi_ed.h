@@ -202,15 +202,17 @@ qsi_status qsi_op_info(const qsi_op* op, int32_t* n_offdiag, int32_t* n_pruned,
 qsi_status qsi_op_set_kernel(qsi_op* op, int32_t kernel, int32_t use_hash, int32_t list_cap);
 /* Launch settings of the tile kernels, kept separately for single-vector
  * applies (which = 0) and batched applies (which = 1; -1 sets both):
- * grid_bps = blocks per SM (0 = built-in choice), vec_chunk = vectors per
- * pass of the FP32 batched kernel (0, 16, 32, 64 or 128; 0 = up to 128).
- * qsi_op_get_tuning also reports the kernel, use_hash (as qsi_op_set_kernel
- * takes it) and list_cap of that class.  No counterpart in the reference (its
- * apply is an OpenMP loop with nothing to tune); results do not depend on
- * these settings. */
-qsi_status qsi_op_set_tuning(qsi_op* op, int32_t which, int32_t grid_bps, int32_t vec_chunk);
+ * grid_bps = blocks per SM (0 = built-in choice), vec_width = FP32 vectors
+ * per lane of the batched kernel (0 or 4, or 8), vec_chunk = vectors per pass
+ * (0, 16, 32, 64, 128 or 256; 0 = 32 lanes' worth).  qsi_op_get_tuning also
+ * reports the kernel, use_hash (as qsi_op_set_kernel takes it) and list_cap
+ * of that class.  No counterpart in the reference (its apply is an OpenMP
+ * loop with nothing to tune); results do not depend on these settings. */
+qsi_status qsi_op_set_tuning(qsi_op* op, int32_t which, int32_t grid_bps, int32_t vec_chunk,
+                             int32_t vec_width);
 qsi_status qsi_op_get_tuning(const qsi_op* op, int32_t which, int32_t* kernel, int32_t* use_hash,
-                             int32_t* list_cap, int32_t* grid_bps, int32_t* vec_chunk);
+                             int32_t* list_cap, int32_t* grid_bps, int32_t* vec_chunk,
+                             int32_t* vec_width);
 /* Autotuner: times applies of R vectors of type dtype (x, y device buffers
  * of dim*R elements, or NULL for scratch the call allocates and frees) and
  * keeps, for the class of R (single vector or batched), the fastest lookup

@@ -115,9 +115,9 @@ SIGNATURES = {
     "qsi_op_info": [_P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32)],
     "qsi_op_write_mtx": [_P, C.c_char_p, _D, C.POINTER(_I64)],
     "qsi_expectations": [_P, _P, _P, _I32, _P, _I32, _P, _P],
-    "qsi_op_set_tuning": [_P, _I32, _I32, _I32],
+    "qsi_op_set_tuning": [_P, _I32, _I32, _I32, _I32],
     "qsi_op_get_tuning": [_P, _I32, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32),
-                          C.POINTER(_I32)],
+                          C.POINTER(_I32), C.POINTER(_I32)],
     "qsi_op_autotune": [_P, _P, _P, _I32, _I32, _I32, _I32, C.c_char_p, C.c_size_t],
     "qsi_op_triplets": [_P, _D, _P, _P, _P, _I64, C.POINTER(_I64)],
     "qsi_op_count_misses": [_P, C.POINTER(_I64)],

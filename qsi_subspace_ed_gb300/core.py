@@ -334,18 +334,18 @@ class LazyOpSum:
         call("qsi_op_info", self._h, *[C.byref(a) for a in v])
         return dict(zip(("offdiag", "pruned", "diag_classes", "diag_generic"), (a.value for a in v)))
 
-    def set_tuning(self, grid_bps: int = 0, vec_chunk: int = 0, which: int = -1) -> None:
-        """Blocks per SM of the tile kernels and vectors per pass of the FP32 batched kernel (0 = built-in)
-        for single-vector (which=0), batched (1) or both (-1) applies."""
-        call("qsi_op_set_tuning", self._h, int(which), int(grid_bps), int(vec_chunk))
+    def set_tuning(self, grid_bps: int = 0, vec_chunk: int = 0, which: int = -1, vec_width: int = 0) -> None:
+        """Blocks per SM of the tile kernels, vectors per pass and vectors per lane (4 or 8) of the FP32 batched
+        kernel (0 = built-in) for single-vector (which=0), batched (1) or both (-1) applies."""
+        call("qsi_op_set_tuning", self._h, int(which), int(grid_bps), int(vec_chunk), int(vec_width))
 
     def tuning(self, which: int = 0) -> dict:
         """Launch settings of single-vector (which=0) or batched (1) applies."""
-        v = [C.c_int32() for _ in range(5)]
+        v = [C.c_int32() for _ in range(6)]
         call("qsi_op_get_tuning", self._h, int(which), *[C.byref(a) for a in v])
-        k, h, cap, g, vc = (a.value for a in v)
+        k, h, cap, g, vc, vw = (a.value for a in v)
         return {"kernel": k, "use_hash": h & 1, "fp64_accumulate": bool(h & 2), "list_cap": cap, "grid_bps": g,
-                "vec_chunk": vc, "bucket_bits": self.basis.index_info()["bucket_bits"]}
+                "vec_chunk": vc, "vec_width": vw, "bucket_bits": self.basis.index_info()["bucket_bits"]}
 
     def autotune(self, R: int = 1, dtype: str = "f64", X=None, Y=None, tune_index: bool = False,
                  tune_lookup: bool = False, reps: int = 2) -> str:

@@ -235,14 +235,19 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, cons
     }
 }
 
-// KM value selecting 16-byte FP32 gathers (see batched_body), and the bases, vector counts and pointers it
-// takes.  Its hit lists mark the diagonal slot with the top bit of the row index.
+// KM values selecting 16-byte FP32 gathers of 4 (kVec4) or 8 (kVec8) vectors per lane (see batched_body), and
+// the bases, vector counts and pointers each takes.  Their hit lists mark the diagonal slot with the top bit of
+// the row index.
 constexpr int kVec4 = 0;
+constexpr int kVec8 = -1;
 constexpr uint32_t kDiagSlot = 0x80000000u;
 inline bool vec4_ok(int64_t n, int R, const void* x, const void* y) {
     return n < (int64_t)kDiagSlot - 1 && R >= 16 && (R & 3) == 0 &&
            (R <= 128 ? (R & (R - 1)) == 0 : (R & 127) == 0) &&
            ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
+}
+inline bool vec8_ok(int64_t n, int R, const void* x, const void* y) {
+    return vec4_ok(n, R, x, y) && R >= 32 && (R <= 256 ? (R & (R - 1)) == 0 : (R & 255) == 0);
 }
 
 // Body of the batched tile kernel for one block (block_id of n_blocks working on this operator).
@@ -260,15 +265,17 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
     double* hc = reinterpret_cast<double*>(adm + n_rounds * 32);  // coefficients (8-byte aligned)
     float2* hcf = reinterpret_cast<float2*>(hc);                   // the same slots as (hi, lo) floats
     uint32_t* hJ = reinterpret_cast<uint32_t*>(hc + cap);
-    // KM == kVec4 (FP32, R accepted by vec4_ok): 16-byte gathers.  A lane owns 4 consecutive vectors,
-    // lpc lanes cover one column's vectors (up to 128 per pass), and the warp's cpw = 32/lpc lane groups
-    // sum cpw rows at once.  Otherwise a lane owns KM vectors and the warp sums one row at a time.
-    constexpr bool v4 = (KM == kVec4);
+    // KM == kVec4 / kVec8 (FP32, R accepted by vec4_ok / vec8_ok): 16-byte gathers.  A lane owns VPL = 4 or 8
+    // consecutive vectors, lpc lanes cover one column's vectors (up to 32*VPL per pass), and the warp's
+    // cpw = 32/lpc lane groups sum cpw rows at once.  Otherwise a lane owns KM vectors and the warp sums one
+    // row at a time.
+    constexpr bool v4 = (KM == kVec4 || KM == kVec8);
+    constexpr int VPL = (KM == kVec8) ? 8 : 4;
     static_assert(!v4 || kFF, "16-byte gathers are for FP32 vectors with double-float accumulation");
     int lpc = 32, cpw = 1;
     if constexpr (v4) {
-        const int vc = P.vchunk > 0 ? P.vchunk : 128;
-        lpc = (R >= vc ? vc : R) / 4;
+        const int vc = P.vchunk > 0 ? P.vchunk : 32 * VPL;
+        lpc = (R >= vc ? vc : R) / VPL;
         cpw = 32 / lpc;
     }
     const int64_t ntiles = (P.B.n + 31) >> 5;
@@ -353,16 +360,17 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                 // FP32 storage, double-float accumulation, no FP64 instruction.  The chunk's hit list
                 // is walked in order across row boundaries with kU column gathers in flight.
                 static_assert(std::is_same<XT, float>::value, "double-float accumulation is for FP32 vectors");
-                constexpr int kU = 8;
+                constexpr int kU = (VPL == 8) ? 4 : 8;  // column gathers in flight per lane (kU * VPL floats)
                 const int kbeg = __shfl_sync(0xffffffffu, base, row_start);
                 const int last = row_end - 1;
                 const int kend = __shfl_sync(0xffffffffu, base + pc, last);
                 if constexpr (v4) {
-                    // Lane group g (lpc lanes, 4 vectors each) sums rows row_start + g, + g + cpw, ...: each
+                    // Lane group g (lpc lanes, VPL vectors each) sums rows row_start + g, + g + cpw, ...: each
                     // group walks its own row's slots, kU column gathers in flight per lane, and the warp
                     // steps as long as its longest row of the set.
-                    const int g = lane / lpc, rr = 4 * (lane % lpc);
-                    for (int r0 = 0; r0 < R; r0 += 4 * lpc) {
+                    constexpr int NQ = VPL / 4;  // float4 loads per lane and column
+                    const int g = lane / lpc, rr = VPL * (lane % lpc);
+                    for (int r0 = 0; r0 < R; r0 += VPL * lpc) {
                         for (int l0 = row_start; l0 < row_end; l0 += cpw) {
                             const int l = l0 + g;
                             const bool mine = l < row_end;
@@ -373,12 +381,12 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                             int steps = nl;
 #pragma unroll
                             for (int o = 16; o; o >>= 1) steps = max(steps, __shfl_xor_sync(0xffffffffu, steps, o));
-                            FF2 acc[2];  // vectors (0, 1) and (2, 3) of this lane
+                            FF2 acc[2 * NQ];  // vector pairs (0, 1), (2, 3), ... of this lane
 #pragma unroll
-                            for (int i = 0; i < 2; ++i) acc[i] = FF2{0, 0};
+                            for (int i = 0; i < 2 * NQ; ++i) acc[i] = FF2{0, 0};
                             auto run_batch = [&](int s0, auto width) {
                                 constexpr int W = decltype(width)::value;
-                                float4 xv[W];
+                                float4 xv[W][NQ];
                                 float2 ck[W];
                                 uint32_t dg = 0;  // bit u: slot u holds the diagonal
 #pragma unroll
@@ -387,17 +395,24 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                                     const uint32_t J = (s0 + u < nl) ? hJ[k] : kEmpty;
                                     if (J != kEmpty && (J & kDiagSlot)) dg |= 1u << u;
                                     ck[u] = (J == kEmpty) ? make_float2(0.f, 0.f) : hcf[k];
-                                    xv[u] = (J == kEmpty) ? make_float4(0.f, 0.f, 0.f, 0.f)
-                                                          : *reinterpret_cast<const float4*>(
-                                                                x + (int64_t)(J & ~kDiagSlot) * R + r0 + rr);
+                                    const float4* src =
+                                        reinterpret_cast<const float4*>(x + (int64_t)(J & ~kDiagSlot) * R + r0 + rr);
+#pragma unroll
+                                    for (int q = 0; q < NQ; ++q)
+                                        xv[u][q] = (J == kEmpty) ? make_float4(0.f, 0.f, 0.f, 0.f) : src[q];
                                 }
 #pragma unroll
                                 for (int u = 0; u < W; ++u) {
                                     const bool all = (dg >> u) & 1;
                                     const uint64_t ch = pk2(ck[u].x, ck[u].x), cn = pk2(-ck[u].x, -ck[u].x),
                                                    cl = pk2(ck[u].y, ck[u].y);
-                                    ff2_fma(acc[0], ch, cn, cl, pk2(tol_select(xv[u].x, all), tol_select(xv[u].y, all)));
-                                    ff2_fma(acc[1], ch, cn, cl, pk2(tol_select(xv[u].z, all), tol_select(xv[u].w, all)));
+#pragma unroll
+                                    for (int q = 0; q < NQ; ++q) {
+                                        ff2_fma(acc[2 * q], ch, cn, cl,
+                                                pk2(tol_select(xv[u][q].x, all), tol_select(xv[u][q].y, all)));
+                                        ff2_fma(acc[2 * q + 1], ch, cn, cl,
+                                                pk2(tol_select(xv[u][q].z, all), tol_select(xv[u][q].w, all)));
+                                    }
                                 }
                             };
                             for (int s0 = 0; s0 < steps;) {  // full batches, and a half batch for a short tail
@@ -412,14 +427,19 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                             const int64_t rl = tile * 32 + l;
                             if (mine && rl < P.B.n) {
                                 float4* yp = reinterpret_cast<float4*>(y + rl * R + r0 + rr);
-                                if (accumulate) {
-                                    const float4 yv = *yp;
-                                    const uint64_t one = pk2(1.0f, 1.0f), mone = pk2(-1.0f, -1.0f), zero = pk2(0.f, 0.f);
-                                    ff2_fma(acc[0], one, mone, zero, pk2(yv.x, yv.y));
-                                    ff2_fma(acc[1], one, mone, zero, pk2(yv.z, yv.w));
+#pragma unroll
+                                for (int q = 0; q < NQ; ++q) {
+                                    if (accumulate) {
+                                        const float4 yv = yp[q];
+                                        const uint64_t one = pk2(1.0f, 1.0f), mone = pk2(-1.0f, -1.0f),
+                                                       zero = pk2(0.f, 0.f);
+                                        ff2_fma(acc[2 * q], one, mone, zero, pk2(yv.x, yv.y));
+                                        ff2_fma(acc[2 * q + 1], one, mone, zero, pk2(yv.z, yv.w));
+                                    }
+                                    const float2 a = unpk2(add2(acc[2 * q].hi, acc[2 * q].lo)),
+                                                 b = unpk2(add2(acc[2 * q + 1].hi, acc[2 * q + 1].lo));
+                                    yp[q] = make_float4(a.x, a.y, b.x, b.y);
                                 }
-                                const float2 a = unpk2(add2(acc[0].hi, acc[0].lo)), b = unpk2(add2(acc[1].hi, acc[1].lo));
-                                *yp = make_float4(a.x, a.y, b.x, b.y);
                             }
                         }
                     }
@@ -539,7 +559,7 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
 }
 
 template <typename XT, class LK, bool kFF, int KM>
-__global__ void __launch_bounds__(256, KM == kVec4 ? 2 : 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
+__global__ void __launch_bounds__(256, KM <= kVec4 ? 2 : 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
                                                             XT* __restrict__ y, int R, int accumulate, int cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     batched_body<XT, LK, kFF, KM>(P, lk, x, y, R, accumulate, cap, blockIdx.x, gridDim.x, smem_raw);
@@ -562,7 +582,7 @@ struct SectorLaunch {
 };
 
 template <int KM, class LK>
-__global__ void __launch_bounds__(256, KM == kVec4 ? 2 : 3) k_apply_sectors(const SectorLaunch* __restrict__ secs, int n_secs,
+__global__ void __launch_bounds__(256, KM <= kVec4 ? 2 : 3) k_apply_sectors(const SectorLaunch* __restrict__ secs, int n_secs,
                                                           int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SectorLaunch L;
@@ -721,8 +741,9 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
                 k<<<one_wave(k, block, smem, ntiles, T.grid_bps), block, smem, st>>>(P, lk, (const double*)x, (double*)y, R,
                                                                          accumulate, cap);
             } else if (op->ff_accumulate) {
-                auto k = vec4_ok(P.B.n, R, x, y) ? k_apply_tile_batched<float, LK, true, kVec4>
-                                                 : k_apply_tile_batched<float, LK, true, KM>;
+                auto k = (T.vec_width == 8 && vec8_ok(P.B.n, R, x, y)) ? k_apply_tile_batched<float, LK, true, kVec8>
+                         : vec4_ok(P.B.n, R, x, y)                        ? k_apply_tile_batched<float, LK, true, kVec4>
+                                                                          : k_apply_tile_batched<float, LK, true, KM>;
                 set_smem(k, smem);
                 k<<<one_wave(k, block, smem, ntiles, T.grid_bps), block, smem, st>>>(P, lk, (const float*)x, (float*)y, R,
                                                                          accumulate, cap);
@@ -750,6 +771,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
                         SectorPlan& plan, const double* weights) {
     std::vector<SectorLaunch> L(n);
     plan.vec4 = true;
+    plan.vec8 = true;
     plan.hash = true;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -774,6 +796,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         L[s].cap = cap;
         maxR = std::max(maxR, R[s]);
         plan.vec4 = plan.vec4 && vec4_ok(op->basis->n, R[s], X[s], Y[s]);
+        plan.vec8 = plan.vec8 && op->tune[1].vec_width == 8 && vec8_ok(op->basis->n, R[s], X[s], Y[s]);
         work_total += weights ? weights[s] : (double)op->basis->n * R[s];
     }
     if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "sector launch: %zu bytes of shared memory needed", smem);
@@ -805,7 +828,8 @@ qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int acc
         set_smem(k, plan.smem);
         k<<<plan.grid, 256, plan.smem, st>>>((const SectorLaunch*)d_records, plan.n, accumulate);
     };
-    if (plan.vec4) go(std::integral_constant<int, kVec4>{});
+    if (plan.vec8) go(std::integral_constant<int, kVec8>{});
+    else if (plan.vec4) go(std::integral_constant<int, kVec4>{});
     else if (plan.maxR <= 32) go(std::integral_constant<int, 1>{});
     else if (plan.maxR <= 64) go(std::integral_constant<int, 2>{});
     else go(std::integral_constant<int, 4>{});

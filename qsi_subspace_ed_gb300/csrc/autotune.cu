@@ -86,20 +86,25 @@ struct Trial {
 
 using namespace qsi;
 
-extern "C" qsi_status qsi_op_set_tuning(qsi_op* op, int32_t which, int32_t grid_bps, int32_t vec_chunk) {
+extern "C" qsi_status qsi_op_set_tuning(qsi_op* op, int32_t which, int32_t grid_bps, int32_t vec_chunk,
+                                        int32_t vec_width) {
     if (!op || which < -1 || which > 1 || grid_bps < 0 || grid_bps > 64 ||
-        !(vec_chunk == 0 || vec_chunk == 16 || vec_chunk == 32 || vec_chunk == 64 || vec_chunk == 128))
+        !(vec_chunk == 0 || vec_chunk == 16 || vec_chunk == 32 || vec_chunk == 64 || vec_chunk == 128 ||
+          vec_chunk == 256) ||
+        !(vec_width == 0 || vec_width == 4 || vec_width == 8))
         return fail(QSI_INVALID_ARG, "qsi_op_set_tuning: bad argument");
     for (int c = 0; c < 2; ++c)
         if (which < 0 || which == c) {
             op->tune[c].grid_bps = grid_bps;
             op->tune[c].vec_chunk = vec_chunk;
+            op->tune[c].vec_width = vec_width;
         }
     return QSI_OK;
 }
 
 extern "C" qsi_status qsi_op_get_tuning(const qsi_op* op, int32_t which, int32_t* kernel, int32_t* use_hash,
-                                        int32_t* list_cap, int32_t* grid_bps, int32_t* vec_chunk) {
+                                        int32_t* list_cap, int32_t* grid_bps, int32_t* vec_chunk,
+                                        int32_t* vec_width) {
     if (!op || which < 0 || which > 1) return fail(QSI_INVALID_ARG, "qsi_op_get_tuning: bad argument");
     const qsi_tuning& T = op->tune[which];
     if (kernel) *kernel = op->kernel;
@@ -107,6 +112,7 @@ extern "C" qsi_status qsi_op_get_tuning(const qsi_op* op, int32_t which, int32_t
     if (list_cap) *list_cap = T.list_cap;
     if (grid_bps) *grid_bps = T.grid_bps;
     if (vec_chunk) *vec_chunk = T.vec_chunk;
+    if (vec_width) *vec_width = T.vec_width;
     return QSI_OK;
 }
 
@@ -167,14 +173,25 @@ extern "C" qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_
         const bool v4 = dtype == QSI_F32 && R > 1 && op->ff_accumulate && R >= 16 && (R & 3) == 0 &&
                         (R <= 128 ? (R & (R - 1)) == 0 : (R & 127) == 0);
         if (s == QSI_OK && v4) {
+            // vectors per lane (8 takes R >= 32, powers of two up to 256 or multiples of 256), then per pass
+            const bool v8 = R >= 32 && (R <= 256 ? (R & (R - 1)) == 0 : (R & 255) == 0);
+            if (v8) {
+                int cur = cfg.vec_width;
+                s = T.sweep("vec_width", {4, 8}, cur, best, [&](int v) {
+                    cfg.vec_width = v;
+                    return QSI_OK;
+                });
+            }
             std::vector<int> vcs;
-            for (int v : {16, 32, 64, 128})
-                if (v <= R) vcs.push_back(v);
+            const int vpl = cfg.vec_width == 8 ? 8 : 4;
+            for (int v : {16, 32, 64, 128, 256})
+                if (v <= R && v >= vpl && v <= 32 * vpl) vcs.push_back(v);
             int cur = cfg.vec_chunk;
-            s = T.sweep("vec_chunk", vcs, cur, best, [&](int v) {
-                cfg.vec_chunk = v;
-                return QSI_OK;
-            });
+            if (s == QSI_OK)
+                s = T.sweep("vec_chunk", vcs, cur, best, [&](int v) {
+                    cfg.vec_chunk = v;
+                    return QSI_OK;
+                });
         }
         if (s == QSI_OK) {
             std::vector<int> g = (R == 1) ? std::vector<int>{3, 4, 6, 12, 16} : std::vector<int>{1, 2, 3, 4, 8};
@@ -193,8 +210,9 @@ extern "C" qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_
         }
         if (s == QSI_OK) {
             char line[128];
-            std::snprintf(line, sizeof line, "best use_hash=%d bucket_bits=%d grid_bps=%d vec_chunk=%d list_cap=%d %.3f ms\n",
-                          cfg.use_hash, op->basis->bits, cfg.grid_bps, cfg.vec_chunk, cfg.list_cap, best);
+            std::snprintf(line, sizeof line,
+                          "best use_hash=%d bucket_bits=%d grid_bps=%d vec_width=%d vec_chunk=%d list_cap=%d %.3f ms\n",
+                          cfg.use_hash, op->basis->bits, cfg.grid_bps, cfg.vec_width, cfg.vec_chunk, cfg.list_cap, best);
             T.log += line;
         }
         if (T.e0) cudaEventDestroy(T.e0);

@@ -210,14 +210,16 @@ def test_double_float_accumulation_matches_fp64(built):
     np.testing.assert_allclose(Yacc, 2 * Y64, rtol=1e-6, atol=1e-6 * np.abs(Y64).max())
 
 
-@pytest.mark.parametrize("R", [16, 24, 32, 64, 128, 256])
-def test_fp32_batched_widths(built, R):
+@pytest.mark.parametrize("vw", [4, 8])
+@pytest.mark.parametrize("R", [16, 24, 32, 64, 128, 256, 512])
+def test_fp32_batched_widths(built, R, vw):
     """FP32 batched applies at vector counts that take 16-byte gathers (16..128, multiples of 128) and one that
     does not (24): each within one FP32 ulp of FP64 accumulation, equal to the oracle's FP64 apply to FP32
     rounding, and bitwise independent of the hit-list size."""
     basis, H, b, op = built["ref32_JpmB"]
     X = np.random.default_rng(R).standard_normal((len(basis), R)).astype(np.float32)
     Yff, Y64, Ysmall = np.zeros_like(X), np.zeros_like(X), np.zeros_like(X)
+    op.set_tuning(0, 0, which=1, vec_width=vw)
     op.set_kernel(1, 1)
     op.apply_batched(X, Yff)
     op.set_kernel(1, 1, list_cap=8)
@@ -225,6 +227,7 @@ def test_fp32_batched_widths(built, R):
     op.set_kernel(1, 1 | 2)
     op.apply_batched(X, Y64)
     op.set_kernel(1, 1)
+    op.set_tuning(0, 0, which=1)
     assert np.array_equal(Yff, Ysmall)
     assert np.all(np.abs(Yff - Y64) <= np.spacing(np.abs(Y64).astype(np.float32)))
     for col in (0, R - 1):
@@ -266,11 +269,11 @@ def test_autotune_keeps_results(built):
     op.evaluate(x, y1)
     op.apply_batched(X, Y1)
     assert np.array_equal(y0, y1) and np.array_equal(Y0, Y1)
-    for vc in (16, 32, 64):
-        op.set_tuning(t["grid_bps"], vc, which=1)
+    for vw, vc in ((4, 16), (4, 32), (4, 64), (8, 16), (8, 32), (8, 64)):
+        op.set_tuning(t["grid_bps"], vc, which=1, vec_width=vw)
         Y2 = np.zeros_like(X)
         op.apply_batched(X, Y2)
-        assert np.array_equal(Y0, Y2)
+        assert np.array_equal(Y0, Y2), (vw, vc)
     with pytest.raises(q.QsiError):
         op.set_tuning(0, 48)
     op.set_tuning(0, 0)

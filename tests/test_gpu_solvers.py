@@ -101,13 +101,17 @@ def test_ftlm_sector_launch_lookup_and_tuning_independent():
     launch settings."""
     cs = cases()
     ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["cfg1", "s4444"]]
-    ref = q.ftlm(ops, [32, 16], M=20, seed=4, precision="mixed")
+    ref = q.ftlm(ops, [32, 32], M=20, seed=4, precision="mixed")
+    for vw in (4, 8):
+        for op in ops:
+            op.set_kernel(1, 0)  # bucket table
+            op.set_tuning(4, 16, which=1, vec_width=vw)
+        other = q.ftlm(ops, [32, 32], M=20, seed=4, precision="mixed")
+        for (a, b), (c, d) in zip(ref, other):
+            assert np.array_equal(a, c) and np.array_equal(b, d)
     for op in ops:
-        op.set_kernel(1, 0)  # bucket table
-        op.set_tuning(4, 16, which=1)
-    other = q.ftlm(ops, [32, 16], M=20, seed=4, precision="mixed")
-    for (a, b), (c, d) in zip(ref, other):
-        assert np.array_equal(a, c) and np.array_equal(b, d)
+        op.set_kernel(1, 1)
+        op.set_tuning(0, 0)
 
 
 def test_tridiag_ritz_matches_numpy():

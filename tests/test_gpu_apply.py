@@ -324,3 +324,64 @@ def test_matrix_market_export(built, name, tmp_path):
     M = scipy.io.mmread(str(p_gpu)).tocsr()
     ref = O.csr_from_triplets(r, c, v, len(basis))
     assert abs(M - ref).max() == 0
+
+
+def _wide_case():
+    """The 32-spin Q=0 basis and ring/Zeeman Hamiltonian with spin i moved to bit 4i+3 (states up to 128 bits,
+    beyond the 96 bits the hash index takes): lookups go through the bucket table."""
+    basis, H = cases()["cfg1"]
+    spins = [(int(lo) | (int(hi) << 64)) for lo, hi in basis]
+    wide = []
+    for s in spins:
+        v = 0
+        for i in range(32):
+            if (s >> i) & 1:
+                v |= 1 << (4 * i + 3)
+        wide.append(v)
+    wide.sort()
+    lohi = np.array([[v & (2**64 - 1), v >> 64] for v in wide], dtype=np.uint64)
+    specs = [(c, ops, [4 * i + 3 for i in ids]) for c, ops, ids in H.specs()]
+    Hw = q.SymbolicOpSum()
+    for c, ops, ids in specs:
+        Hw.add_term(c, q.SymbolicPMROperator(ops, ids))
+    return lohi, Hw, specs
+
+
+def test_states_up_to_128_bits():
+    lohi, Hw, specs = _wide_case()
+    assert int(lohi[:, 1].max()) >> 62  # bits above 96 are in use
+    b = q.ZBasis(lohi)
+    assert not b.index_info()["hash"]
+    op = q.LazyOpSum(b, Hw)
+    r, c, v = op.triplets()
+    assert O.triplet_digest(r, c, v) == O.triplet_digest(*O.triplets_port(lohi, specs))
+    x = np.random.default_rng(8).standard_normal(len(lohi))
+    y = np.zeros_like(x)
+    op.evaluate(x, y)
+    ref = O.apply_port(lohi, specs, x, threads=1)
+    np.testing.assert_allclose(y, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    X = np.random.default_rng(9).standard_normal((len(lohi), 64)).astype(np.float32)
+    for vw in (4, 8):
+        op.set_tuning(0, 0, which=1, vec_width=vw)
+        Y = np.zeros_like(X)
+        op.apply_batched(X, Y)
+        ref0 = O.apply_port(lohi, specs, X[:, 5].astype(np.float64), threads=1)
+        np.testing.assert_allclose(Y[:, 5], ref0, rtol=0, atol=4e-6 * np.abs(ref0).max())
+
+
+def test_degenerate_sizes():
+    """One-state basis, an operator without terms, and vector counts of 1 and 3 (no 16-byte path)."""
+    one = np.array([[5, 0]], dtype=np.uint64)
+    op = q.LazyOpSum(q.ZBasis(one), q.SymbolicOpSum())
+    y = np.ones(1)
+    op.evaluate(np.array([2.0]), y)
+    assert y[0] == 0.0
+    basis, H = cases()["s4444"]
+    op2 = q.LazyOpSum(q.ZBasis(basis), H)
+    for R in (1, 3):
+        X = np.random.default_rng(R).standard_normal((len(basis), R))
+        Y = np.zeros_like(X)
+        op2.apply_batched(X, Y)
+        for col in range(R):
+            ref = O.apply_port(basis, H.specs(), X[:, col], threads=1)
+            np.testing.assert_allclose(Y[:, col], ref, rtol=0, atol=1e-12 * np.abs(ref).max())

@@ -203,8 +203,8 @@ qsi_status qsi_op_set_kernel(qsi_op* op, int32_t kernel, int32_t use_hash, int32
 /* Launch settings of the tile kernels, kept separately for single-vector
  * applies (which = 0) and batched applies (which = 1; -1 sets both):
  * grid_bps = blocks per SM (0 = built-in choice), vec_width = FP32 vectors
- * per lane of the batched kernel (0 or 4, or 8), vec_chunk = vectors per pass
- * (0, 16, 32, 64, 128 or 256; 0 = 32 lanes' worth).  qsi_op_get_tuning also
+ * per lane of the batched kernel (0 or 4, 8, 16), vec_chunk = vectors per pass
+ * (0, 16, 32, 64, 128, 256 or 512; 0 = 32 lanes' worth).  qsi_op_get_tuning also
  * reports the kernel, use_hash (as qsi_op_set_kernel takes it) and list_cap
  * of that class.  No counterpart in the reference (its apply is an OpenMP
  * loop with nothing to tune); results do not depend on these settings. */

@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, cons
 // the row index.
 constexpr int kVec4 = 0;
 constexpr int kVec8 = -1;
+constexpr int kVec16 = -2;
 constexpr uint32_t kDiagSlot = 0x80000000u;
 inline bool vec4_ok(int64_t n, int R, const void* x, const void* y) {
     return n < (int64_t)kDiagSlot - 1 && R >= 16 && (R & 3) == 0 &&
@@ -248,6 +249,9 @@ inline bool vec4_ok(int64_t n, int R, const void* x, const void* y) {
 }
 inline bool vec8_ok(int64_t n, int R, const void* x, const void* y) {
     return vec4_ok(n, R, x, y) && R >= 32 && (R <= 256 ? (R & (R - 1)) == 0 : (R & 255) == 0);
+}
+inline bool vec16_ok(int64_t n, int R, const void* x, const void* y) {
+    return vec4_ok(n, R, x, y) && R >= 64 && (R <= 512 ? (R & (R - 1)) == 0 : (R & 511) == 0);
 }
 
 // Body of the batched tile kernel for one block (block_id of n_blocks working on this operator).
@@ -269,8 +273,8 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
     // consecutive vectors, lpc lanes cover one column's vectors (up to 32*VPL per pass), and the warp's
     // cpw = 32/lpc lane groups sum cpw rows at once.  Otherwise a lane owns KM vectors and the warp sums one
     // row at a time.
-    constexpr bool v4 = (KM == kVec4 || KM == kVec8);
-    constexpr int VPL = (KM == kVec8) ? 8 : 4;
+    constexpr bool v4 = (KM == kVec4 || KM == kVec8 || KM == kVec16);
+    constexpr int VPL = (KM == kVec16) ? 16 : (KM == kVec8) ? 8 : 4;
     static_assert(!v4 || kFF, "16-byte gathers are for FP32 vectors with double-float accumulation");
     int lpc = 32, cpw = 1;
     if constexpr (v4) {
@@ -360,7 +364,7 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                 // FP32 storage, double-float accumulation, no FP64 instruction.  The chunk's hit list
                 // is walked in order across row boundaries with kU column gathers in flight.
                 static_assert(std::is_same<XT, float>::value, "double-float accumulation is for FP32 vectors");
-                constexpr int kU = (VPL == 8) ? 4 : 8;  // column gathers in flight per lane (kU * VPL floats)
+                constexpr int kU = 32 / VPL;  // column gathers in flight per lane (kU * VPL = 32 floats)
                 const int kbeg = __shfl_sync(0xffffffffu, base, row_start);
                 const int last = row_end - 1;
                 const int kend = __shfl_sync(0xffffffffu, base + pc, last);
@@ -420,8 +424,9 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                                     run_batch(s0, std::integral_constant<int, kU>{});
                                     s0 += kU;
                                 } else {
-                                    run_batch(s0, std::integral_constant<int, kU / 2>{});
-                                    s0 += kU / 2;
+                                    constexpr int kH = kU / 2 > 0 ? kU / 2 : 1;
+                                    run_batch(s0, std::integral_constant<int, kH>{});
+                                    s0 += kH;
                                 }
                             }
                             const int64_t rl = tile * 32 + l;
@@ -741,7 +746,8 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
                 k<<<one_wave(k, block, smem, ntiles, T.grid_bps), block, smem, st>>>(P, lk, (const double*)x, (double*)y, R,
                                                                          accumulate, cap);
             } else if (op->ff_accumulate) {
-                auto k = (T.vec_width == 8 && vec8_ok(P.B.n, R, x, y)) ? k_apply_tile_batched<float, LK, true, kVec8>
+                auto k = (T.vec_width == 16 && vec16_ok(P.B.n, R, x, y)) ? k_apply_tile_batched<float, LK, true, kVec16>
+                         : (T.vec_width == 8 && vec8_ok(P.B.n, R, x, y))  ? k_apply_tile_batched<float, LK, true, kVec8>
                          : vec4_ok(P.B.n, R, x, y)                        ? k_apply_tile_batched<float, LK, true, kVec4>
                                                                           : k_apply_tile_batched<float, LK, true, KM>;
                 set_smem(k, smem);
@@ -772,6 +778,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
     std::vector<SectorLaunch> L(n);
     plan.vec4 = true;
     plan.vec8 = true;
+    plan.vec16 = true;
     plan.hash = true;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -797,6 +804,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         maxR = std::max(maxR, R[s]);
         plan.vec4 = plan.vec4 && vec4_ok(op->basis->n, R[s], X[s], Y[s]);
         plan.vec8 = plan.vec8 && op->tune[1].vec_width == 8 && vec8_ok(op->basis->n, R[s], X[s], Y[s]);
+        plan.vec16 = plan.vec16 && op->tune[1].vec_width == 16 && vec16_ok(op->basis->n, R[s], X[s], Y[s]);
         work_total += weights ? weights[s] : (double)op->basis->n * R[s];
     }
     if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "sector launch: %zu bytes of shared memory needed", smem);
@@ -828,7 +836,8 @@ qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int acc
         set_smem(k, plan.smem);
         k<<<plan.grid, 256, plan.smem, st>>>((const SectorLaunch*)d_records, plan.n, accumulate);
     };
-    if (plan.vec8) go(std::integral_constant<int, kVec8>{});
+    if (plan.vec16) go(std::integral_constant<int, kVec16>{});
+    else if (plan.vec8) go(std::integral_constant<int, kVec8>{});
     else if (plan.vec4) go(std::integral_constant<int, kVec4>{});
     else if (plan.maxR <= 32) go(std::integral_constant<int, 1>{});
     else if (plan.maxR <= 64) go(std::integral_constant<int, 2>{});

@@ -90,8 +90,8 @@ extern "C" qsi_status qsi_op_set_tuning(qsi_op* op, int32_t which, int32_t grid_
                                         int32_t vec_width) {
     if (!op || which < -1 || which > 1 || grid_bps < 0 || grid_bps > 64 ||
         !(vec_chunk == 0 || vec_chunk == 16 || vec_chunk == 32 || vec_chunk == 64 || vec_chunk == 128 ||
-          vec_chunk == 256) ||
-        !(vec_width == 0 || vec_width == 4 || vec_width == 8))
+          vec_chunk == 256 || vec_chunk == 512) ||
+        !(vec_width == 0 || vec_width == 4 || vec_width == 8 || vec_width == 16))
         return fail(QSI_INVALID_ARG, "qsi_op_set_tuning: bad argument");
     for (int c = 0; c < 2; ++c)
         if (which < 0 || which == c) {
@@ -175,16 +175,19 @@ extern "C" qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_
         if (s == QSI_OK && v4) {
             // vectors per lane (8 takes R >= 32, powers of two up to 256 or multiples of 256), then per pass
             const bool v8 = R >= 32 && (R <= 256 ? (R & (R - 1)) == 0 : (R & 255) == 0);
+            const bool v16 = R >= 64 && (R <= 512 ? (R & (R - 1)) == 0 : (R & 511) == 0);
             if (v8) {
                 int cur = cfg.vec_width;
-                s = T.sweep("vec_width", {4, 8}, cur, best, [&](int v) {
+                std::vector<int> widths{4, 8};
+                if (v16) widths.push_back(16);
+                s = T.sweep("vec_width", widths, cur, best, [&](int v) {
                     cfg.vec_width = v;
                     return QSI_OK;
                 });
             }
             std::vector<int> vcs;
-            const int vpl = cfg.vec_width == 8 ? 8 : 4;
-            for (int v : {16, 32, 64, 128, 256})
+            const int vpl = cfg.vec_width >= 8 ? cfg.vec_width : 4;
+            for (int v : {16, 32, 64, 128, 256, 512})
                 if (v <= R && v >= vpl && v <= 32 * vpl) vcs.push_back(v);
             int cur = cfg.vec_chunk;
             if (s == QSI_OK)

@@ -24,7 +24,7 @@ struct qsi_tuning {
     int list_cap = 256;  // hit-list entries per warp in the batched tile kernel
     int grid_bps = 0;    // tile-kernel blocks per SM (0: built-in choice)
     int vec_chunk = 0;   // vectors per pass of the 16-byte batched kernel (0: up to 32 lanes' worth)
-    int vec_width = 0;   // FP32 vectors per lane of the 16-byte batched kernel: 4 (0) or 8
+    int vec_width = 0;   // FP32 vectors per lane of the 16-byte batched kernel: 4 (0), 8 or 16
 };
 
 struct qsi_op {
@@ -68,6 +68,7 @@ struct SectorPlan {
     int maxR = 1, grid = 0, n = 0;
     bool vec4 = true;  // every sector's R and vectors take 16-byte gathers
     bool vec8 = true;  // ... of 8 vectors per lane, and every sector's batched applies are set to them
+    bool vec16 = true; // ... of 16 vectors per lane, likewise
     bool hash = true;  // every sector's batched applies look columns up through the hash index
 };
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,

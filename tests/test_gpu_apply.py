@@ -210,7 +210,7 @@ def test_double_float_accumulation_matches_fp64(built):
     np.testing.assert_allclose(Yacc, 2 * Y64, rtol=1e-6, atol=1e-6 * np.abs(Y64).max())
 
 
-@pytest.mark.parametrize("vw", [4, 8])
+@pytest.mark.parametrize("vw", [4, 8, 16])
 @pytest.mark.parametrize("R", [16, 24, 32, 64, 128, 256, 512])
 def test_fp32_batched_widths(built, R, vw):
     """FP32 batched applies at vector counts that take 16-byte gathers (16..128, multiples of 128) and one that
@@ -269,7 +269,7 @@ def test_autotune_keeps_results(built):
     op.evaluate(x, y1)
     op.apply_batched(X, Y1)
     assert np.array_equal(y0, y1) and np.array_equal(Y0, Y1)
-    for vw, vc in ((4, 16), (4, 32), (4, 64), (8, 16), (8, 32), (8, 64)):
+    for vw, vc in ((4, 16), (4, 32), (4, 64), (8, 16), (8, 32), (8, 64), (16, 16), (16, 64)):
         op.set_tuning(t["grid_bps"], vc, which=1, vec_width=vw)
         Y2 = np.zeros_like(X)
         op.apply_batched(X, Y2)
@@ -361,7 +361,7 @@ def test_states_up_to_128_bits():
     ref = O.apply_port(lohi, specs, x, threads=1)
     np.testing.assert_allclose(y, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
     X = np.random.default_rng(9).standard_normal((len(lohi), 64)).astype(np.float32)
-    for vw in (4, 8):
+    for vw in (4, 8, 16):
         op.set_tuning(0, 0, which=1, vec_width=vw)
         Y = np.zeros_like(X)
         op.apply_batched(X, Y)

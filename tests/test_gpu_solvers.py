@@ -101,12 +101,12 @@ def test_ftlm_sector_launch_lookup_and_tuning_independent():
     launch settings."""
     cs = cases()
     ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["cfg1", "s4444"]]
-    ref = q.ftlm(ops, [32, 32], M=20, seed=4, precision="mixed")
-    for vw in (4, 8):
+    ref = q.ftlm(ops, [64, 64], M=20, seed=4, precision="mixed")
+    for vw in (4, 8, 16):
         for op in ops:
             op.set_kernel(1, 0)  # bucket table
             op.set_tuning(4, 16, which=1, vec_width=vw)
-        other = q.ftlm(ops, [32, 32], M=20, seed=4, precision="mixed")
+        other = q.ftlm(ops, [64, 64], M=20, seed=4, precision="mixed")
         for (a, b), (c, d) in zip(ref, other):
             assert np.array_equal(a, c) and np.array_equal(b, d)
     for op in ops:

@@ -17,7 +17,8 @@
  * Pointer kinds: entry points that take vectors accept either host or device
  * memory, selected by QSI_PTR_HOST / QSI_PTR_DEVICE in `flags`.  With host
  * pointers the call copies in, computes on the GPU and copies out, and is
- * synchronous.  With device pointers the work is enqueued on `stream`
+ * synchronous; a page-locked (pinned) result buffer of an apply without
+ * accumulation is written by the kernel directly, without a staging copy.  With device pointers the work is enqueued on `stream`
  * (a cudaStream_t, or NULL for the handle's own stream).
  */
 #ifndef QSI_ED_H

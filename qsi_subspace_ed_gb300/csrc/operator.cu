@@ -650,6 +650,16 @@ static qsi_status ensure_host_staging(qsi_op* op, size_t bytes) {
     return QSI_OK;
 }
 
+// Device address of page-locked host memory mapped into the device's address space (nullptr otherwise).
+static void* mapped_host(void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+}
+
 qsi_status apply_any(qsi_op* op, const void* x, void* y, int R, int dtype, int accumulate, int flags, void* stream) {
     if (!op || !x || !y || R <= 0 || (dtype != QSI_F64 && dtype != QSI_F32))
         return fail(QSI_INVALID_ARG, "apply: bad argument");
@@ -659,10 +669,14 @@ qsi_status apply_any(qsi_op* op, const void* x, void* y, int R, int dtype, int a
     qsi_status s = ensure_host_staging(op, bytes);
     if (s != QSI_OK) return s;
     QSI_CUDA(cudaMemcpyAsync(op->d_x, x, bytes, cudaMemcpyHostToDevice, st));
+    // A pinned, mapped result buffer (y = H x, no accumulation) takes the kernel's row stores directly over the
+    // host link (every kernel writes each y element once and reads y only when accumulating), so no device-to-host
+    // copy follows the apply.  Pageable buffers go through the staging copy.
+    void* y_mapped = accumulate ? nullptr : mapped_host(y);
     if (accumulate) QSI_CUDA(cudaMemcpyAsync(op->d_y, y, bytes, cudaMemcpyHostToDevice, st));
-    s = launch_apply(op, op->d_x, op->d_y, R, dtype, accumulate, st);
+    s = launch_apply(op, op->d_x, y_mapped ? y_mapped : op->d_y, R, dtype, accumulate, st);
     if (s != QSI_OK) return s;
-    QSI_CUDA(cudaMemcpyAsync(y, op->d_y, bytes, cudaMemcpyDeviceToHost, st));
+    if (!y_mapped) QSI_CUDA(cudaMemcpyAsync(y, op->d_y, bytes, cudaMemcpyDeviceToHost, st));
     QSI_CUDA(cudaStreamSynchronize(st));
     return QSI_OK;
 }

@@ -1,4 +1,6 @@
 """GPU apply, lookup and connectivity through the C-ABI against the oracle."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -118,6 +120,32 @@ def test_device_pointers_and_stream(built):
     torch.cuda.synchronize()
     y_ref = O.apply_port(basis, H.specs(), x.cpu().numpy(), threads=1)
     np.testing.assert_allclose(y.cpu().numpy(), y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+
+
+def test_pinned_host_result_buffers(built):
+    """Host pointers into page-locked buffers: the result is written straight into the host buffer (no staging
+    copy) and equals the staged and the device-pointer applies bitwise; accumulation still adds to it."""
+    torch = pytest.importorskip("torch")
+    basis, H, b, op = built["cfg1"]
+    n, R = len(basis), 32
+    xh = torch.randn(n, dtype=torch.float64).pin_memory()
+    yh = torch.full((n,), 3.0, dtype=torch.float64).pin_memory()
+    lib = q.load()
+    assert lib.qsi_op_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), 0, 0, None) == 0
+    y_staged = np.zeros(n)
+    op.evaluate(xh.numpy(), y_staged)
+    assert np.array_equal(yh.numpy(), y_staged)
+    assert lib.qsi_op_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), 1, 0, None) == 0
+    assert np.array_equal(yh.numpy(), 2 * y_staged)
+    Xh = torch.randn(n, R, dtype=torch.float32).pin_memory()
+    Yh = torch.zeros(n, R, dtype=torch.float32).pin_memory()
+    assert lib.qsi_op_apply_batched(op._h, C.c_void_p(Xh.data_ptr()), C.c_void_p(Yh.data_ptr()), R, 1, 0, 0,
+                                    None) == 0
+    Xd = Xh.cuda()
+    Yd = torch.zeros_like(Xd)
+    op.apply_batched(Xd, Yd)
+    torch.cuda.synchronize()
+    assert np.array_equal(Yh.numpy(), Yd.cpu().numpy())
 
 
 def test_projected_hopping_drops_misses():

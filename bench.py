@@ -43,7 +43,7 @@ def parse():
     p.add_argument("--lattice", default="pyro_1x2x3", help="pyro_1x2x1 | pyro_1x2x2 | pyro_1x2x3")
     p.add_argument("--full-basis", action="store_true", help="all Q=0 states instead of the equal sector")
     p.add_argument("--sector", default="", help="comma-separated sublattice up-counts (default: equal sector)")
-    p.add_argument("--R", default="64,128",
+    p.add_argument("--R", default="128,64",
                    help="vector counts of the batched mixed apply legs (the first is `batched_mixed`, as FTLM's R)")
     p.add_argument("--no-tune", action="store_true", help="skip the launch autotuner (built-in settings)")
     p.add_argument("--ftlm-steps", type=int, default=30, help="Lanczos steps of the timed FTLM runs")
@@ -54,7 +54,8 @@ def parse():
                    help="extra legs after the FP64 headline (also: lanczos = FP64 vs mixed 10-eigenvalue solves)")
     p.add_argument("--nev", type=int, default=10)
     p.add_argument("--serve-n", type=int, default=240)
-    p.add_argument("--ftlm-R", type=int, default=64)
+    p.add_argument("--ftlm-R", type=int, default=0,
+                   help="FTLM vectors per sector (0: the first of --R; the config-4 leg: 64)")
     p.add_argument("--ftlm-M", type=int, default=100)
     p.add_argument("--serve-rate", type=float, default=40.0)
     p.add_argument("--serve-slots", type=int, default=8)
@@ -220,7 +221,7 @@ def ftlm4_leg(args):
             ("pyro_1x2x1.n2", l32, q.enumerate_basis(l32, n_spinon_pairs=2))]
     t_enum = time.time() - t0
     ops = [q.LazyOpSum(q.ZBasis(b), q.build_ring_zeeman(lat, g, B, Jpm=0.05)) for _, lat, b in secs]
-    R, M = args.ftlm_R, args.ftlm_M
+    R, M = args.ftlm_R or 64, args.ftlm_M
     T = np.logspace(-2, 1, 200)
     out = {"R": R, "M": M, "Jpm": 0.05, "g": g, "B": B, "sectors": {nm: int(len(b)) for nm, _, b in secs},
            "enumerate_s": round(t_enum, 2), "note": "the 2-spinon-pair sector is taken on the 32-spin cell "
@@ -454,7 +455,8 @@ def run_ours(args):
             torch.cuda.empty_cache()
     if "ftlm" in legs and rank == 0:
         # FTLM vector-steps/s on the same operator: batched mixed precision (ftlm-R FP32 vectors, one apply
-        # launch per step, the run captured in one CUDA graph) against plain FP64 single-vector Lanczos.
+        # launch per step, the run captured in one CUDA graph; two vector blocks instead of three when three do
+        # not fit, as at R = 128 on the 96-spin sector) against plain FP64 single-vector Lanczos.
         # Per-step rates come from the difference of an M and an M/3 step run (setup, capture and readout
         # cancel); the rates including setup are given beside them.
         M1 = max(3, args.ftlm_steps)
@@ -472,7 +474,10 @@ def run_ours(args):
             return {"R": R, "precision": prec, "ms_per_step": per * 1e3, "vec_steps_per_s": R / per,
                     "vec_steps_per_s_incl_setup": R * M1 / t[M1], "seconds": {str(M0): t[M0], str(M1): t[M1]}}
 
-        mixed = ftlm_rate(args.ftlm_R, "mixed")  # the batched settings tuned for R = first of --R
+        R_ftlm = args.ftlm_R or int(str(args.R).split(",")[0])
+        mixed = ftlm_rate(R_ftlm, "mixed")  # the batched settings tuned for R = first of --R
+        free_b, total_b = torch.cuda.mem_get_info()
+        mixed["vector_blocks"] = 3 if 3 * n * R_ftlm * 4 + (4 << 30) <= free_b else 2
         torch.cuda.empty_cache()
         plain = ftlm_rate(1, "f64")
         line["ftlm"] = {"value": mixed["vec_steps_per_s"], "unit": "vec-steps/s", "mixed": mixed, "plain_fp64": plain,

@@ -311,6 +311,15 @@ qsi_status qsi_ftlm_run(qsi_op** ops, int32_t n_sectors, const int32_t* R,
                         int32_t M, uint64_t seed, int32_t precision,
                         double* alphas, double* betas);
 
+/* qsi_ftlm_run with the number of R-vector blocks kept per sector: 3 (H q in
+ * its own block), 2 (in-place recurrence: H q accumulated into the previous
+ * vector block, so R can double at the same device-memory footprint), or 0 =
+ * three when they fit in free device memory, else two (what qsi_ftlm_run
+ * does).  Both layouts give the same recurrences up to rounding. */
+qsi_status qsi_ftlm_run_blocks(qsi_op** ops, int32_t n_sectors, const int32_t* R,
+                               int32_t M, uint64_t seed, int32_t precision,
+                               int32_t blocks, double* alphas, double* betas);
+
 /* Expectation values of n_ops operators between nvec vectors, as eval_observables
  * computes them (src/expectation_eval.cpp:27-110, src/eval_observables.cpp:134-208):
  * operator l is the term list terms[op_offsets[l] .. op_offsets[l+1]) (a

@@ -127,6 +127,7 @@ SIGNATURES = {
     "qsi_eigval0_checkpointed": [_P, C.POINTER(Eigval0Cfg), C.c_char_p, _I32, _I32, _D, C.POINTER(_D), _P,
                                  C.POINTER(_I32)],
     "qsi_ftlm_run": [_P, _I32, _P, _I32, _U64, _I32, _P, _P],
+    "qsi_ftlm_run_blocks": [_P, _I32, _P, _I32, _U64, _I32, _I32, _P, _P],
     "qsi_tridiag_ritz": [_P, _P, _I32, _I32, _P, _P],
 }
 _RESTYPES = {"qsi_version": C.c_char_p, "qsi_free_host": None}

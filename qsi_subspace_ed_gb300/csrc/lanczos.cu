@@ -1286,7 +1286,8 @@ __global__ void __launch_bounds__(256) k_col_dots(const VT* __restrict__ a, cons
 // out[r] = sum over blocks of partial[b][r] (its square root with sqrt_out, and then also the column's
 // scale 1/out[r] for k_col_scale: FP64 and as a (hi, lo) float pair).
 __global__ void k_col_reduce(const double* __restrict__ partial, int nblocks, int R, double* __restrict__ out,
-                             int sqrt_out, double* __restrict__ inv = nullptr, float2* __restrict__ inv_ff = nullptr) {
+                             int sqrt_out, double* __restrict__ inv = nullptr, float2* __restrict__ inv_ff = nullptr,
+                             float2* __restrict__ neg_ff = nullptr) {
     for (int r = threadIdx.x; r < R; r += blockDim.x) {
         double t = 0.0;
         for (int b = 0; b < nblocks; ++b) t += partial[(int64_t)b * R + r];
@@ -1297,11 +1298,16 @@ __global__ void k_col_reduce(const double* __restrict__ partial, int nblocks, in
             inv[r] = v;
             inv_ff[r] = make_float2(h, (float)(v - (double)h));
         }
+        if (neg_ff) {  // -out[r] as a (hi, lo) float pair
+            const float h = (float)(-out[r]);
+            neg_ff[r] = make_float2(h, (float)(-out[r] - (double)h));
+        }
     }
 }
 
-// prev <- w - alpha cur - beta_prev prev (per column), with partial column sums of its square.
-template <typename VT, int VW>
+// prev <- w - alpha cur - beta_prev prev (per column), with partial column sums of its square.  kInPlace
+// (two-block recurrence): prev already holds H cur - beta_prev prev, and prev <- prev - alpha cur (w unused).
+template <typename VT, int VW, bool kInPlace = false>
 __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, const VT* __restrict__ cur,
                                                      const VT* __restrict__ w, const double* __restrict__ alpha,
                                                      const double* __restrict__ beta_prev, int64_t n, int R,
@@ -1312,7 +1318,7 @@ __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, cons
 #pragma unroll
     for (int k = 0; k < VW; ++k) {
         a[k] = alpha[L.c0 + k];
-        b[k] = beta_prev ? beta_prev[L.c0 + k] : 0.0;
+        b[k] = (beta_prev && !kInPlace) ? beta_prev[L.c0 + k] : 0.0;
     }
     if constexpr (sizeof(VT) == 4) {
         float ah[VW], al[VW], bh[VW], bl[VW];
@@ -1329,7 +1335,7 @@ __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, cons
             for (int u = 0; u < kColUnroll; ++u) {
                 const int64_t ii = i + (int64_t)u * L.rpp;
                 if (ii < L.i1) {
-                    load_vec<VT, VW>(w + ii * R + L.c0, wv[u]);
+                    if constexpr (!kInPlace) load_vec<VT, VW>(w + ii * R + L.c0, wv[u]);
                     load_vec<VT, VW>(cur + ii * R + L.c0, cv[u]);
                     load_vec<VT, VW>(prev + ii * R + L.c0, pv[u]);
                 }
@@ -1341,9 +1347,9 @@ __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, cons
                 VT out[VW];
 #pragma unroll
                 for (int k = 0; k < VW; ++k) {
-                    F2 v{(float)wv[u][k], 0.f};
+                    F2 v{(float)(kInPlace ? pv[u][k] : wv[u][k]), 0.f};
                     f2_fma(v, ah[k], al[k], (float)cv[u][k]);
-                    f2_fma(v, bh[k], bl[k], (float)pv[u][k]);
+                    if constexpr (!kInPlace) f2_fma(v, bh[k], bl[k], (float)pv[u][k]);
                     const float vf = v.hi + v.lo;
                     out[k] = (VT)vf;
                     f2_fma(nrm[k], vf, 0.f, vf);
@@ -1362,7 +1368,7 @@ __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, cons
             for (int u = 0; u < kColUnroll; ++u) {
                 const int64_t ii = i + (int64_t)u * L.rpp;
                 if (ii < L.i1) {
-                    load_vec<VT, VW>(w + ii * R + L.c0, wv[u]);
+                    if constexpr (!kInPlace) load_vec<VT, VW>(w + ii * R + L.c0, wv[u]);
                     load_vec<VT, VW>(cur + ii * R + L.c0, cv[u]);
                     load_vec<VT, VW>(prev + ii * R + L.c0, pv[u]);
                 }
@@ -1374,7 +1380,8 @@ __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, cons
                 VT out[VW];
 #pragma unroll
                 for (int k = 0; k < VW; ++k) {
-                    const double v = (double)wv[u][k] - a[k] * (double)cv[u][k] - b[k] * (double)pv[u][k];
+                    const double v = kInPlace ? (double)pv[u][k] - a[k] * (double)cv[u][k]
+                                              : (double)wv[u][k] - a[k] * (double)cv[u][k] - b[k] * (double)pv[u][k];
                     out[k] = (VT)v;
                     res[k] += v * v;
                 }
@@ -1385,11 +1392,22 @@ __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, cons
     col_block_sum<VW>(L, res, R, sh, partial);
 }
 
-// v *= inv per column (1/beta from k_col_reduce; a double-float multiply for FP32 storage).  R is a
-// power of two.
+// v *= inv per column (1/beta from k_col_reduce; a double-float multiply for FP32 storage).  With v2 (the
+// two-block recurrence) also v2 *= -beta, the next step's accumulated term.  R is a power of two.
+template <typename VT, int VW>
+__device__ __forceinline__ VT col_mul(VT x, double c, float2 c_ff) {
+    if constexpr (sizeof(VT) == 4) {
+        const float xf = (float)x;
+        const float p = c_ff.x * xf;
+        return (VT)(p + (fmaf(c_ff.x, xf, -p) + c_ff.y * xf));
+    } else {
+        return (VT)((double)x * c);
+    }
+}
 template <typename VT, int VW>
 __global__ void k_col_scale(VT* __restrict__ v, const double* __restrict__ inv, const float2* __restrict__ inv_ff,
-                            int64_t n, int R) {
+                            int64_t n, int R, VT* __restrict__ v2 = nullptr, const double* __restrict__ beta = nullptr,
+                            const float2* __restrict__ nbeta_ff = nullptr) {
     const int64_t total = n * R / VW;
 #pragma unroll 4
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
@@ -1397,17 +1415,17 @@ __global__ void k_col_scale(VT* __restrict__ v, const double* __restrict__ inv, 
         VT x[VW];
         load_vec<VT, VW>(v + e * VW, x);
 #pragma unroll
-        for (int k = 0; k < VW; ++k) {
-            if constexpr (sizeof(VT) == 4) {
-                const float2 ic = inv_ff[c0 + k];
-                const float xf = (float)x[k];
-                const float p = ic.x * xf;
-                x[k] = (VT)(p + (fmaf(ic.x, xf, -p) + ic.y * xf));
-            } else {
-                x[k] = (VT)((double)x[k] * inv[c0 + k]);
-            }
-        }
+        for (int k = 0; k < VW; ++k)
+            x[k] = col_mul<VT, VW>(x[k], inv[c0 + k], sizeof(VT) == 4 ? inv_ff[c0 + k] : make_float2(0.f, 0.f));
         store_vec<VT, VW>(v + e * VW, x);
+        if (v2) {
+            load_vec<VT, VW>(v2 + e * VW, x);
+#pragma unroll
+            for (int k = 0; k < VW; ++k)
+                x[k] = col_mul<VT, VW>(x[k], -beta[c0 + k],
+                                       sizeof(VT) == 4 ? nbeta_ff[c0 + k] : make_float2(0.f, 0.f));
+            store_vec<VT, VW>(v2 + e * VW, x);
+        }
     }
 }
 
@@ -1420,32 +1438,52 @@ struct FtlmSector {
     int64_t n;
     DevBuf<VT> P, C, W;
     DevBuf<double> partial, ab, inv;
-    DevBuf<float2> inv_ff;
+    DevBuf<float2> inv_ff, nbeta_ff;
 };
 
 // All sectors advance together: per step one apply launch covering every sector
 // (FP32 storage with hash indexes) or one per sector, then the per-sector
 // recurrence kernels.  The whole M-step run is captured into one CUDA graph.
+//
+// Three blocks of R vectors per sector (prev P, current C, W = H C):
+//   W = H C;  alpha = <C, W>;  P <- W - alpha C - beta_prev P;  beta = |P|;  P /= beta;  swap(P, C).
+// Two blocks (blocks == 2, or blocks == 0 when three do not fit in free device memory), the in-place
+// recurrence with P holding -beta_prev q_prev at the start of a step:
+//   P += H C;  alpha = <C, P>;  P <- P - alpha C;  beta = |P|;  P /= beta,  C *= -beta;  swap(P, C).
+// It moves two more blocks per step than the three-block form and lets R double at the same footprint.
 template <typename VT>
 static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint64_t seed, double* alphas,
-                           double* betas) {
+                           double* betas, int blocks) {
     cudaStream_t st = ops[0]->stream;
     std::vector<FtlmSector<VT>> S(ns);
     bool one_launch = (sizeof(VT) == 4);
+    size_t block_bytes = 0;
     for (int s = 0; s < ns; ++s) {
         const int R = Rs[s];
         if (R <= 0 || R > 256 || (R & (R - 1))) return fail(QSI_INVALID_ARG, "ftlm: R must be a power of two in [1,256]");
         if (ops[s]->basis->n < 1) return fail(QSI_INVALID_ARG, "ftlm: empty sector");
+        block_bytes += (size_t)ops[s]->basis->n * R * sizeof(VT);
+    }
+    if (blocks == 0) {  // three blocks when they fit with 4 GiB to spare, else two
+        size_t free_b = 0, total_b = 0;
+        QSI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        blocks = (3 * block_bytes + ((size_t)4 << 30) <= free_b) ? 3 : 2;
+    }
+    if (blocks != 2 && blocks != 3) return fail(QSI_INVALID_ARG, "ftlm: blocks must be 0, 2 or 3");
+    const bool two = (blocks == 2);
+    for (int s = 0; s < ns; ++s) {
+        const int R = Rs[s];
         S[s].op = ops[s];
         S[s].R = R;
         S[s].n = ops[s]->basis->n;
         QSI_CUDA(S[s].P.alloc((size_t)S[s].n * R, st));
         QSI_CUDA(S[s].C.alloc((size_t)S[s].n * R, st));
-        QSI_CUDA(S[s].W.alloc((size_t)S[s].n * R, st));
+        if (!two) QSI_CUDA(S[s].W.alloc((size_t)S[s].n * R, st));
         QSI_CUDA(S[s].partial.alloc((size_t)kColGrid * R, st));
         QSI_CUDA(S[s].ab.alloc((size_t)2 * M * R, st));
         QSI_CUDA(S[s].inv.alloc((size_t)R, st));
         QSI_CUDA(S[s].inv_ff.alloc((size_t)R, st));
+        QSI_CUDA(S[s].nbeta_ff.alloc((size_t)R, st));
         one_launch = one_launch && ops[s]->kernel == 1 &&
                      ops[s]->ff_accumulate;
         k_ftlm_init<VT><<<grid_for(S[s].n * R, 256), 256, 0, st>>>(S[s].C.p, S[s].P.p, S[s].n, R, seed + (uint64_t)s);
@@ -1466,9 +1504,10 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
             QSI_CUDA(cudaEventCreate(&e1));
             qsi_status ts = QSI_OK;
             for (int s = 0; s < ns && ts == QSI_OK; ++s) {
-                ts = launch_apply(ops[s], S[s].C.p, S[s].W.p, S[s].R, QSI_F32, 0, st);
+                VT* out = two ? S[s].P.p : S[s].W.p;  // P is zeroed again below
+                ts = launch_apply(ops[s], S[s].C.p, out, S[s].R, QSI_F32, 0, st);
                 if (ts == QSI_OK && cudaEventRecord(e0, st) != cudaSuccess) ts = QSI_CUDA_ERROR;
-                if (ts == QSI_OK) ts = launch_apply(ops[s], S[s].C.p, S[s].W.p, S[s].R, QSI_F32, 0, st);
+                if (ts == QSI_OK) ts = launch_apply(ops[s], S[s].C.p, out, S[s].R, QSI_F32, 0, st);
                 float ms = 0.f;
                 if (ts == QSI_OK && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
                                      cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
@@ -1478,13 +1517,16 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             if (ts != QSI_OK) return ts;
+            if (two)
+                for (int s = 0; s < ns; ++s)
+                    QSI_CUDA(cudaMemsetAsync(S[s].P.p, 0, (size_t)S[s].n * S[s].R * sizeof(VT), st));
         }
         for (int parity = 0; parity < 2; ++parity) {
             std::vector<const float*> X(ns);
             std::vector<float*> Y(ns);
             for (int s = 0; s < ns; ++s) {
                 X[s] = (const float*)(parity ? S[s].P.p : S[s].C.p);
-                Y[s] = (float*)S[s].W.p;
+                Y[s] = (float*)(two ? (parity ? S[s].C.p : S[s].P.p) : S[s].W.p);
             }
             qsi_status ps = plan_sectors(opv.data(), ns, X.data(), Y.data(), Rs, plan[parity], weight.data());
             if (ps != QSI_OK) return ps;
@@ -1500,27 +1542,34 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
     qsi_status status = QSI_OK;
     const int blk = 256;
     for (int j = 0; j < M && status == QSI_OK; ++j) {
+        // two blocks: the apply accumulates into prev, which holds -beta_prev q_prev (zero at the first step)
         if (one_launch) {
-            status = launch_sectors(d_plan[j & 1].p, plan[j & 1], 0, st);
+            status = launch_sectors(d_plan[j & 1].p, plan[j & 1], two ? 1 : 0, st);
         } else {
             for (int s = 0; s < ns && status == QSI_OK; ++s)
-                status = launch_apply(ops[s], cur[s], S[s].W.p, S[s].R, sizeof(VT) == 4 ? QSI_F32 : QSI_F64, 0, st);
+                status = launch_apply(ops[s], cur[s], two ? prev[s] : S[s].W.p, S[s].R,
+                                      sizeof(VT) == 4 ? QSI_F32 : QSI_F64, two ? 1 : 0, st);
         }
         for (int s = 0; s < ns; ++s) {
             FtlmSector<VT>& F = S[s];
             double* dA = F.ab.p;
             double* dB = F.ab.p + (size_t)M * F.R;
             const double* bprev = j ? dB + (size_t)(j - 1) * F.R : nullptr;
+            double* beta = dB + (size_t)j * F.R;
             auto col_step = [&](auto vw) {
                 constexpr int VW = decltype(vw)::value;
-                k_col_dots<VT, VW><<<kColGrid, blk, 0, st>>>(cur[s], F.W.p, F.n, F.R, F.partial.p);
+                k_col_dots<VT, VW><<<kColGrid, blk, 0, st>>>(cur[s], two ? prev[s] : F.W.p, F.n, F.R, F.partial.p);
                 k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dA + (size_t)j * F.R, 0);
-                k_ftlm_update<VT, VW><<<kColGrid, blk, 0, st>>>(prev[s], cur[s], F.W.p, dA + (size_t)j * F.R, bprev,
-                                                                F.n, F.R, F.partial.p);
-                k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dB + (size_t)j * F.R, 1, F.inv.p,
-                                                F.inv_ff.p);
-                k_col_scale<VT, VW><<<grid_for(F.n * F.R / VW, 256), 256, 0, st>>>(prev[s], F.inv.p, F.inv_ff.p,
-                                                                                  F.n, F.R);
+                if (two)
+                    k_ftlm_update<VT, VW, true><<<kColGrid, blk, 0, st>>>(prev[s], cur[s], nullptr, dA + (size_t)j * F.R,
+                                                                          nullptr, F.n, F.R, F.partial.p);
+                else
+                    k_ftlm_update<VT, VW><<<kColGrid, blk, 0, st>>>(prev[s], cur[s], F.W.p, dA + (size_t)j * F.R,
+                                                                    bprev, F.n, F.R, F.partial.p);
+                k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, beta, 1, F.inv.p, F.inv_ff.p,
+                                                two ? F.nbeta_ff.p : nullptr);
+                k_col_scale<VT, VW><<<grid_for(F.n * F.R / VW, 256), 256, 0, st>>>(
+                    prev[s], F.inv.p, F.inv_ff.p, F.n, F.R, two ? cur[s] : nullptr, beta, F.nbeta_ff.p);
             };
             constexpr int kVW = 16 / sizeof(VT);  // 16-byte accesses when R allows
             if (F.R % kVW == 0) col_step(std::integral_constant<int, kVW>{});
@@ -1565,8 +1614,19 @@ extern "C" qsi_status qsi_ftlm_run(qsi_op** ops, int32_t n_sectors, const int32_
         for (int s = 0; s < n_sectors; ++s)
             if (!ops[s]) return fail(QSI_INVALID_ARG, "qsi_ftlm_run: null operator");
         // sector s uses seed + s, so a sector run alone with seed + s gets the same vectors
-        return (precision == QSI_F32) ? ftlm_run<float>(ops, n_sectors, R, M, seed, alphas, betas)
-                                      : ftlm_run<double>(ops, n_sectors, R, M, seed, alphas, betas);
+        return (precision == QSI_F32) ? ftlm_run<float>(ops, n_sectors, R, M, seed, alphas, betas, 0)
+                                      : ftlm_run<double>(ops, n_sectors, R, M, seed, alphas, betas, 0);
+    });
+}
+
+extern "C" qsi_status qsi_ftlm_run_blocks(qsi_op** ops, int32_t n_sectors, const int32_t* R, int32_t M, uint64_t seed,
+                                          int32_t precision, int32_t blocks, double* alphas, double* betas) {
+    return guarded([&]() -> qsi_status {
+        if (!ops || n_sectors <= 0 || !R || M <= 0 || !alphas || !betas) return fail(QSI_INVALID_ARG, "qsi_ftlm_run_blocks: bad argument");
+        for (int s = 0; s < n_sectors; ++s)
+            if (!ops[s]) return fail(QSI_INVALID_ARG, "qsi_ftlm_run_blocks: null operator");
+        return (precision == QSI_F32) ? ftlm_run<float>(ops, n_sectors, R, M, seed, alphas, betas, blocks)
+                                      : ftlm_run<double>(ops, n_sectors, R, M, seed, alphas, betas, blocks);
     });
 }
 

@@ -75,9 +75,11 @@ def eigval0(op: LazyOpSum, seed: int = 10, abs_tol: float = 1e-8, rel_tol: float
     return e0.value, vec, its.value
 
 
-def ftlm(ops, R, M: int = 100, seed: int = 0, precision: str = "mixed"):
+def ftlm(ops, R, M: int = 100, seed: int = 0, precision: str = "mixed", blocks: int = 0):
     """Batched FTLM Lanczos recurrences: R[s] Rademacher vectors per sector, M steps.
 
+    blocks: R-vector blocks kept per sector, 3 (H q in its own block) or 2 (in-place recurrence, R can double at
+    the same device memory); 0 = three when they fit in free device memory, else two.
     Returns a list of (alphas (R[s], M), betas (R[s], M)) per sector.
     """
     ops = list(ops)
@@ -87,8 +89,8 @@ def ftlm(ops, R, M: int = 100, seed: int = 0, precision: str = "mixed"):
     tot = int(sum(R)) * M
     a = np.zeros(tot)
     b = np.zeros(tot)
-    call("qsi_ftlm_run", C.cast(handles, C.c_void_p), len(ops), ptr(Rs), M, seed,
-         _lib.QSI_F32 if precision == "mixed" else _lib.QSI_F64, ptr(a), ptr(b))
+    call("qsi_ftlm_run_blocks", C.cast(handles, C.c_void_p), len(ops), ptr(Rs), M, seed,
+         _lib.QSI_F32 if precision == "mixed" else _lib.QSI_F64, int(blocks), ptr(a), ptr(b))
     out, off = [], 0
     for r in R:
         out.append((a[off:off + r * M].reshape(r, M), b[off:off + r * M].reshape(r, M)))

@@ -86,6 +86,29 @@ def test_ftlm_mixed_matches_fp64():
     np.testing.assert_allclose(t32["C"], t64["C"], rtol=1e-3, atol=1e-4)
 
 
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_ftlm_two_block_recurrence(precision):
+    """The in-place two-block recurrence (H q accumulated into the previous vector block) gives the three-block
+    recurrences up to rounding and the same thermodynamics, in single- and multi-sector launches."""
+    cs = cases()
+    names = ["cfg1", "s4444"]
+    ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in names]
+    three = q.ftlm(ops, [32, 16], M=40, seed=6, precision=precision, blocks=3)
+    two = q.ftlm(ops, [32, 16], M=40, seed=6, precision=precision, blocks=2)
+    alone = q.ftlm(ops[:1], [32], M=40, seed=6, precision=precision, blocks=2)
+    T = np.logspace(-2, 1, 100)
+    tol = 1e-10 if precision == "f64" else 1e-5
+    for (a3, b3), (a2, b2), name in zip(three, two, names):
+        np.testing.assert_allclose(a2[:, :10], a3[:, :10], rtol=0, atol=tol)
+        np.testing.assert_allclose(b2[:, :10], b3[:, :10], rtol=0, atol=tol)
+        t3 = q.ftlm_thermo(a3, b3, len(cs[name][0]), T)
+        t2 = q.ftlm_thermo(a2, b2, len(cs[name][0]), T)
+        np.testing.assert_allclose(t2["C"], t3["C"], rtol=1e-3, atol=1e-4)
+    np.testing.assert_allclose(alone[0][0][:, :10], two[0][0][:, :10], rtol=0, atol=tol)
+    with pytest.raises(q.QsiError):
+        q.ftlm(ops[:1], [8], M=5, blocks=4)
+
+
 def test_ftlm_multi_sector_batch():
     cs = cases()
     ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["cfg1", "s4444"]]

@@ -258,7 +258,9 @@ inline bool vec16_ok(int64_t n, int R, const void* x, const void* y) {
 template <typename XT, class LK, bool kFF, int KM>
 __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, const XT* __restrict__ x,
                                              XT* __restrict__ y, int R, int accumulate, int cap, int64_t block_id,
-                                             int64_t n_blocks, unsigned char* smem_raw) {
+                                             int64_t n_blocks, unsigned char* smem_raw,
+                                             const float2* __restrict__ ycoef = nullptr) {
+    // accumulate: y <- H x + c y per column, c = 1, or the (hi, lo) float pair ycoef[column] (double-float paths)
     const TileSmem S = stage_terms(P, smem_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int n_rounds = (P.n_off + 31) >> 5;
@@ -436,10 +438,20 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                                 for (int q = 0; q < NQ; ++q) {
                                     if (accumulate) {
                                         const float4 yv = yp[q];
-                                        const uint64_t one = pk2(1.0f, 1.0f), mone = pk2(-1.0f, -1.0f),
-                                                       zero = pk2(0.f, 0.f);
-                                        ff2_fma(acc[2 * q], one, mone, zero, pk2(yv.x, yv.y));
-                                        ff2_fma(acc[2 * q + 1], one, mone, zero, pk2(yv.z, yv.w));
+                                        if (ycoef) {
+                                            const float4 ca = *reinterpret_cast<const float4*>(ycoef + r0 + rr + 4 * q);
+                                            const float4 cb =
+                                                *reinterpret_cast<const float4*>(ycoef + r0 + rr + 4 * q + 2);
+                                            ff2_fma(acc[2 * q], pk2(ca.x, ca.z), pk2(-ca.x, -ca.z), pk2(ca.y, ca.w),
+                                                    pk2(yv.x, yv.y));
+                                            ff2_fma(acc[2 * q + 1], pk2(cb.x, cb.z), pk2(-cb.x, -cb.z),
+                                                    pk2(cb.y, cb.w), pk2(yv.z, yv.w));
+                                        } else {
+                                            const uint64_t one = pk2(1.0f, 1.0f), mone = pk2(-1.0f, -1.0f),
+                                                           zero = pk2(0.f, 0.f);
+                                            ff2_fma(acc[2 * q], one, mone, zero, pk2(yv.x, yv.y));
+                                            ff2_fma(acc[2 * q + 1], one, mone, zero, pk2(yv.z, yv.w));
+                                        }
                                     }
                                     const float2 a = unpk2(add2(acc[2 * q].hi, acc[2 * q].lo)),
                                                  b = unpk2(add2(acc[2 * q + 1].hi, acc[2 * q + 1].lo));
@@ -470,7 +482,10 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                         for (int m = 0; m < KM; ++m) {
                             const int rr = r0 + lane + 32 * m;
                             if (rr < R) {
-                                if (accumulate) ff_fma(acc[m], 1.0f, 0.0f, (float)y[rl * R + rr]);
+                                if (accumulate) {
+                                    const float2 c = ycoef ? ycoef[rr] : make_float2(1.0f, 0.0f);
+                                    ff_fma(acc[m], c.x, c.y, (float)y[rl * R + rr]);
+                                }
                                 y[rl * R + rr] = (XT)(acc[m].hi + acc[m].lo);
                             }
                         }
@@ -580,6 +595,7 @@ struct SectorLaunch {
     HashView H;
     const float* x;
     float* y;
+    const float2* ycoef;  // accumulating launches: y <- H x + ycoef[c] y per column (nullptr: coefficient 1)
     int R;
     int cap;
     int block_begin;
@@ -601,7 +617,7 @@ __global__ void __launch_bounds__(256, KM <= kVec4 ? 2 : 3) k_apply_sectors(cons
     if constexpr (std::is_same<LK, LookupHash>::value) lk = LookupHash{L.H};
     else lk = LookupTable{L.P.B};
     batched_body<float, LK, true, KM>(L.P, lk, L.x, L.y, L.R, accumulate, L.cap, (int64_t)blockIdx.x - L.block_begin,
-                                      L.n_blocks, smem_raw);
+                                      L.n_blocks, smem_raw, L.ycoef);
 }
 
 // Per-row diagonal, evaluated once per operator with the same arithmetic as
@@ -774,7 +790,7 @@ static qsi_status launch_tiles_lk(qsi_op* op, LK lk, const void* x, void* y, int
 // else to rows x vectors; shared memory for the largest sector); the caller copies plan.records to device memory once, and launch_sectors enqueues the
 // kernel (capturable into a CUDA graph: it does no host-to-device copy).
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
-                        SectorPlan& plan, const double* weights) {
+                        SectorPlan& plan, const double* weights, const float2* const* ycoef) {
     std::vector<SectorLaunch> L(n);
     plan.vec4 = true;
     plan.vec8 = true;
@@ -799,6 +815,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         L[s].H = op->basis->hview();
         L[s].x = X[s];
         L[s].y = Y[s];
+        L[s].ycoef = ycoef ? ycoef[s] : nullptr;
         L[s].R = R[s];
         L[s].cap = cap;
         maxR = std::max(maxR, R[s]);

@@ -1448,9 +1448,11 @@ struct FtlmSector {
 // Three blocks of R vectors per sector (prev P, current C, W = H C):
 //   W = H C;  alpha = <C, W>;  P <- W - alpha C - beta_prev P;  beta = |P|;  P /= beta;  swap(P, C).
 // Two blocks (blocks == 2, or blocks == 0 when three do not fit in free device memory), the in-place
-// recurrence with P holding -beta_prev q_prev at the start of a step:
-//   P += H C;  alpha = <C, P>;  P <- P - alpha C;  beta = |P|;  P /= beta,  C *= -beta;  swap(P, C).
-// It moves two more blocks per step than the three-block form and lets R double at the same footprint.
+// recurrence with P holding q_prev at the start of a step:
+//   P <- H C - beta_prev P;  alpha = <C, P>;  P <- P - alpha C;  beta = |P|;  P /= beta;  swap(P, C).
+// The one-launch sector apply takes -beta_prev per column as its accumulate coefficient (double-float); the
+// per-sector launches instead have the column pass also scale C by -beta for the next step.  R can double at
+// the same footprint; the in-launch form moves as many blocks per step as the three-block one.
 template <typename VT>
 static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint64_t seed, double* alphas,
                            double* betas, int blocks) {
@@ -1484,6 +1486,7 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
         QSI_CUDA(S[s].inv.alloc((size_t)R, st));
         QSI_CUDA(S[s].inv_ff.alloc((size_t)R, st));
         QSI_CUDA(S[s].nbeta_ff.alloc((size_t)R, st));
+        QSI_CUDA(cudaMemsetAsync(S[s].nbeta_ff.p, 0, (size_t)R * sizeof(float2), st));
         one_launch = one_launch && ops[s]->kernel == 1 &&
                      ops[s]->ff_accumulate;
         k_ftlm_init<VT><<<grid_for(S[s].n * R, 256), 256, 0, st>>>(S[s].C.p, S[s].P.p, S[s].n, R, seed + (uint64_t)s);
@@ -1528,7 +1531,11 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
                 X[s] = (const float*)(parity ? S[s].P.p : S[s].C.p);
                 Y[s] = (float*)(two ? (parity ? S[s].C.p : S[s].P.p) : S[s].W.p);
             }
-            qsi_status ps = plan_sectors(opv.data(), ns, X.data(), Y.data(), Rs, plan[parity], weight.data());
+            // two blocks: the accumulating apply scales the previous block by -beta_prev itself
+            std::vector<const float2*> yc(ns);
+            for (int s = 0; s < ns; ++s) yc[s] = S[s].nbeta_ff.p;
+            qsi_status ps = plan_sectors(opv.data(), ns, X.data(), Y.data(), Rs, plan[parity], weight.data(),
+                                         two ? yc.data() : nullptr);
             if (ps != QSI_OK) return ps;
             QSI_CUDA(d_plan[parity].alloc(plan[parity].records.size(), st));
             QSI_CUDA(cudaMemcpyAsync(d_plan[parity].p, plan[parity].records.data(), plan[parity].records.size(),
@@ -1542,7 +1549,8 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
     qsi_status status = QSI_OK;
     const int blk = 256;
     for (int j = 0; j < M && status == QSI_OK; ++j) {
-        // two blocks: the apply accumulates into prev, which holds -beta_prev q_prev (zero at the first step)
+        // two blocks: the apply accumulates into prev, which holds q_prev (zero at the first step) and is scaled
+        // by -beta_prev on the way: inside the sector launch, else by the previous step's column pass
         if (one_launch) {
             status = launch_sectors(d_plan[j & 1].p, plan[j & 1], two ? 1 : 0, st);
         } else {
@@ -1569,7 +1577,8 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
                 k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, beta, 1, F.inv.p, F.inv_ff.p,
                                                 two ? F.nbeta_ff.p : nullptr);
                 k_col_scale<VT, VW><<<grid_for(F.n * F.R / VW, 256), 256, 0, st>>>(
-                    prev[s], F.inv.p, F.inv_ff.p, F.n, F.R, two ? cur[s] : nullptr, beta, F.nbeta_ff.p);
+                    prev[s], F.inv.p, F.inv_ff.p, F.n, F.R, (two && !one_launch) ? cur[s] : nullptr, beta,
+                    F.nbeta_ff.p);
             };
             constexpr int kVW = 16 / sizeof(VT);  // 16-byte accesses when R allows
             if (F.R % kVW == 0) col_step(std::integral_constant<int, kVW>{});

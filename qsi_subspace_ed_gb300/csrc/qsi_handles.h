@@ -72,7 +72,7 @@ struct SectorPlan {
     bool hash = true;  // every sector's batched applies look columns up through the hash index
 };
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
-                        SectorPlan& plan, const double* weights = nullptr);
+                        SectorPlan& plan, const double* weights = nullptr, const float2* const* ycoef = nullptr);
 qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int accumulate, cudaStream_t st);
 qsi_status jacobi_eigh(const std::vector<double>& A, int m, int n_mat, std::vector<double>& w, std::vector<double>& V, cudaStream_t st);
 }  // namespace qsi

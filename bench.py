@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--nev", type=int, default=10)
     p.add_argument("--serve-n", type=int, default=240)
     p.add_argument("--ftlm-R", type=int, default=0,
-                   help="FTLM vectors per sector (0: the first of --R; the config-4 leg: 64)")
+                   help="FTLM vectors per sector (0: the first of --R; the ftlm_sectors leg: 64)")
     p.add_argument("--ftlm-M", type=int, default=100)
     p.add_argument("--serve-rate", type=float, default=40.0)
     p.add_argument("--serve-slots", type=int, default=8)
@@ -204,7 +204,7 @@ def cpu_baseline(w, H, seconds: float):
                       f"[0,{rows}) of {n} of {w.name}; {dt:.1f}s"}
 
 
-def ftlm4_leg(args):
+def ftlm_sectors_leg(args):
     """Config-4 style FTLM: R Rademacher vectors, M steps, three sectors of uneven dimension advanced together
     (one apply launch per step for all sectors, the run captured in one CUDA graph), FP32 vectors with FP64
     recurrence coefficients, against the same run in plain FP64."""
@@ -483,7 +483,7 @@ def run_ours(args):
         line["ftlm"] = {"value": mixed["vec_steps_per_s"], "unit": "vec-steps/s", "mixed": mixed, "plain_fp64": plain,
                         "speedup_vs_plain_fp64": mixed["vec_steps_per_s"] / plain["vec_steps_per_s"]}
     if "lanczos" in legs and rank == 0:
-        # BASELINE configs 2/3: the nev lowest eigenpairs in plain FP64 and in mixed precision (FP32 Krylov
+        # 96-spin eigen-solves: the nev lowest eigenpairs in plain FP64 and in mixed precision (FP32 Krylov
         # vectors and gathers, FP64 recurrences, FP64 Rayleigh-Ritz polish), errors of the mixed eigenvalues
         del x, y
         torch.cuda.empty_cache()
@@ -509,8 +509,8 @@ def run_ours(args):
         out["levels_compared"] = int(len(err))
         out["speedup_mixed_vs_f64"] = out["f64"]["seconds"] / out["mixed"]["seconds"]
         line["lanczos"] = out
-    if "ftlm4" in legs and rank == 0:
-        line["ftlm_config4"] = ftlm4_leg(args)
+    if "ftlm_sectors" in legs and rank == 0:
+        line["ftlm_sectors"] = ftlm_sectors_leg(args)
     if "serve" in legs and rank == 0:
         line["serve"] = serve_leg(args)
     if "cpu" in legs and rank == 0:

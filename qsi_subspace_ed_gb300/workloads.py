@@ -53,7 +53,7 @@ def ring_zeeman_params(seed: int, g_range=None, b_amp=0.2):
     return g, B
 
 
-def config1(seed: int = 1) -> Workload:
+def q0_32spin(seed: int = 1) -> Workload:
     """32 spins, full Q=0 basis (3,618 states), g=(1,0.8,0.6,0.4), B ~ U[-0.2,0.2]^3."""
     lat = lattice("pyro_1x2x1")
     g, B = ring_zeeman_params(seed)
@@ -73,7 +73,7 @@ def sector_workload(name: str, seed: int = 3, g_range=(0.2, 1.0), b_amp=0.5, lat
                     enum(lat, sector=equal_sector(lat)), g, B)
 
 
-def config3(seed: int = 3) -> Workload:
+def sector_96spin(seed: int = 3) -> Workload:
     """96 spins, 12.12.12.12 sector, g ~ U[0.2,1]^4, B ~ U[-0.5,0.5]^3."""
     return sector_workload("pyro_1x2x3", seed)
 

@@ -12,8 +12,8 @@ writes small files next to this script:
   golden48_evec.npy        its stored eigenvector (float32)
   term_kats.json           masks/signs/applications from the reference's SymbolicPMROperator
   triplets.json            connectivity counts + SHA-256 digests from the reference code
-  apply_ref32.npy, apply_cfg1.npy   y = H x from the reference code (seeded x)
-  eigs_cfg1.json           FP64 lowest eigenvalues of the 32-spin config-1 Hamiltonian
+  apply_ref32.npy, apply_q0_32.npy   y = H x from the reference code (seeded x)
+  eigs_q0_32.json           FP64 lowest eigenvalues of the 32-spin Q=0 ring/Zeeman Hamiltonian
   thermo_s4444.npz         exact E(T), C(T) of the 32-spin 4.4.4.4 sector
   observables48.npz        ring, ring_ring, partial_vol_sl0..3 of the reference's stored .eigs.out.h5
 
@@ -106,13 +106,13 @@ def main():
     # connectivity digests and applies from the reference code
     lat48 = q.Lattice.load(HERE / "lattices" / "golden48.json")
     lat32 = q.Lattice.load(HERE / "lattices" / "ref32.json")
-    cfg1 = workloads.config1()
+    q0_32 = workloads.q0_32spin()
     sec4 = workloads.sector_workload("pyro_1x2x1", seed=3)
     cases = {
         "golden48_JpmB": (bases["golden48"], q.build_hamiltonian(lat48, 0.02, [0.1, 0.1, 0.1])),
         "ref32_g": (bases["ref32"], q.build_hamiltonian_g(lat32, [1.0, -0.2, -0.2, -0.2])),
         "ref32_JpmB": (bases["ref32"], q.build_hamiltonian(lat32, 0.05, [0.3, -0.1, 0.2])),
-        "cfg1": (cfg1.basis_lohi, cfg1.hamiltonian()),
+        "q0_32": (q0_32.basis_lohi, q0_32.hamiltonian()),
         "s4444": (sec4.basis_lohi, sec4.hamiltonian()),
     }
     trip = {}
@@ -126,15 +126,15 @@ def main():
     x32 = rng.standard_normal(len(bases["ref32"]))
     np.save(HERE / "apply_ref32.npy", np.stack([x32, O.apply_ref(bases["ref32"], cases["ref32_g"][1].specs(), x32,
                                                                  threads=1)]))
-    x1 = rng.standard_normal(len(cfg1.basis_lohi))
-    np.save(HERE / "apply_cfg1.npy", np.stack([x1, O.apply_ref(cfg1.basis_lohi, cases["cfg1"][1].specs(), x1,
+    x1 = rng.standard_normal(len(q0_32.basis_lohi))
+    np.save(HERE / "apply_q0_32.npy", np.stack([x1, O.apply_ref(q0_32.basis_lohi, cases["q0_32"][1].specs(), x1,
                                                                threads=1)]))
 
-    # FP64 eigen-oracle for config 1 (dense, n = 3618)
-    r, c, v = O.triplets_port(cfg1.basis_lohi, cases["cfg1"][1].specs())
-    w, _ = O.lowest_eigs(r, c, v, len(cfg1.basis_lohi), k=10)
-    json.dump({"g": cfg1.g, "B": cfg1.B, "evals": [float(x) for x in w], "n": int(len(cfg1.basis_lohi))},
-              open(HERE / "eigs_cfg1.json", "w"), indent=1)
+    # FP64 eigen-oracle for the 32-spin Q=0 case (dense, n = 3618)
+    r, c, v = O.triplets_port(q0_32.basis_lohi, cases["q0_32"][1].specs())
+    w, _ = O.lowest_eigs(r, c, v, len(q0_32.basis_lohi), k=10)
+    json.dump({"g": q0_32.g, "B": q0_32.B, "evals": [float(x) for x in w], "n": int(len(q0_32.basis_lohi))},
+              open(HERE / "eigs_q0_32.json", "w"), indent=1)
     # exact thermodynamics of the 4.4.4.4 sector (n = 388)
     r, c, v = O.triplets_port(sec4.basis_lohi, cases["s4444"][1].specs())
     H = O.csr_from_triplets(r, c, v, len(sec4.basis_lohi)).toarray()

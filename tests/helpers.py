@@ -24,12 +24,12 @@ def cases():
     lat48 = q.Lattice.load(GOLDEN / "lattices" / "golden48.json")
     lat32 = q.Lattice.load(GOLDEN / "lattices" / "ref32.json")
     b32 = np.load(GOLDEN / "basis_ref32.npy")
-    cfg1 = workloads.config1()
+    q0_32 = workloads.q0_32spin()
     sec4 = workloads.sector_workload("pyro_1x2x1", seed=3)
     return {
         "golden48_JpmB": (q.enumerate_basis(lat48), q.build_hamiltonian(lat48, 0.02, [0.1, 0.1, 0.1])),
         "ref32_g": (b32, q.build_hamiltonian_g(lat32, [1.0, -0.2, -0.2, -0.2])),
         "ref32_JpmB": (b32, q.build_hamiltonian(lat32, 0.05, [0.3, -0.1, 0.2])),
-        "cfg1": (cfg1.basis_lohi, cfg1.hamiltonian()),
+        "q0_32": (q0_32.basis_lohi, q0_32.hamiltonian()),
         "s4444": (sec4.basis_lohi, sec4.hamiltonian()),
     }

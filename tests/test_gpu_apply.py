@@ -10,7 +10,7 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["golden48_JpmB", "ref32_g", "ref32_JpmB", "cfg1", "s4444"]
+CASES = ["golden48_JpmB", "ref32_g", "ref32_JpmB", "q0_32", "s4444"]
 
 
 @pytest.fixture(scope="module")
@@ -74,7 +74,7 @@ def test_apply_fp64_matches_oracle(built, name):
 
 
 def test_apply_matches_reference_stored_applies(built):
-    for fname, name in [("apply_ref32.npy", "ref32_g"), ("apply_cfg1.npy", "cfg1")]:
+    for fname, name in [("apply_ref32.npy", "ref32_g"), ("apply_q0_32.npy", "q0_32")]:
         x, y_ref = np.load(GOLDEN / fname)
         y = np.zeros_like(x)
         built[name][3].evaluate(x, y)
@@ -82,7 +82,7 @@ def test_apply_matches_reference_stored_applies(built):
 
 
 def test_apply_tol_skips_tiny_sources(built):
-    basis, H, b, op = built["cfg1"]
+    basis, H, b, op = built["q0_32"]
     x = np.zeros(len(basis))
     x[5] = 1.0
     x[17] = 5e-16  # below APPLY_TOL: its off-diagonal pushes are dropped
@@ -113,7 +113,7 @@ def test_batched_apply(built, R):
 
 def test_device_pointers_and_stream(built):
     torch = pytest.importorskip("torch")
-    basis, H, b, op = built["cfg1"]
+    basis, H, b, op = built["q0_32"]
     x = torch.randn(len(basis), dtype=torch.float64, device="cuda")
     y = torch.zeros_like(x)
     op.evaluate(x, y)
@@ -126,7 +126,7 @@ def test_pinned_host_result_buffers(built):
     """Host pointers into page-locked buffers: the result is written straight into the host buffer (no staging
     copy) and equals the staged and the device-pointer applies bitwise; accumulation still adds to it."""
     torch = pytest.importorskip("torch")
-    basis, H, b, op = built["cfg1"]
+    basis, H, b, op = built["q0_32"]
     n, R = len(basis), 32
     xh = torch.randn(n, dtype=torch.float64).pin_memory()
     yh = torch.full((n,), 3.0, dtype=torch.float64).pin_memory()
@@ -283,7 +283,7 @@ def test_fp32_batched_unaligned_device_vectors(built):
 
 def test_autotune_keeps_results(built):
     """The autotuner changes launch settings only: applies before and after are bitwise equal."""
-    basis, H, b, op = built["cfg1"]
+    basis, H, b, op = built["q0_32"]
     x = np.random.default_rng(31).standard_normal(len(basis))
     X = np.random.default_rng(32).standard_normal((len(basis), 64)).astype(np.float32)
     y0, Y0 = np.zeros_like(x), np.zeros_like(X)
@@ -357,7 +357,7 @@ def test_matrix_market_export(built, name, tmp_path):
 def _wide_case():
     """The 32-spin Q=0 basis and ring/Zeeman Hamiltonian with spin i moved to bit 4i+3 (states up to 128 bits,
     beyond the 96 bits the hash index takes): lookups go through the bucket table."""
-    basis, H = cases()["cfg1"]
+    basis, H = cases()["q0_32"]
     spins = [(int(lo) | (int(hi) << 64)) for lo, hi in basis]
     wide = []
     for s in spins:

@@ -33,10 +33,10 @@ def test_golden_e0_through_eigval0():
 
 
 @pytest.mark.parametrize("precision", ["f64", "mixed"])
-def test_config1_lowest_five(precision):
-    """Config 1: ncv=15, 5 eigenvalues, tol 1e-10, against the FP64 dense oracle."""
-    basis, H = cases()["cfg1"]
-    ref = golden_json("eigs_cfg1.json")["evals"]
+def test_q0_32spin_lowest_five(precision):
+    """32-spin Q=0 basis (3,618 states): ncv=15, 5 eigenvalues, tol 1e-10, against the FP64 dense oracle."""
+    basis, H = cases()["q0_32"]
+    ref = golden_json("eigs_q0_32.json")["evals"]
     op = q.LazyOpSum(q.ZBasis(basis), H)
     w, V, rep = q.diagonalise(op, nev=5, ncv=15, tol=1e-10, seed=1, precision=precision,
                               polish_steps=2 if precision == "mixed" else 0)
@@ -75,7 +75,7 @@ def test_ftlm_against_exact_thermodynamics(precision):
 
 
 def test_ftlm_mixed_matches_fp64():
-    basis, H = cases()["cfg1"]
+    basis, H = cases()["q0_32"]
     op = q.LazyOpSum(q.ZBasis(basis), H)
     T = np.logspace(-2, 1, 200)
     (a64, b64), = q.ftlm([op], [32], M=50, seed=9, precision="f64")
@@ -91,7 +91,7 @@ def test_ftlm_two_block_recurrence(precision):
     """The in-place two-block recurrence (H q accumulated into the previous vector block) gives the three-block
     recurrences up to rounding and the same thermodynamics, in single- and multi-sector launches."""
     cs = cases()
-    names = ["cfg1", "s4444"]
+    names = ["q0_32", "s4444"]
     ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in names]
     three = q.ftlm(ops, [32, 16], M=40, seed=6, precision=precision, blocks=3)
     two = q.ftlm(ops, [32, 16], M=40, seed=6, precision=precision, blocks=2)
@@ -111,7 +111,7 @@ def test_ftlm_two_block_recurrence(precision):
 
 def test_ftlm_multi_sector_batch():
     cs = cases()
-    ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["cfg1", "s4444"]]
+    ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["q0_32", "s4444"]]
     res = q.ftlm(ops, [32, 16], M=30, seed=2, precision="mixed")
     assert [r[0].shape for r in res] == [(32, 30), (16, 30)]
     # each sector alone (seed + sector index) gives bit-identical recurrences
@@ -123,7 +123,7 @@ def test_ftlm_sector_launch_lookup_and_tuning_independent():
     """The one-launch sector apply gives the same recurrences with hash or bucket-table lookups and under any
     launch settings."""
     cs = cases()
-    ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["cfg1", "s4444"]]
+    ops = [q.LazyOpSum(q.ZBasis(cs[n][0]), cs[n][1]) for n in ["q0_32", "s4444"]]
     ref = q.ftlm(ops, [64, 64], M=20, seed=4, precision="mixed")
     for vw in (4, 8, 16):
         for op in ops:
@@ -152,7 +152,7 @@ def test_tridiag_ritz_matches_numpy():
 def test_eigval0_checkpoint_resume_is_bitwise(tmp_path):
     """A run stopped at an iteration limit and resumed from its checkpoint gives the uninterrupted result bitwise;
     the checkpoint file holds the reference's checkpoint datasets."""
-    basis, H = cases()["cfg1"]
+    basis, H = cases()["q0_32"]
     op = q.LazyOpSum(q.ZBasis(basis), H)
     kw = dict(seed=5, max_iterations=150, min_iterations=10, abs_tol=1e-10, rel_tol=1e-10)
     e_ref, v_ref, it_ref = q.eigval0(op, **kw)

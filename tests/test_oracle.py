@@ -15,7 +15,7 @@ def test_oracle_term_compiler_matches_reference_masks():
         assert int(t[0, 72:76].view(np.int32)[0]) == kat["sign"], kat["spec"]
 
 
-@pytest.mark.parametrize("name", ["golden48_JpmB", "ref32_g", "ref32_JpmB", "cfg1", "s4444"])
+@pytest.mark.parametrize("name", ["golden48_JpmB", "ref32_g", "ref32_JpmB", "q0_32", "s4444"])
 def test_oracle_triplets_match_reference_digest(name):
     basis, H = cases()[name]
     ref = golden_json("triplets.json")[name]
@@ -27,7 +27,7 @@ def test_oracle_triplets_match_reference_digest(name):
 
 def test_oracle_apply_matches_reference_apply():
     cs = cases()
-    for fname, case in [("apply_ref32.npy", "ref32_g"), ("apply_cfg1.npy", "cfg1")]:
+    for fname, case in [("apply_ref32.npy", "ref32_g"), ("apply_q0_32.npy", "q0_32")]:
         x, y_ref = np.load(GOLDEN / fname)
         basis, H = cs[case]
         y = O.apply_port(basis, H.specs(), x, threads=1)
@@ -44,9 +44,9 @@ def test_oracle_golden_ground_state_energy():
     assert abs(abs(ev @ V[:, 0]) / np.linalg.norm(ev) - 1.0) < 1e-6
 
 
-def test_oracle_config1_eigs():
-    basis, H = cases()["cfg1"]
-    ref = golden_json("eigs_cfg1.json")["evals"]
+def test_oracle_q0_32spin_eigs():
+    basis, H = cases()["q0_32"]
+    ref = golden_json("eigs_q0_32.json")["evals"]
     r, c, v = O.triplets_port(basis, H.specs())
     w, _ = O.lowest_eigs(r, c, v, len(basis), k=5)
     np.testing.assert_allclose(w, ref[:5], atol=1e-12)

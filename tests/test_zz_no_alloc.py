@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _op():
-    w = workloads.config1()
+    w = workloads.q0_32spin()
     return q.LazyOpSum(q.ZBasis(w.basis_lohi), w.hamiltonian())
 
 

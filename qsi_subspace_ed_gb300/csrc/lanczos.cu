@@ -1140,9 +1140,10 @@ template <typename VT>
 __global__ void k_ftlm_init(VT* __restrict__ cur, VT* __restrict__ prev, int64_t n, int R, uint64_t seed) {
     const double inv = rsqrt((double)n);
     const int64_t total = n * R;
+    const int shift = __ffs(R) - 1;  // R is a power of two
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = e / R;
-        const int r = (int)(e % R);
+        const int64_t i = e >> shift;
+        const int r = (int)(e & (R - 1));
         uint64_t h = splitmix64(seed ^ splitmix64(((uint64_t)r << 40) ^ (uint64_t)i));
         cur[e] = (VT)((h >> 63) ? inv : -inv);
         prev[e] = (VT)0;

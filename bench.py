@@ -205,7 +205,7 @@ def cpu_baseline(w, H, seconds: float):
 
 
 def ftlm_sectors_leg(args):
-    """Config-4 style FTLM: R Rademacher vectors, M steps, three sectors of uneven dimension advanced together
+    """Multi-sector FTLM: R Rademacher vectors, M steps, three sectors of uneven dimension advanced together
     (one apply launch per step for all sectors, the run captured in one CUDA graph), FP32 vectors with FP64
     recurrence coefficients, against the same run in plain FP64."""
     import numpy as np
@@ -253,7 +253,7 @@ def torch_sync():
 
 
 def serve_leg(args):
-    """Config-5 style request loop: Poisson phase-diagram points over three resident sectors, served with
+    """Request loop: Poisson phase-diagram points over three resident sectors, served with
     `slots` concurrent solves, against the same requests solved one after another."""
     import qsi_subspace_ed_gb300 as q
     from qsi_subspace_ed_gb300 import serve, workloads

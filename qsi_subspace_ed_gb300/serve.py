@@ -190,7 +190,7 @@ class RequestLoop:
 
 def poisson_requests(n: int, rate: float, sector_weights: dict[str, float], seed: int = 5, nev: int = 5,
                      tol: float = 1e-9) -> list[tuple[float, Request]]:
-    """Config-5 style arrivals: g ~ U[0,1]^4, B = |B| n with |B| ~ U[0,1] and n uniform on the sphere."""
+    """Phase-diagram arrivals: g ~ U[0,1]^4, B = |B| n with |B| ~ U[0,1] and n uniform on the sphere."""
     rng = np.random.default_rng(seed)
     names = list(sector_weights)
     p = np.array([sector_weights[k] for k in names], dtype=float)

@@ -254,7 +254,9 @@ typedef struct qsi_lanczos_cfg {
     int32_t precision;    /* QSI_F64, or QSI_F32 = FP32 vectors + FP64 recurrences */
     double tol;           /* relative residual tolerance (10^--atol) */
     uint64_t seed;        /* start vector seed (N(0,1)) */
-    int32_t polish_steps; /* FP64 Rayleigh-Ritz polish rounds after convergence */
+    int32_t polish_steps; /* FP64 Rayleigh-Ritz polish rounds after convergence; with QSI_F32 and
+                             >= 2 rounds the FP32 Krylov phase stops at max(tol, 1e-7) and the
+                             FP64 rounds (the 2nd on [X, HX - X theta]) refine the pairs */
     int32_t want_vectors; /* write eigenvectors */
 } qsi_lanczos_cfg;
 

@@ -478,7 +478,11 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     int nev = std::min(cfg.nev, std::max(1, m - 1));  // compute_spectrum_iterative clamps, matrix_diag_bits.hpp:64-66
     if (nev < 1 || m < 2) return fail(QSI_INVALID_ARG, "lanczos: need ncv >= 2 and nev >= 1");
     if (m > 126) return fail(QSI_INVALID_ARG, "lanczos: ncv must be <= 126");
-    const double tol = cfg.tol > 0 ? cfg.tol : 1e-10;
+    // FP32 Krylov vectors followed by at least two FP64 polish rounds (Rayleigh-Ritz, then residual-augmented
+    // Rayleigh-Ritz): the Krylov phase stops at a residual FP32 vectors resolve (1e-7 relative) and the FP64
+    // rounds take the pairs the rest of the way; otherwise it runs to tol itself.
+    const double tol_req = cfg.tol > 0 ? cfg.tol : 1e-10;
+    const double tol = (sizeof(VT) == 4 && cfg.polish_steps >= 2) ? std::max(tol_req, 1e-7) : tol_req;
     const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
     Vecs vx;
     qsi_status s = vx.init(n, st);

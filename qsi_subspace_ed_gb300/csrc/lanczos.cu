@@ -1399,7 +1399,7 @@ __global__ void __launch_bounds__(256) k_ftlm_update(VT* __restrict__ prev, cons
 
 // v *= inv per column (1/beta from k_col_reduce; a double-float multiply for FP32 storage).  With v2 (the
 // two-block recurrence) also v2 *= -beta, the next step's accumulated term.  R is a power of two.
-template <typename VT, int VW>
+template <typename VT>
 __device__ __forceinline__ VT col_mul(VT x, double c, float2 c_ff) {
     if constexpr (sizeof(VT) == 4) {
         const float xf = (float)x;
@@ -1421,14 +1421,13 @@ __global__ void k_col_scale(VT* __restrict__ v, const double* __restrict__ inv, 
         load_vec<VT, VW>(v + e * VW, x);
 #pragma unroll
         for (int k = 0; k < VW; ++k)
-            x[k] = col_mul<VT, VW>(x[k], inv[c0 + k], sizeof(VT) == 4 ? inv_ff[c0 + k] : make_float2(0.f, 0.f));
+            x[k] = col_mul<VT>(x[k], inv[c0 + k], sizeof(VT) == 4 ? inv_ff[c0 + k] : make_float2(0.f, 0.f));
         store_vec<VT, VW>(v + e * VW, x);
         if (v2) {
             load_vec<VT, VW>(v2 + e * VW, x);
 #pragma unroll
             for (int k = 0; k < VW; ++k)
-                x[k] = col_mul<VT, VW>(x[k], -beta[c0 + k],
-                                       sizeof(VT) == 4 ? nbeta_ff[c0 + k] : make_float2(0.f, 0.f));
+                x[k] = col_mul<VT>(x[k], -beta[c0 + k], sizeof(VT) == 4 ? nbeta_ff[c0 + k] : make_float2(0.f, 0.f));
             store_vec<VT, VW>(v2 + e * VW, x);
         }
     }

@@ -16,8 +16,10 @@ writes small files next to this script:
   eigs_q0_32.json           FP64 lowest eigenvalues of the 32-spin Q=0 ring/Zeeman Hamiltonian
   thermo_s4444.npz         exact E(T), C(T) of the 32-spin 4.4.4.4 sector
   observables48.npz        ring, ring_ring, partial_vol_sl0..3 of the reference's stored .eigs.out.h5
+  wide128.json, apply_wide128.npy   connectivity digest and y = H x from the reference code for the 32-spin
+                           Q=0 case with spin i at bit 4i+3 (states up to 128 bits)
 
-`python tests/golden/make_fixtures.py [REFERENCE_ROOT] observables` writes only the last file.
+`python tests/golden/make_fixtures.py [REFERENCE_ROOT] observables` (or `wide`) writes only those files.
 """
 from __future__ import annotations
 
@@ -152,9 +154,27 @@ def observables():
     print("observables48.npz written to", HERE)
 
 
+def wide():
+    """Reference connectivity and apply for states up to 128 bits (tests/helpers.py wide_case)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from helpers import wide_case
+
+    lohi, H, specs = wide_case()
+    r, c, v = O.triplets_ref(lohi, specs)
+    assert O.triplet_digest(r, c, v) == O.triplet_digest(*O.triplets_port(lohi, specs))
+    json.dump({"n_basis": int(len(lohi)), "basis_sha256": sha(lohi), "n_terms": len(specs), "n_triplets": int(len(r)),
+               "sha256": O.triplet_digest(r, c, v)}, open(HERE / "wide128.json", "w"), indent=1)
+    x = np.random.default_rng(128).standard_normal(len(lohi))
+    np.save(HERE / "apply_wide128.npy", np.stack([x, O.apply_ref(lohi, specs, x, threads=1)]))
+    print("wide128 fixtures written to", HERE)
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "observables":
         observables()
+    elif len(sys.argv) > 2 and sys.argv[2] == "wide":
+        wide()
     else:
         main()
         observables()
+        wide()

@@ -33,3 +33,28 @@ def cases():
         "q0_32": (q0_32.basis_lohi, q0_32.hamiltonian()),
         "s4444": (sec4.basis_lohi, sec4.hamiltonian()),
     }
+
+
+def wide_case():
+    """The 32-spin Q=0 basis and ring/Zeeman Hamiltonian with spin i moved to bit 4i+3 (states up to 128 bits,
+    beyond the 96 bits the hash index takes): (basis lohi, SymbolicOpSum, specs), matching
+    tests/golden/make_fixtures.py."""
+    import qsi_subspace_ed_gb300 as q
+    from qsi_subspace_ed_gb300 import workloads
+
+    w = workloads.q0_32spin()
+    wide = []
+    for lo, hi in w.basis_lohi:
+        s = int(lo) | (int(hi) << 64)
+        v = 0
+        for i in range(32):
+            if (s >> i) & 1:
+                v |= 1 << (4 * i + 3)
+        wide.append(v)
+    wide.sort()
+    lohi = np.array([[v & (2**64 - 1), v >> 64] for v in wide], dtype=np.uint64)
+    specs = [(c, ops, [4 * i + 3 for i in ids]) for c, ops, ids in w.hamiltonian().specs()]
+    H = q.SymbolicOpSum()
+    for c, ops, ids in specs:
+        H.add_term(c, q.SymbolicPMROperator(ops, ids))
+    return lohi, H, specs

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import qsi_subspace_ed_gb300 as q
-from helpers import GOLDEN, cases, golden_json
+from helpers import GOLDEN, cases, golden_json, wide_case
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -354,37 +354,22 @@ def test_matrix_market_export(built, name, tmp_path):
     assert abs(M - ref).max() == 0
 
 
-def _wide_case():
-    """The 32-spin Q=0 basis and ring/Zeeman Hamiltonian with spin i moved to bit 4i+3 (states up to 128 bits,
-    beyond the 96 bits the hash index takes): lookups go through the bucket table."""
-    basis, H = cases()["q0_32"]
-    spins = [(int(lo) | (int(hi) << 64)) for lo, hi in basis]
-    wide = []
-    for s in spins:
-        v = 0
-        for i in range(32):
-            if (s >> i) & 1:
-                v |= 1 << (4 * i + 3)
-        wide.append(v)
-    wide.sort()
-    lohi = np.array([[v & (2**64 - 1), v >> 64] for v in wide], dtype=np.uint64)
-    specs = [(c, ops, [4 * i + 3 for i in ids]) for c, ops, ids in H.specs()]
-    Hw = q.SymbolicOpSum()
-    for c, ops, ids in specs:
-        Hw.add_term(c, q.SymbolicPMROperator(ops, ids))
-    return lohi, Hw, specs
-
-
 def test_states_up_to_128_bits():
-    lohi, Hw, specs = _wide_case()
+    """The 32-spin Q=0 basis and ring/Zeeman Hamiltonian with spin i moved to bit 4i+3 (states up to 128 bits,
+    beyond the 96 bits the hash index takes): lookups go through the bucket table; connectivity and applies
+    equal the reference code's (fixtures) and the oracle's."""
+    lohi, Hw, specs = wide_case()
     assert int(lohi[:, 1].max()) >> 62  # bits above 96 are in use
     b = q.ZBasis(lohi)
     assert not b.index_info()["hash"]
     op = q.LazyOpSum(b, Hw)
     r, c, v = op.triplets()
-    assert O.triplet_digest(r, c, v) == O.triplet_digest(*O.triplets_port(lohi, specs))
-    x = np.random.default_rng(8).standard_normal(len(lohi))
+    assert O.triplet_digest(r, c, v) == golden_json("wide128.json")["sha256"]
+    x, y_ref = np.load(GOLDEN / "apply_wide128.npy")
     y = np.zeros_like(x)
+    op.evaluate(x, y)
+    np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+    x = np.random.default_rng(8).standard_normal(len(lohi))
     op.evaluate(x, y)
     ref = O.apply_port(lohi, specs, x, threads=1)
     np.testing.assert_allclose(y, ref, rtol=0, atol=1e-12 * np.abs(ref).max())

@@ -34,6 +34,22 @@ def test_oracle_apply_matches_reference_apply():
         np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-13 * np.abs(y_ref).max())
 
 
+def test_oracle_wide_states_match_reference():
+    """States up to 128 bits (spin i at bit 4i+3): connectivity digest and y = H x from the reference's own
+    operator code."""
+    from helpers import wide_case
+
+    lohi, H, specs = wide_case()
+    ref = golden_json("wide128.json")
+    assert len(lohi) == ref["n_basis"] and sha(lohi) == ref["basis_sha256"]
+    assert int(lohi[:, 1].max()) >> 62
+    r, c, v = O.triplets_port(lohi, specs)
+    assert len(r) == ref["n_triplets"] and O.triplet_digest(r, c, v) == ref["sha256"]
+    x, y_ref = np.load(GOLDEN / "apply_wide128.npy")
+    y = O.apply_port(lohi, specs, x, threads=1)
+    np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-13 * np.abs(y_ref).max())
+
+
 def test_oracle_golden_ground_state_energy():
     basis, H = cases()["golden48_JpmB"]
     g = golden_json("golden48.json")

@@ -475,9 +475,20 @@ def run_ours(args):
                     "vec_steps_per_s_incl_setup": R * M1 / t[M1], "seconds": {str(M0): t[M0], str(M1): t[M1]}}
 
         R_ftlm = args.ftlm_R or int(str(args.R).split(",")[0])
-        mixed = ftlm_rate(R_ftlm, "mixed")  # the batched settings tuned for R = first of --R
+        note = None
+        try:
+            mixed = ftlm_rate(R_ftlm, "mixed")  # the batched settings tuned for R = first of --R
+        except q.QsiError as e:  # device memory taken by others: half the vectors
+            if R_ftlm <= 16:
+                raise
+            note = f"R={R_ftlm} failed ({str(e)[:120]}); R={R_ftlm // 2} instead"
+            R_ftlm //= 2
+            torch.cuda.empty_cache()
+            mixed = ftlm_rate(R_ftlm, "mixed")
         free_b, total_b = torch.cuda.mem_get_info()
         mixed["vector_blocks"] = 3 if 3 * n * R_ftlm * 4 + (4 << 30) <= free_b else 2
+        if note:
+            mixed["note"] = note
         torch.cuda.empty_cache()
         plain = ftlm_rate(1, "f64")
         line["ftlm"] = {"value": mixed["vec_steps_per_s"], "unit": "vec-steps/s", "mixed": mixed, "plain_fp64": plain,

@@ -60,6 +60,37 @@ def test_oracle_golden_ground_state_energy():
     assert abs(abs(ev @ V[:, 0]) / np.linalg.norm(ev) - 1.0) < 1e-6
 
 
+def test_two_block_recurrence_equals_three_term_recurrence():
+    """The in-place two-block FTLM recurrence the GPU runs when three vector blocks do not fit
+    (P <- H C - beta_prev P; alpha = <C, P>; P <- P - alpha C; beta = |P|; P /= beta; swap) gives the three-term
+    recurrence's alphas and betas (W = H C; alpha = <C, W>; P <- W - alpha C - beta_prev P), FP64 numpy."""
+    basis, H = cases()["s4444"]
+    r, c, v = O.triplets_port(basis, H.specs())
+    A = O.csr_from_triplets(r, c, v, len(basis))
+    n, M = len(basis), 30
+    q0 = np.random.default_rng(3).choice([-1.0, 1.0], size=n) / np.sqrt(n)
+    a3, b3 = [], []
+    C, P, bp = q0.copy(), np.zeros(n), 0.0
+    for _ in range(M):
+        W = A @ C
+        al = C @ W
+        P = W - al * C - bp * P
+        bp = np.linalg.norm(P)
+        a3.append(al), b3.append(bp)
+        P, C = C, P / bp
+    a2, b2 = [], []
+    C, P, bp = q0.copy(), np.zeros(n), 0.0
+    for _ in range(M):
+        P = A @ C - bp * P
+        al = C @ P
+        P = P - al * C
+        bp = np.linalg.norm(P)
+        a2.append(al), b2.append(bp)
+        P, C = C, P / bp
+    np.testing.assert_allclose(a2[:20], a3[:20], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(b2[:20], b3[:20], rtol=0, atol=1e-12)
+
+
 def test_oracle_q0_32spin_eigs():
     basis, H = cases()["q0_32"]
     ref = golden_json("eigs_q0_32.json")["evals"]

@@ -417,11 +417,13 @@ def run_ours(args):
         Rs = [int(v) for v in str(args.R).split(",") if v]
         for R in Rs[1:] + Rs[:1]:
             tkey = "batched" if R == Rs[0] else f"batched_r{R}"
+            X = Y = None
             try:
                 X = torch.randn(n, R, dtype=torch.float32, device=dev)
                 Y = torch.zeros_like(X)
             except torch.cuda.OutOfMemoryError as e:  # device memory taken by others: report, go on
                 line["batched_mixed" if R == Rs[0] else f"batched_mixed_r{R}"] = {"R": R, "skipped": str(e)[:160]}
+                X = Y = None
                 torch.cuda.empty_cache()
                 continue
             if not args.no_tune:

@@ -70,12 +70,16 @@ def basis_footprint(dim: int) -> int:
 
 
 class RequestLoop:
+    """slots worker threads; solve(req, basis, sector) -> eigenvalues and make_basis(basis_lohi) -> resident basis
+    default to the device solve and ZBasis (both replaceable, e.g. by host-side fakes)."""
+
     def __init__(self, sectors: dict[str, Sector], slots: int = 4, hbm_budget: int = 200 << 30,
-                 solve: Callable | None = None):
+                 solve: Callable | None = None, make_basis: Callable | None = None):
         self.sectors = sectors
         self.slots = slots
         self.budget = hbm_budget
         self._solve = solve or self._solve_default
+        self._make_basis = make_basis or ZBasis
         self._lock = threading.Condition()
         self._waiting: deque[Request] = deque()
         self._running: dict[int, Request] = {}
@@ -162,7 +166,7 @@ class RequestLoop:
                 basis = self._bases.get(req.sector)
                 if basis is None:
                     sec = self.sectors[req.sector]
-                    basis = ZBasis(sec.basis_lohi)
+                    basis = self._make_basis(sec.basis_lohi)
                     self._bases[req.sector] = basis
                     self._in_use += basis_footprint(sec.dim)  # stays resident and accounted for
             req.start = time.perf_counter()

@@ -41,7 +41,11 @@ def build_port() -> Path:
     return PORT_SO
 
 
-def build_ref(reference_root: str = "/root/reference") -> Path | None:
+# where the reference checkout lies in the container that builds the checker (absent on GPU hosts)
+REFERENCE_ROOT = os.environ.get("QSI_REFERENCE_ROOT", "/root/reference")
+
+
+def build_ref(reference_root: str = REFERENCE_ROOT) -> Path | None:
     if not Path(reference_root).exists():
         return None
     deps = [HERE / "ref_harness.cpp", HERE / "build_ref.sh", HERE / "ref_shim" / "hdf5.h"]

@@ -169,3 +169,40 @@ def test_h5_string_round_trip(tmp_path):
     q._lib.call("qsi_h5_write_string", str(p).encode(), b"dset_name", b"basis", 1)
     assert _read_string_h5(p, "latfile_json") == "pyro_2,0,0_0,2,0_0,0,3.json"
     assert _read_string_h5(p, "dset_name") == "basis"
+
+
+def test_integration_binding_compiles_against_the_reference_headers(tmp_path):
+    """The C++ adaptor INTEGRATION.md gives (GB300LazyOpSum over SymbolicOpSum / ZBasisBST) compiles against the
+    reference's own operator.hpp and operator.cpp and links against libqsi_ed.so (no GPU call is made)."""
+    import shutil
+    import subprocess
+
+    from oracle import oracle as O
+
+    ref = Path(O.REFERENCE_ROOT)
+    if not shutil.which("g++") or not (ref / "components" / "operator" / "src" / "operator.cpp").exists():
+        pytest.skip("needs g++ and the reference checkout")
+    code = re.search(r"```cpp\n(.*?)```", (ROOT / "INTEGRATION.md").read_text(), re.S).group(1)
+    main = """
+int main(int argc, char**) {
+    if (argc < 0) {
+        ZBasisBST basis;
+        SymbolicOpSum<double> H;
+        GB300LazyOpSum<ZBasisBST> op(basis, H);
+        std::vector<double> x(op.rows()), y(op.rows());
+        op.evaluate(x.data(), y.data());
+        op.evaluate_add(x.data(), y.data());
+    }
+    return 0;
+}
+"""
+    src = tmp_path / "binding.cpp"
+    src.write_text(code + main)
+    lib = Path(_lib.LIB_PATH)
+    cmd = ["g++", "-std=c++17", "-fopenmp", f"-I{ROOT / 'oracle' / 'ref_shim'}",
+           f"-I{ref / 'components' / 'operator' / 'include'}", f"-I{ref / 'components' / 'common' / 'include'}",
+           f"-I{ROOT / 'include'}", str(src), str(ref / "components" / "operator" / "src" / "operator.cpp"),
+           f"-L{lib.parent}", "-lqsi_ed", f"-Wl,-rpath,{lib.parent}", "-o", str(tmp_path / "binding")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert subprocess.run([str(tmp_path / "binding")]).returncode == 0

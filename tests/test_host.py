@@ -206,3 +206,22 @@ int main(int argc, char**) {
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
     assert subprocess.run([str(tmp_path / "binding")]).returncode == 0
+
+
+def test_reference_arm_runs_on_the_host():
+    """`bench.py --impl reference` (the restated push loop on the host cores) prints one contract line."""
+    import json
+    import subprocess
+    import sys
+
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--lattice", "pyro_1x2x1",
+                        "--full-basis", "--steps", "1", "--warmup", "1", "--cpu-seconds", "0.5"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = lines[0]
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "states/s"
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == "pyro_1x2x1.Q0" and d["config"]["n_states"] == 3618

@@ -225,3 +225,14 @@ def test_reference_arm_runs_on_the_host():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"] == "pyro_1x2x1.Q0" and d["config"]["n_states"] == 3618
+
+
+def test_device_path_fails_loudly_without_a_gpu():
+    """No host fallback: without a usable GPU the device entry points return an error, never a CPU result."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    basis = workloads.q0_32spin().basis_lohi
+    with pytest.raises(q.QsiError, match="QSI_CUDA_ERROR"):
+        q.ZBasis(basis)

@@ -223,6 +223,15 @@ def term_masks_ref(ops: str, ids):
     return m, sg.value
 
 
+def apply_state_ref(ops: str, ids, state: int):
+    """(new state, sign) of the reference's SymbolicPMROperator::applyState on a 128-bit state."""
+    lib = ref()
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    st = np.array([state & (2**64 - 1), state >> 64], dtype=np.uint64)
+    sg = lib.ref_apply_state(ops.encode(), _p(ids), len(ops), _p(st))
+    return int(st[0]) | (int(st[1]) << 64), int(sg)
+
+
 def triplets_ref(basis: np.ndarray, specs, tol: float = 1e-14):
     lib = ref()
     ops, ids, lens, coef, keep = _spec_args(specs)

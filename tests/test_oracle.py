@@ -145,3 +145,37 @@ def test_oracle_term_product_matches_reference_kats():
         assert sign_p == sign_w, kat["spec"]
         if sign_w != 0:  # a vanished operator's masks carry no meaning
             assert prod.tobytes() == whole.tobytes(), kat["spec"]
+
+
+def test_term_compiler_and_apply_state_match_the_reference_on_random_strings():
+    """2,000 seeded random operator strings (x X z Z + - p P q Q, repeated sites allowed, sites up to 127): the
+    library's term compiler gives the reference SymbolicPMROperator's masks and sign, and applyState on random
+    128-bit states gives its state and sign."""
+    import qsi_subspace_ed_gb300 as q
+
+    if O.ref() is None:
+        pytest.skip("the reference checkout is absent")
+    rng = np.random.default_rng(2024)
+    alphabet = "xXzZ+-pPqQ"
+    for _ in range(2000):
+        k = int(rng.integers(1, 9))
+        ops = "".join(rng.choice(list(alphabet), size=k))
+        if rng.random() < 0.03:  # an operator letter neither accepts
+            ops = ops[:-1] + "y"
+        hi = 128 if rng.random() < 0.5 else 16  # small site ranges make repeated sites common
+        ids = [int(v) for v in rng.integers(0, hi, size=k)]
+        try:
+            m_ref, sg_ref = O.term_masks_ref(ops, ids)
+        except ValueError:
+            with pytest.raises(q.QsiError):
+                q.SymbolicPMROperator(ops, ids)
+            continue
+        op = q.SymbolicPMROperator(ops, ids)
+        words = [op.t.x[0], op.t.x[1], op.t.z[0], op.t.z[1], op.t.up[0], op.t.up[1], op.t.down[0], op.t.down[1]]
+        assert [int(w) for w in words] == [int(w) for w in m_ref], (ops, ids)
+        assert op.sign == sg_ref, (ops, ids)
+        for _ in range(4):
+            s = int(rng.integers(0, 2**63)) | (int(rng.integers(0, 2**63)) << 64)
+            if rng.random() < 0.5:  # states that satisfy the string's requirements as well
+                s = (s | int(m_ref[4]) | (int(m_ref[5]) << 64)) & ~(int(m_ref[6]) | (int(m_ref[7]) << 64))
+            assert op.applyState(s) == O.apply_state_ref(ops, ids, s), (ops, ids, s)

@@ -179,3 +179,50 @@ def test_term_compiler_and_apply_state_match_the_reference_on_random_strings():
             if rng.random() < 0.5:  # states that satisfy the string's requirements as well
                 s = (s | int(m_ref[4]) | (int(m_ref[5]) << 64)) & ~(int(m_ref[6]) | (int(m_ref[7]) << 64))
             assert op.applyState(s) == O.apply_state_ref(ops, ids, s), (ops, ids, s)
+
+
+def test_oracle_connectivity_matches_the_reference_on_random_128_bit_bases():
+    """Seeded random ring-like terms on sites up to 127 and bases grown from random states by those terms (hits
+    inside, misses at the frontier): the oracle's triplets are the reference's bit for bit, and its applies agree."""
+    if O.ref() is None:
+        pytest.skip("the reference checkout is absent")
+    rng = np.random.default_rng(77)
+    for case in range(3):
+        specs = []
+        for _ in range(12):
+            sites = [int(v) for v in rng.choice(128, size=6, replace=False)]
+            c = float(rng.uniform(-1, 1))
+            specs += [(c, "+-+-+-", sites), (c, "-+-+-+", sites)]
+        specs += [(float(rng.uniform(-1, 1)), "z", [int(rng.integers(0, 128))]) for _ in range(4)]
+        seen = set()
+        frontier = []
+        for _ in range(20):  # random states with as many rings as possible set to a flippable pattern
+            s = int(rng.integers(0, 2**63)) | (int(rng.integers(0, 2**63)) << 64) | (1 << 127) * int(case == 2)
+            fixed = {}
+            for _, ops, ids in specs[0:24:2]:
+                phase = int(rng.integers(0, 2))
+                want = [(k % 2) ^ phase for k in range(6)]  # alternating, either phase
+                if all(fixed.get(i, w) == w for i, w in zip(ids, want)):
+                    for i, w in zip(ids, want):
+                        fixed[i] = w
+            for i, w in fixed.items():
+                s = (s | (1 << i)) if w else (s & ~(1 << i))
+            seen.add(s)
+            frontier.append(s)
+        while frontier and len(seen) < 3000:
+            s = frontier.pop(0)
+            for _, ops, ids in specs:
+                t, sg = O.apply_state_ref(ops, ids, s)
+                if sg and t not in seen and rng.random() < 0.7:  # leave some targets out: misses
+                    seen.add(t)
+                    frontier.append(t)
+        states = sorted(seen)
+        basis = np.array([[v & (2**64 - 1), v >> 64] for v in states], dtype=np.uint64)
+        r1, c1, v1 = O.triplets_port(basis, specs)
+        r2, c2, v2 = O.triplets_ref(basis, specs)
+        assert len(basis) > 1000 and len(r1) > 4 * len(basis)  # off-diagonal hits present
+        assert O.triplet_digest(r1, c1, v1) == O.triplet_digest(r2, c2, v2), case
+        x = rng.standard_normal(len(basis))
+        y1 = O.apply_port(basis, specs, x, threads=1)
+        y2 = O.apply_ref(basis, specs, x, threads=1)
+        np.testing.assert_allclose(y1, y2, rtol=0, atol=1e-13 * np.abs(y2).max())

@@ -83,6 +83,16 @@ def port():
         lib.oracle_evaluate_add_rows.restype = C.c_int
         lib.oracle_evaluate_add_rows.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_int,
                                                  C.c_void_p, C.c_void_p, C.c_int]
+        lib.oracle_interp_build.restype = C.c_void_p
+        lib.oracle_interp_build.argtypes = [C.c_void_p, C.c_int64]
+        lib.oracle_interp_free.restype = None
+        lib.oracle_interp_free.argtypes = [C.c_void_p]
+        lib.oracle_interp_search_many.restype = None
+        lib.oracle_interp_search_many.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        lib.oracle_evaluate_add_rows_interp.restype = C.c_int
+        lib.oracle_evaluate_add_rows_interp.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
+                                                        C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                                        C.c_void_p]
         _port = lib
     return _port
 
@@ -190,6 +200,48 @@ def apply_rows_port(basis: np.ndarray, terms: np.ndarray, x: np.ndarray, y: np.n
     """Push loop over source rows [row_begin, row_end) only (CPU-baseline sample)."""
     port().oracle_evaluate_add_rows(_p(basis), len(basis), row_begin, row_end, _p(terms), len(terms), _p(x), _p(y),
                                     threads)
+
+
+class InterpIndex:
+    """ZBasisInterp's high-word bounds over a sorted basis (restated; the basis array must outlive it)."""
+
+    def __init__(self, basis: np.ndarray):
+        self.basis = np.ascontiguousarray(basis, dtype=np.uint64)
+        self.h = port().oracle_interp_build(_p(self.basis), len(self.basis))
+        if not self.h:
+            raise MemoryError("interp index")
+
+    def search(self, queries: np.ndarray) -> np.ndarray:
+        """Index per query, -1 when absent, -2 for an unseen high word (where the reference throws)."""
+        q = np.ascontiguousarray(queries, dtype=np.uint64)
+        idx = np.zeros(len(q), np.int64)
+        port().oracle_interp_search_many(self.h, _p(self.basis), _p(q), len(q), _p(idx))
+        return idx
+
+    def apply_rows(self, terms: np.ndarray, x: np.ndarray, y: np.ndarray, row_begin: int, row_end: int,
+                   threads: int = 0) -> int:
+        """The push loop with ZBasisInterp lookups over source rows [row_begin, row_end); returns the number of
+        lookups with an unseen high word."""
+        unseen = C.c_int64(0)
+        rc = port().oracle_evaluate_add_rows_interp(_p(self.basis), len(self.basis), row_begin, row_end, _p(terms),
+                                                    len(terms), _p(x), _p(y), threads, self.h, C.byref(unseen))
+        if rc != 0:
+            raise RuntimeError("oracle_evaluate_add_rows_interp failed")
+        return unseen.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            port().oracle_interp_free(self.h)
+            self.h = None
+
+
+def search_interp_ref(basis: np.ndarray, queries: np.ndarray) -> np.ndarray:
+    """The reference's ZBasisInterp::search: index, -1 absent, -2 where it throws (unseen high word)."""
+    lib = ref()
+    q = np.ascontiguousarray(queries, dtype=np.uint64)
+    idx = np.zeros(len(q), np.int64)
+    lib.ref_search_interp(_p(basis), C.c_int64(len(basis)), _p(q), C.c_int64(len(q)), _p(idx))
+    return idx
 
 
 def triplets_port(basis: np.ndarray, specs, tol: float = 1e-14):

@@ -9,6 +9,8 @@
  *                         (components/operator/include/operator.hpp:383-466)
  *   oracle_apply_state    SymbolicPMROperator::applyState (operator.hpp:232-254)
  *   oracle_search         ZBasisBST::search (components/operator/src/operator.cpp:4-34)
+ *   oracle_interp_*       ZBasisInterp::find_bounds + search (operator.cpp:38-86), the basis class of
+ *                         diag_DOQSI_ham and bench_apply (src/diag_DOQSI_ham.cpp:97, bench/bench_apply.cpp:44)
  *   oracle_evaluate_add   LazyOpSum::evaluate_add_off_diag_omp + evaluate_add_diagonal
  *                         (components/operator/src/operator_matrix.cpp:28-82,108-112):
  *                         per term, an OpenMP loop over rows, push y[J] += c x[i] sign
@@ -73,6 +75,105 @@ int oracle_search(const uint64_t* basis, int64_t n, const uint64_t st[2], int64_
     return 0;
 }
 
+/* ZBasisInterp: find_bounds keeps, per high 64-bit word, the first and last index of the states that carry it
+ * (an std::unordered_map there, open addressing here); search takes those bounds (an unseen high word makes
+ * bounds.at throw there: here the lookup is a miss, counted), bisects on the LOW word only while the window
+ * exceeds 32 entries, then compares whole states four at a time and one at a time. */
+typedef struct {
+    uint64_t key;
+    int64_t first, last;
+    int used;
+} ibucket;
+typedef struct {
+    ibucket* t;
+    uint64_t mask;
+} interp_t;
+
+static inline uint64_t mix64(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdULL;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ULL;
+    k ^= k >> 33;
+    return k;
+}
+
+static const ibucket* interp_find(const interp_t* ip, uint64_t key) {
+    for (uint64_t s = mix64(key) & ip->mask;; s = (s + 1) & ip->mask) {
+        const ibucket* b = &ip->t[s];
+        if (!b->used) return NULL;
+        if (b->key == key) return b;
+    }
+}
+
+void* oracle_interp_build(const uint64_t* basis, int64_t n) {
+    int64_t distinct = 0;
+    for (int64_t j = 0; j < n; ++j)
+        if (j == 0 || basis[2 * j + 1] != basis[2 * j - 1]) ++distinct;
+    uint64_t cap = 16;
+    while (cap < 2 * (uint64_t)distinct) cap <<= 1;
+    interp_t* ip = (interp_t*)malloc(sizeof(interp_t));
+    if (!ip) return NULL;
+    ip->t = (ibucket*)calloc(cap, sizeof(ibucket));
+    ip->mask = cap - 1;
+    if (!ip->t) {
+        free(ip);
+        return NULL;
+    }
+    /* the basis is sorted by (hi, lo): each high word's states are one run [first, last] */
+    for (int64_t j = 0; j < n;) {
+        const uint64_t key = basis[2 * j + 1];
+        int64_t e = j;
+        while (e + 1 < n && basis[2 * (e + 1) + 1] == key) ++e;
+        uint64_t s = mix64(key) & ip->mask;
+        while (ip->t[s].used) s = (s + 1) & ip->mask;
+        ip->t[s].used = 1;
+        ip->t[s].key = key;
+        ip->t[s].first = j;
+        ip->t[s].last = e;
+        j = e + 1;
+    }
+    return ip;
+}
+
+void oracle_interp_free(void* h) {
+    interp_t* ip = (interp_t*)h;
+    if (ip) free(ip->t);
+    free(ip);
+}
+
+/* 1 = found (J), 0 = absent, -1 = absent with an unseen high word (where the reference throws) */
+int oracle_interp_search(const void* h, const uint64_t* basis, const uint64_t st[2], int64_t* J) {
+    const ibucket* b = interp_find((const interp_t*)h, st[1]);
+    if (!b) return -1;
+    const u128 s = mk(st);
+    int64_t left = b->first, right = b->last;
+    while (right - left > 32) {
+        int64_t mid = (left + right) / 2;
+        if (basis[2 * mid] < st[0]) left = mid + 1;
+        else right = mid;
+    }
+    int64_t j = left;
+    for (; j + 3 <= right; j += 4) {
+        if (mk(basis + 2 * j) == s) { *J = j; return 1; }
+        if (mk(basis + 2 * (j + 1)) == s) { *J = j + 1; return 1; }
+        if (mk(basis + 2 * (j + 2)) == s) { *J = j + 2; return 1; }
+        if (mk(basis + 2 * (j + 3)) == s) { *J = j + 3; return 1; }
+    }
+    for (; j <= right; ++j)
+        if (j >= 0 && mk(basis + 2 * j) == s) { *J = j; return 1; }
+    return 0;
+}
+
+/* ZBasisInterp::search over nq queries: index, -1 absent, -2 unseen high word */
+void oracle_interp_search_many(const void* h, const uint64_t* basis, const uint64_t* q, int64_t nq, int64_t* idx) {
+    for (int64_t k = 0; k < nq; ++k) {
+        int64_t J = -1;
+        const int f = oracle_interp_search(h, basis, q + 2 * k, &J);
+        idx[k] = f == 1 ? J : (f == 0 ? -1 : -2);
+    }
+}
+
 static void split_terms(const oterm* terms, int n, const oterm** off, int* n_off, const oterm** dg, int* n_dg) {
     int a = 0, b = 0;
     for (int k = 0; k < n; ++k) {
@@ -126,6 +227,58 @@ int oracle_evaluate_add(const uint64_t* basis, int64_t n, const oterm* terms, in
             y[i] += dy;
         }
     }
+    free(off);
+    free(dg);
+    return 0;
+}
+
+/* The push loop over source rows [row_begin, row_end) with ZBasisInterp lookups (interp from
+ * oracle_interp_build), as diag_DOQSI_ham and bench_apply run it; *unseen counts the lookups whose high word the
+ * basis lacks (the reference throws on the first).  A bounded sample of one apply for the CPU baseline. */
+int oracle_evaluate_add_rows_interp(const uint64_t* basis, int64_t n, int64_t row_begin, int64_t row_end,
+                                    const oterm* terms, int n_terms, const double* x, double* y, int n_threads,
+                                    const void* interp, int64_t* unseen) {
+    const oterm** off = (const oterm**)malloc(sizeof(oterm*) * (size_t)(n_terms + 1));
+    const oterm** dg = (const oterm**)malloc(sizeof(oterm*) * (size_t)(n_terms + 1));
+    if (!off || !dg || !interp) return -1;
+    (void)n;
+    int n_off, n_dg;
+    split_terms(terms, n_terms, off, &n_off, dg, &n_dg);
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+    (void)n_threads;
+#endif
+    int64_t bad = 0;
+    for (int t = 0; t < n_off; ++t) {
+        const oterm* T = off[t];
+        const double c = T->c;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+        for (int64_t i = row_begin; i < row_end; ++i) {
+            uint64_t st[2] = {basis[2 * i], basis[2 * i + 1]};
+            int sign = oracle_apply_state(T, st);
+            if (sign != 0 && fabs(x[i]) > 1e-15) {
+                int64_t J = 0;
+                const int f = oracle_interp_search(interp, basis, st, &J);
+                if (f < 0) ++bad;
+                if (f == 1) {
+                    double dy = c * x[i] * sign;
+#pragma omp atomic
+                    y[J] += dy;
+                }
+            }
+        }
+    }
+    for (int t = 0; t < n_dg; ++t) {
+        const oterm* T = dg[t];
+        const double c = T->c;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = row_begin; i < row_end; ++i) {
+            uint64_t st[2] = {basis[2 * i], basis[2 * i + 1]};
+            y[i] += c * x[i] * (double)oracle_apply_state(T, st);
+        }
+    }
+    if (unseen) *unseen = bad;
     free(off);
     free(dg);
     return 0;

@@ -7,6 +7,7 @@
 // compiled here because they need Eigen.
 #include <cmath>
 #include <cstring>
+#include <stdexcept>
 #include <vector>
 #include <omp.h>
 
@@ -29,6 +30,15 @@ struct RefBasis : ZBasisBST {
     RefBasis(const uint64_t* lohi, int64_t n) {
         states.resize(n);
         for (int64_t i = 0; i < n; ++i) states[i] = Uint128(lohi[2 * i + 1], lohi[2 * i]);
+    }
+};
+
+// The basis class diag_DOQSI_ham and bench_apply use: high-word buckets (find_bounds) + ZBasisInterp::search.
+struct RefInterp : ZBasisInterp {
+    RefInterp(const uint64_t* lohi, int64_t n) {
+        states.resize(n);
+        for (int64_t i = 0; i < n; ++i) states[i] = Uint128(lohi[2 * i + 1], lohi[2 * i]);
+        find_bounds();
     }
 };
 
@@ -77,6 +87,21 @@ int ref_search(const uint64_t* basis, int64_t n, const uint64_t* q, int64_t nq, 
         ZBasisBase::idx_t J = 0;
         int f = B.search(Uint128(q[2 * k + 1], q[2 * k]), J);
         idx[k] = f ? J : -1;
+    }
+    return 0;
+}
+
+// ZBasisInterp::search per query: the index, -1 when absent, -2 when the reference throws (an unseen high word).
+int ref_search_interp(const uint64_t* basis, int64_t n, const uint64_t* q, int64_t nq, int64_t* idx) {
+    RefInterp B(basis, n);
+    for (int64_t k = 0; k < nq; ++k) {
+        ZBasisBase::idx_t J = 0;
+        try {
+            int f = B.search(Uint128(q[2 * k + 1], q[2 * k]), J);
+            idx[k] = f ? J : -1;
+        } catch (const std::out_of_range&) {
+            idx[k] = -2;
+        }
     }
     return 0;
 }

@@ -226,3 +226,40 @@ def test_oracle_connectivity_matches_the_reference_on_random_128_bit_bases():
         y1 = O.apply_port(basis, specs, x, threads=1)
         y2 = O.apply_ref(basis, specs, x, threads=1)
         np.testing.assert_allclose(y1, y2, rtol=0, atol=1e-13 * np.abs(y2).max())
+
+
+def test_interp_search_restatement_matches_the_reference():
+    """ZBasisInterp (high-word bounds + low-word bisection, the basis class of diag_DOQSI_ham and bench_apply):
+    the restatement returns the reference's answer for members, absent states and unseen high words."""
+    from helpers import wide_case
+
+    if O.ref() is None:
+        pytest.skip("the reference checkout is absent")
+    rng = np.random.default_rng(5)
+    bases = [cases()["q0_32"][0], wide_case()[0]]
+    # a 128-bit basis with many high words and a few long runs of one high word
+    pairs = sorted({(int(h) << 40, int(v)) for h, v in zip(rng.integers(0, 50, 6000), rng.integers(0, 2**63, 6000))})
+    bases.append(np.array([[v, h] for h, v in pairs], dtype=np.uint64))
+    for basis in bases:
+        flipped = basis[rng.integers(0, len(basis), 400)].copy()
+        flipped[:, 0] ^= np.uint64(1) << np.uint64(int(rng.integers(0, 64)))
+        unseen = basis[rng.integers(0, len(basis), 100)].copy()
+        unseen[:, 1] ^= np.uint64(1) << np.uint64(63)
+        queries = np.concatenate([basis[rng.integers(0, len(basis), 500)], flipped, unseen])
+        ix = O.InterpIndex(basis)
+        got, want = ix.search(queries), O.search_interp_ref(basis, queries)
+        assert np.array_equal(got, want)
+        assert (got[:500] >= 0).all() and (got[-100:] == -2).all()
+
+
+def test_interp_push_loop_equals_the_bisection_push_loop():
+    """The push loop with ZBasisInterp lookups (the CPU baseline) gives the ZBasisBST push loop's y bitwise."""
+    from helpers import wide_case
+
+    for basis, specs in [(cases()["q0_32"][0], cases()["q0_32"][1].specs()), wide_case()[::2]]:
+        terms = O.terms_array(specs)
+        x = np.random.default_rng(1).standard_normal(len(basis))
+        y1, y2 = np.zeros(len(basis)), np.zeros(len(basis))
+        O.apply_rows_port(basis, terms, x, y1, 0, len(basis), threads=1)
+        assert O.InterpIndex(basis).apply_rows(terms, x, y2, 0, len(basis), threads=1) == 0
+        assert np.array_equal(y1, y2)

@@ -191,22 +191,33 @@ def cpu_baseline(w, H, seconds: float):
     n = len(w.basis_lohi)
     ix = getattr(w, "_interp_index", None)
     if ix is None:
-        ix = O.InterpIndex(w.basis_lohi)
+        try:
+            ix = O.InterpIndex(w.basis_lohi)
+        except MemoryError:
+            ix = False  # no room for the high-word bounds: whole-basis bisection (ZBasisBST) instead
         w._interp_index = ix
+
+    def run(rows):
+        if ix:
+            return ix.apply_rows(terms, x, y, 0, rows, threads)
+        O.apply_rows_port(w.basis_lohi, terms, x, y, 0, rows, threads)
+        return 0
+
     x = np.random.default_rng(0).standard_normal(n)
     y = np.zeros(n)
     rows = min(n, 20000)
     t0 = time.time()
-    unseen = ix.apply_rows(terms, x, y, 0, rows, threads)
+    unseen = run(rows)
     dt = time.time() - t0
     if dt < seconds / 4 and rows < n:
         rows = int(min(n, rows * max(1.0, seconds / max(dt, 1e-3))))
         y[:] = 0
         t0 = time.time()
-        unseen = ix.apply_rows(terms, x, y, 0, rows, threads)
+        unseen = run(rows)
         dt = time.time() - t0
+    lookups = "ZBasisInterp lookups" if ix else "ZBasisBST lookups"
     out = {"value": rows / dt, "unit": "states/s", "cores": threads, "kind": "port",
-           "sample": f"push-form apply (per-term OpenMP pass, atomic scatter, ZBasisInterp lookups) over source "
+           "sample": f"push-form apply (per-term OpenMP pass, atomic scatter, {lookups}) over source "
                      f"rows [0,{rows}) of {n} of {w.name}; {dt:.1f}s"}
     if unseen:
         out["note"] = f"{unseen} lookups hit an unseen high word (the reference throws there)"

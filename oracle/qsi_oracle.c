@@ -81,8 +81,7 @@ int oracle_search(const uint64_t* basis, int64_t n, const uint64_t st[2], int64_
  * exceeds 32 entries, then compares whole states four at a time and one at a time. */
 typedef struct {
     uint64_t key;
-    int64_t first, last;
-    int used;
+    uint32_t first, count; /* count 0: an empty slot */
 } ibucket;
 typedef struct {
     ibucket* t;
@@ -101,17 +100,18 @@ static inline uint64_t mix64(uint64_t k) {
 static const ibucket* interp_find(const interp_t* ip, uint64_t key) {
     for (uint64_t s = mix64(key) & ip->mask;; s = (s + 1) & ip->mask) {
         const ibucket* b = &ip->t[s];
-        if (!b->used) return NULL;
+        if (!b->count) return NULL;
         if (b->key == key) return b;
     }
 }
 
 void* oracle_interp_build(const uint64_t* basis, int64_t n) {
+    if (n < 1 || n >= ((int64_t)1 << 32)) return NULL;
     int64_t distinct = 0;
     for (int64_t j = 0; j < n; ++j)
         if (j == 0 || basis[2 * j + 1] != basis[2 * j - 1]) ++distinct;
     uint64_t cap = 16;
-    while (cap < 2 * (uint64_t)distinct) cap <<= 1;
+    while (cap < (uint64_t)distinct + (uint64_t)distinct / 2) cap <<= 1; /* load factor <= 2/3 */
     interp_t* ip = (interp_t*)malloc(sizeof(interp_t));
     if (!ip) return NULL;
     ip->t = (ibucket*)calloc(cap, sizeof(ibucket));
@@ -126,11 +126,10 @@ void* oracle_interp_build(const uint64_t* basis, int64_t n) {
         int64_t e = j;
         while (e + 1 < n && basis[2 * (e + 1) + 1] == key) ++e;
         uint64_t s = mix64(key) & ip->mask;
-        while (ip->t[s].used) s = (s + 1) & ip->mask;
-        ip->t[s].used = 1;
+        while (ip->t[s].count) s = (s + 1) & ip->mask;
         ip->t[s].key = key;
-        ip->t[s].first = j;
-        ip->t[s].last = e;
+        ip->t[s].first = (uint32_t)j;
+        ip->t[s].count = (uint32_t)(e - j + 1);
         j = e + 1;
     }
     return ip;
@@ -147,7 +146,7 @@ int oracle_interp_search(const void* h, const uint64_t* basis, const uint64_t st
     const ibucket* b = interp_find((const interp_t*)h, st[1]);
     if (!b) return -1;
     const u128 s = mk(st);
-    int64_t left = b->first, right = b->last;
+    int64_t left = b->first, right = (int64_t)b->first + b->count - 1;
     while (right - left > 32) {
         int64_t mid = (left + right) / 2;
         if (basis[2 * mid] < st[0]) left = mid + 1;

@@ -171,9 +171,9 @@ def test_h5_string_round_trip(tmp_path):
     assert _read_string_h5(p, "dset_name") == "basis"
 
 
-def test_integration_binding_compiles_against_the_reference_headers(tmp_path):
-    """The C++ adaptor INTEGRATION.md gives (GB300LazyOpSum over SymbolicOpSum / ZBasisBST) compiles against the
-    reference's own operator.hpp and operator.cpp and links against libqsi_ed.so (no GPU call is made)."""
+def test_reference_side_adaptor_compiles_against_the_reference_headers(tmp_path):
+    """include/gb300_lazy_op.hpp (GB300LazyOpSum over SymbolicOpSum / ZBasisBST) compiles against the reference's
+    own operator.hpp and operator.cpp and links against libqsi_ed.so (no GPU call is made)."""
     import shutil
     import subprocess
 
@@ -182,8 +182,7 @@ def test_integration_binding_compiles_against_the_reference_headers(tmp_path):
     ref = Path(O.REFERENCE_ROOT)
     if not shutil.which("g++") or not (ref / "components" / "operator" / "src" / "operator.cpp").exists():
         pytest.skip("needs g++ and the reference checkout")
-    code = re.search(r"```cpp\n(.*?)```", (ROOT / "INTEGRATION.md").read_text(), re.S).group(1)
-    main = """
+    main = """#include "gb300_lazy_op.hpp"
 int main(int argc, char**) {
     if (argc < 0) {
         ZBasisBST basis;
@@ -197,7 +196,7 @@ int main(int argc, char**) {
 }
 """
     src = tmp_path / "binding.cpp"
-    src.write_text(code + main)
+    src.write_text(main)
     lib = Path(_lib.LIB_PATH)
     cmd = ["g++", "-std=c++17", "-fopenmp", f"-I{ROOT / 'oracle' / 'ref_shim'}",
            f"-I{ref / 'components' / 'operator' / 'include'}", f"-I{ref / 'components' / 'common' / 'include'}",

@@ -29,28 +29,39 @@ REF_SO = HERE / "_ref" / "libqsi_ref.so"
 
 
 def build_port() -> Path:
-    srcs = [HERE / "qsi_oracle.c", HERE / "start_vector.cpp"]
+    srcs = [HERE / "qsi_oracle.c", HERE / "enumerate_oracle.c", HERE / "start_vector.cpp"]
     if not PORT_SO.exists() or PORT_SO.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
         tmp = PORT_SO.with_suffix(".tmp.so")
-        subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-c", str(srcs[0]), "-o", str(HERE / "qsi_oracle.o")],
-                       check=True)
-        subprocess.run(["g++", "-O2", "-fPIC", "-c", str(srcs[1]), "-o", str(HERE / "start_vector.o")], check=True)
-        subprocess.run(["g++", "-shared", "-fopenmp", str(HERE / "qsi_oracle.o"), str(HERE / "start_vector.o"),
-                        "-o", str(tmp)], check=True)
+        objs = []
+        for src in srcs:
+            obj = HERE / (src.stem + ".o")
+            cc = ["gcc", "-O3", "-fopenmp"] if src.suffix == ".c" else ["g++", "-O2"]
+            subprocess.run([*cc, "-fPIC", "-c", str(src), "-o", str(obj)], check=True)
+            objs.append(str(obj))
+        subprocess.run(["g++", "-shared", "-fopenmp", *objs, "-o", str(tmp)], check=True)
         os.replace(tmp, PORT_SO)
     return PORT_SO
 
 
-# where the reference checkout lies in the container that builds the checker (absent on GPU hosts)
-REFERENCE_ROOT = os.environ.get("QSI_REFERENCE_ROOT", "/root/reference")
+def reference_root() -> str | None:
+    """The qsi_subspace_ED checkout the reference-built checker compiles from: $QSI_REFERENCE_ROOT, else a
+    directory named `reference` beside this repository, else None (GPU hosts have no checkout)."""
+    env = os.environ.get("QSI_REFERENCE_ROOT")
+    if env:
+        return env if Path(env).exists() else None
+    sib = HERE.parent.parent / "reference"
+    return str(sib) if (sib / "components" / "operator").exists() else None
 
 
-def build_ref(reference_root: str = REFERENCE_ROOT) -> Path | None:
-    if not Path(reference_root).exists():
+def build_ref(root: str | None = None) -> Path | None:
+    """Builds the reference-built checker from the checkout at `root` (default: reference_root()); None where
+    there is no checkout."""
+    root = root or reference_root()
+    if not root or not Path(root).exists():
         return None
     deps = [HERE / "ref_harness.cpp", HERE / "build_ref.sh", HERE / "ref_shim" / "hdf5.h"]
     if not REF_SO.exists() or REF_SO.stat().st_mtime < max(d.stat().st_mtime for d in deps):
-        subprocess.run(["sh", str(HERE / "build_ref.sh"), reference_root], check=True, capture_output=True)
+        subprocess.run(["sh", str(HERE / "build_ref.sh"), root], check=True, capture_output=True)
     return REF_SO
 
 
@@ -93,6 +104,11 @@ def port():
         lib.oracle_evaluate_add_rows_interp.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
                                                         C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                                         C.c_void_p]
+        lib.oracle_enumerate.restype = C.c_int64
+        lib.oracle_enumerate.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                         C.c_int, C.c_int, C.POINTER(C.POINTER(C.c_uint64))]
+        lib.oracle_free.restype = None
+        lib.oracle_free.argtypes = [C.c_void_p]
         _port = lib
     return _port
 
@@ -406,6 +422,124 @@ def ftlm_oracle(r, c, v, n, R, M, seed, temps):
     E2 = (bf @ (ww * x * x)) / Z
     return {"T": np.asarray(temps), "E": E1 + e0, "C": (E2 - E1 * E1) / np.asarray(temps) ** 2, "ritz": ev,
             "weights": w}
+
+
+def _splitmix64(z: np.ndarray) -> np.ndarray:
+    """SplitMix64 finaliser (Steele, Lea, Flood 2014), elementwise on uint64 (wrapping arithmetic)."""
+    z = (z + np.uint64(0x9E3779B97F4A7C15)).astype(np.uint64)
+    z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)).astype(np.uint64)
+    z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)).astype(np.uint64)
+    return z ^ (z >> np.uint64(31))
+
+
+def ftlm_start_vectors(n: int, R: int, seed: int) -> np.ndarray:
+    """The engine's FTLM start block for one sector, restated: element (i, r) is +1/sqrt(n) when the top bit of
+    splitmix64(seed ^ splitmix64((r << 40) ^ i)) is set, else -1/sqrt(n).  Returns (n, R) FP64 (the
+    Rademacher start vectors of the FTLM workload; a sector s of a multi-sector run uses seed + s)."""
+    i = np.arange(n, dtype=np.uint64)
+    inv = 1.0 / np.sqrt(float(n))
+    out = np.empty((n, R))
+    with np.errstate(over="ignore"):
+        for r in range(R):
+            h = _splitmix64(np.uint64(seed) ^ _splitmix64((np.uint64(r) << np.uint64(40)) ^ i))
+            out[:, r] = np.where((h >> np.uint64(63)) != 0, inv, -inv)
+    return out
+
+
+def ftlm_recurrences(r, c, v, n, Q0: np.ndarray, M: int):
+    """Per-vector FP64 three-term Lanczos from the given start vectors (columns of Q0), M steps each:
+    w = H q; alpha = <q, w>; w -= alpha q + beta_prev q_prev; beta = |w|; q_prev, q = q, w / beta.
+    Returns (alphas, betas), each (R, M) -- the standard FTLM recurrence the ftlm workload defines (the
+    reference's own C++ FTLM, include/ftlm.hpp:19-142, is unbuilt)."""
+    H = csr_from_triplets(r, c, v, n)
+    R = Q0.shape[1]
+    A = np.zeros((R, M))
+    B = np.zeros((R, M))
+    for k in range(R):
+        q = Q0[:, k].copy()
+        qp = np.zeros(n)
+        beta = 0.0
+        for j in range(M):
+            w = H @ q
+            al = float(q @ w)
+            w -= al * q + beta * qp
+            beta = float(np.sqrt(w @ w))
+            A[k, j], B[k, j] = al, beta
+            qp, q = q, w / beta
+    return A, B
+
+
+def ftlm_thermo_oracle(alphas, betas, n: int, temps, e_ref: float | None = None):
+    """E(T) and C(T) from FTLM recurrences: Ritz values e_rj and weights (first eigenvector component)^2 of each
+    tridiagonal by numpy eigh, Z = n/R sum exp(-(e - e_ref)/T) w, C = (<E^2> - <E>^2) / T^2."""
+    R, M = alphas.shape
+    ev, ww = [], []
+    for k in range(R):
+        T = np.diag(alphas[k]) + np.diag(betas[k, :-1], 1) + np.diag(betas[k, :-1], -1)
+        w, Y = np.linalg.eigh(T)
+        ev.append(w)
+        ww.append(Y[0] ** 2)
+    ev = np.array(ev)
+    e0 = float(ev.min()) if e_ref is None else e_ref
+    x = (ev - e0).reshape(-1)
+    wt = np.array(ww).reshape(-1) * (n / R)
+    temps = np.asarray(temps, np.float64)
+    bf = np.exp(-np.outer(1.0 / temps, x))
+    Z = bf @ wt
+    E1 = (bf @ (wt * x)) / Z
+    E2 = (bf @ (wt * x * x)) / Z
+    return {"T": temps, "E": E1 + e0, "C": (E2 - E1 * E1) / temps ** 2, "e_ref": e0}
+
+
+def ring_zeeman_specs(lat: dict, g, B, Jpm: float = 0.0, kappa: float = 0.5):
+    """Term list [(c, op characters, spin ids)] of H = -sum_hex g[sl] (O + O^dagger) - sum_i (B . z_a(i)) kappa
+    z_i [- Jpm sum_bonds (S+_i S-_j + h.c.)], off-diagonal terms first, each group in insertion order
+    (SymbolicOpSum::add_term's split, components/operator/include/operator.hpp:489-495).  Ring operators follow
+    get_ring_ops (include/physics/geometry.hpp:29-62: six-member rings only, sign +1 -> '+', -1 -> '-', O^dagger
+    with the signs flipped) and are added as (-g, O^dagger) then (-g, O) per hexagon, as
+    include/hamiltonian_setup.hpp:36-43 adds them with its coupling; z_a are the rows of get_loc_z
+    (include/physics/Jring.hpp:6-14), B . z_a summed as (B0 z0 + B1 z1) + B2 z2."""
+    off, diag = [], []
+    for ring in lat.get("rings", []):
+        ids = [int(i) for i in ring["member_spin_idx"]]
+        if len(ids) != 6:
+            continue
+        ops = "".join("+" if v == 1 else "-" for v in ring["signs"])
+        conj = "".join("-" if v == 1 else "+" for v in ring["signs"])
+        off.append((-float(g[int(ring["sl"])]), conj, ids))
+        off.append((-float(g[int(ring["sl"])]), ops, ids))
+    if Jpm:
+        for bond in lat.get("bonds", []):
+            i, j = int(bond["from_idx"]), int(bond["to_idx"])
+            off.append((-float(Jpm), "+-", [i, j]))
+            off.append((-float(Jpm), "-+", [i, j]))
+    lz = np.array([[1.0, 1.0, 1.0], [1.0, -1.0, -1.0], [-1.0, 1.0, -1.0], [-1.0, -1.0, 1.0]]) / np.sqrt(3.0)
+    for i, a in enumerate(lat["atoms"]):
+        z = lz[int(a["sl"])]
+        h = (float(B[0]) * float(z[0]) + float(B[1]) * float(z[1])) + float(B[2]) * float(z[2])
+        diag.append((-h * kappa, "z", [i]))
+    return off + diag
+
+
+def enumerate_basis_oracle(lat: dict, sector=None, n_spinon_pairs: int = 0, threads: int = 0) -> np.ndarray:
+    """The reference's basis enumeration restated (oracle/enumerate_oracle.c): sorted (n, 2) uint64 (lo, hi)
+    rows for a lattice dict (atoms[{sl}], tetrahedra[{member_spin_idx}]); sector = per-sublattice up counts."""
+    sl = np.array([int(a["sl"]) for a in lat["atoms"]], dtype=np.int32)
+    mem = [list(t["member_spin_idx"]) for t in lat["tetrahedra"]]
+    off = np.zeros(len(mem) + 1, dtype=np.int32)
+    off[1:] = np.cumsum([len(m) for m in mem])
+    flat = np.array([i for m in mem for i in m], dtype=np.int32)
+    sec = None if sector is None else np.ascontiguousarray(sector, dtype=np.int32)
+    out = C.POINTER(C.c_uint64)()
+    n = port().oracle_enumerate(len(sl), _p(sl), len(mem), _p(off), _p(flat), None if sec is None else _p(sec),
+                                0 if sec is None else len(sec), int(n_spinon_pairs), int(threads), C.byref(out))
+    if n < 0:
+        raise MemoryError("oracle_enumerate failed (bad lattice or out of memory)")
+    try:
+        a = np.ctypeslib.as_array(out, shape=(max(int(n), 1) * 2,))[: 2 * int(n)].copy()
+    finally:
+        port().oracle_free(out)
+    return a.reshape(-1, 2)
 
 
 def set_random_unit(n: int, seed: int) -> np.ndarray:

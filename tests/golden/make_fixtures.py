@@ -1,7 +1,7 @@
 """Generates the golden fixtures of tests/golden from the reference checkout.
 
 Run where the reference exists (python tests/golden/make_fixtures.py
-[REFERENCE_ROOT]).  It reads the reference's own test data and drives the
+REFERENCE_ROOT).  It reads the reference's own test data and drives the
 reference's own operator code (oracle/_ref, built by oracle/build_ref.sh), and
 writes small files next to this script:
 
@@ -19,7 +19,7 @@ writes small files next to this script:
   wide128.json, apply_wide128.npy   connectivity digest and y = H x from the reference code for the 32-spin
                            Q=0 case with spin i at bit 4i+3 (states up to 128 bits)
 
-`python tests/golden/make_fixtures.py [REFERENCE_ROOT] observables` (or `wide`) writes only those files.
+`python tests/golden/make_fixtures.py REFERENCE_ROOT observables` (or `wide`) writes only those files.
 """
 from __future__ import annotations
 
@@ -39,7 +39,9 @@ import qsi_subspace_ed_gb300 as q  # noqa: E402
 from qsi_subspace_ed_gb300 import workloads  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) < 2:
+    sys.exit("usage: make_fixtures.py REFERENCE_ROOT  (the qsi_subspace_ED checkout the fixtures are made from)")
+REF = Path(sys.argv[1])
 T = REF / "test"
 GOLDEN_EIGS = T / "data" / "REFERENCE_Jpm=0.0200%Bx=0.1000%By=0.1000%Bz=0.1000%.eigs.h5"
 GOLDEN_OBS = T / "data" / "REFERENCE_Jpm=0.0200%Bx=0.1000%By=0.1000%Bz=0.1000%.eigs.out.h5"

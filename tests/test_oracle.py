@@ -1,4 +1,6 @@
 """The oracle (CPU restatement) against the reference's golden data."""
+import json
+
 import numpy as np
 import pytest
 
@@ -263,3 +265,44 @@ def test_interp_push_loop_equals_the_bisection_push_loop():
         O.apply_rows_port(basis, terms, x, y1, 0, len(basis), threads=1)
         assert O.InterpIndex(basis).apply_rows(terms, x, y2, 0, len(basis), threads=1) == 0
         assert np.array_equal(y1, y2)
+
+
+def test_oracle_enumerator_reproduces_reference_bases():
+    """The oracle's restatement of the reference's enumerator gives the reference's stored bases (digests of
+    test/data/*.reference.basis.h5 and the golden 48-spin basis)."""
+    ref = golden_json("bases.json")
+    for name in ["ref16", "ref32", "golden48"]:
+        lat = json.load(open(GOLDEN / "lattices" / f"{name}.json"))
+        b = O.enumerate_basis_oracle(lat)
+        assert len(b) == ref[name]["n"] and sha(b) == ref[name]["sha256"], name
+
+
+def test_oracle_enumerator_matches_the_engine_with_sectors_and_spinon_pairs():
+    """Sectors and 1-2 spinon pairs (whose set depends on the reference's admission test and visiting order):
+    the oracle's restatement and the engine's host enumerator give the same sorted bases."""
+    import qsi_subspace_ed_gb300 as q
+    from qsi_subspace_ed_gb300 import workloads
+
+    l32, l64 = workloads.lattice("pyro_1x2x1"), workloads.lattice("pyro_1x2x2")
+    for lat, sec, pairs, n in ((l32, None, 0, 3618), (l32, [4, 4, 4, 4], 0, 388), (l32, None, 1, 7236),
+                               (l32, None, 2, 234044), (l64, [8, 8, 8, 8], 0, 221628), (l64, [6, 8, 9, 9], 0, None)):
+        a = O.enumerate_basis_oracle(lat.data, sec, pairs)
+        b = q.enumerate_basis(lat, n_spinon_pairs=pairs, sector=sec)
+        assert np.array_equal(a, b), (lat.name(), sec, pairs)
+        if n is not None:
+            assert len(a) == n
+
+
+def test_oracle_hamiltonian_specs_match_the_engine():
+    """The oracle's ring/Zeeman/hopping term list equals the engine's, coefficients bitwise (the reference arm of
+    the benchmark builds its operator from it without the engine's library)."""
+    import qsi_subspace_ed_gb300 as q
+    from qsi_subspace_ed_gb300 import workloads
+
+    for name in ("pyro_1x2x1", "pyro_1x2x3"):
+        lat = workloads.lattice(name)
+        g, B = workloads.ring_zeeman_params(3, (0.2, 1.0), 0.5)
+        for Jpm in (0.0, 0.05):
+            a = O.ring_zeeman_specs(lat.data, g, B, Jpm)
+            b = q.build_ring_zeeman(lat, g, B, Jpm).specs()
+            assert [(c, ops, list(ids)) for c, ops, ids in a] == [(c, ops, list(ids)) for c, ops, ids in b]

@@ -129,14 +129,35 @@ qsi_status qsi_enumerate_basis(int32_t n_spins, const int32_t* tetra_spins,
                                int32_t ordering, int32_t n_threads,
                                uint64_t** out_lohi, int64_t* n_out);
 void qsi_free_host(void* p);
-/* The same enumeration on the GPU for bases without spinon pairs (ordering is
- * the greedy order; states of at most 128 spins, at most 128 tetrahedra and
- * 8 sublattices).  The sorted result is returned in host memory
- * (release with qsi_free_host). */
+/* The same enumeration on the GPU (ordering is the greedy order; states of at
+ * most 128 spins, at most 128 tetrahedra and 8 sublattices), with up to 64
+ * spinon pairs: the forking rule of fork_state_impl
+ * (components/build_basis/src/pyro_tree.cpp:168-189) with the reference's own
+ * admission test, so the set equals qsi_enumerate_basis's.  The sorted result
+ * is returned in host memory (release with qsi_free_host). */
 qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* tetra_spins,
                                    int32_t n_tetra, int32_t tetra_size,
                                    const int32_t* sublattice, int32_t n_sublattices,
-                                   const int32_t* sector, uint64_t** out_lohi, int64_t* n_out);
+                                   const int32_t* sector, int32_t n_spinon_pairs,
+                                   uint64_t** out_lohi, int64_t* n_out);
+/* Sublattice-polarisation sectors of a basis, on the GPU (replaces
+ * partition_basis_hdf5, components/build_basis/partition_basis.cpp:13-231):
+ * the sector of a state is its up count on each of the n_sl (1..8) sublattice
+ * masks (sl_masks: n_sl (lo, hi) pairs).  out_lohi (n x 2) receives the states
+ * grouped by sector, sectors in ascending order of their counts (first
+ * sublattice most significant), basis order kept inside each sector;
+ * sector_counts (n_sectors x n_sl) and sector_start (n_sectors + 1 entries,
+ * the last = n) describe the groups.  With out_lohi NULL only *n_sectors is
+ * set; more sectors than max_sectors is QSI_INVALID_ARG. */
+qsi_status qsi_partition_basis(const uint64_t* lohi, int64_t n, const uint64_t* sl_masks,
+                               int32_t n_sl, uint64_t* out_lohi, int32_t* sector_counts,
+                               int64_t* sector_start, int32_t max_sectors, int32_t* n_sectors);
+/* The partition_basis tool (partition_basis.cpp:231-269): reads the basis
+ * dataset (NULL: "basis") of in_path and writes out_path with one dataset per
+ * sector, named as make_sector_string names it (basis_io_h5.hpp:77-87):
+ * basis_s<n0>.<n1>...  (the datasets diag_DOQSI_ham --sector reads). */
+qsi_status qsi_partition_basis_h5(const char* in_path, const char* dataset, const char* out_path,
+                                  const uint64_t* sl_masks, int32_t n_sl);
 
 /* ---------------------------------------------------------------- device basis */
 /* Copies a sorted basis to the device and builds its top-bits bucket table.
@@ -172,13 +193,15 @@ qsi_status qsi_op_apply(qsi_op* op, const double* x, double* y, int32_t accumula
                         int32_t flags, void* stream);
 /* y = H x (accumulate = 0) or y += H x (accumulate = 1) for HOST x and y,
  * without allocating device memory: the vectors are staged through two
- * fixed arrays compiled into the library (4 MiB per GPU that loads it), for
- * callers whose process cannot make new device allocations (GPU memory owned
- * by another allocator or an exhausted quota).  At most 262,144 basis states
- * (QSI_INVALID_ARG beyond).  Calls share the arrays: calls that overlap on
- * the GPU race; consecutive calls from one thread do not.  The first call on
- * a device looks the arrays up, so make it before any stream capture; the
- * current device must be the operator's.  No counterpart in the reference. */
+ * fixed arrays compiled into the library, for callers whose process cannot
+ * make new device allocations (GPU memory owned by another allocator or an
+ * exhausted quota).  The arrays (4 MiB) and the apply kernels' code are
+ * reserved on a device by the first qsi_op_create there (CUDA loads device
+ * code lazily), not at library load; the call itself then reserves nothing.
+ * At most 262,144 basis states (QSI_INVALID_ARG beyond).  Calls share the
+ * arrays: calls that overlap on the GPU race; consecutive calls from one
+ * thread do not.  A call runs on the operator's device whatever the current
+ * device is.  No counterpart in the reference. */
 qsi_status qsi_op_apply_static(qsi_op* op, const double* x, double* y, int32_t accumulate);
 /* Batched apply over R vectors stored row-major [dim][R] (element type dtype:
  * QSI_F64, or QSI_F32 storage with FP64 per-row accumulation). */

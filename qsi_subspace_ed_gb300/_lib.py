@@ -99,7 +99,10 @@ SIGNATURES = {
     "qsi_enumerate_basis": [_I32, _P, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32,
                             C.POINTER(C.POINTER(C.c_uint64)), C.POINTER(_I64)],
     "qsi_free_host": [_P],
-    "qsi_enumerate_basis_gpu": [_I32, _P, _I32, _I32, _P, _I32, _P, C.POINTER(C.POINTER(C.c_uint64)), C.POINTER(_I64)],
+    "qsi_enumerate_basis_gpu": [_I32, _P, _I32, _I32, _P, _I32, _P, _I32, C.POINTER(C.POINTER(C.c_uint64)),
+                                C.POINTER(_I64)],
+    "qsi_partition_basis": [_P, _I64, _P, _I32, _P, _P, _P, _I32, C.POINTER(_I32)],
+    "qsi_partition_basis_h5": [C.c_char_p, C.c_char_p, C.c_char_p, _P, _I32],
     "qsi_basis_create": [_P, _I64, _I32, C.POINTER(_P)],
     "qsi_basis_destroy": [_P],
     "qsi_basis_dim": [_P, C.POINTER(_I64)],

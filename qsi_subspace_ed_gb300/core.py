@@ -233,8 +233,8 @@ def enumerate_basis(lattice, n_spinon_pairs: int = 0, sector=None, ordering: str
     return a
 
 
-def enumerate_basis_gpu(lattice, sector=None) -> np.ndarray:
-    """Sorted spin-ice basis without spinon pairs, enumerated on the GPU (same set as enumerate_basis)."""
+def enumerate_basis_gpu(lattice, sector=None, n_spinon_pairs: int = 0) -> np.ndarray:
+    """Sorted spin-ice basis enumerated on the GPU (same set as enumerate_basis, spinon pairs included)."""
     from .lattice import Lattice
 
     L = lattice if isinstance(lattice, Lattice) else Lattice.load(lattice)
@@ -244,12 +244,57 @@ def enumerate_basis_gpu(lattice, sector=None) -> np.ndarray:
     out = C.POINTER(C.c_uint64)()
     n = C.c_int64()
     call("qsi_enumerate_basis_gpu", L.n_spins, ptr(tets), tets.shape[0], tets.shape[1], ptr(sl), int(sl.max()) + 1,
-         ptr(sec) if sec is not None else None, C.byref(out), C.byref(n))
+         ptr(sec) if sec is not None else None, int(n_spinon_pairs), C.byref(out), C.byref(n))
     try:
         a = np.ctypeslib.as_array(out, shape=(max(1, n.value) * 2,))[: n.value * 2].reshape(-1, 2).copy()
     finally:
         _lib.load().qsi_free_host(C.cast(out, C.c_void_p))
     return a
+
+
+def sublattice_masks(lattice) -> np.ndarray:
+    """(n_sl, 2) uint64 (lo, hi) masks of the spins of each sublattice (partition_basis.cpp:256-260)."""
+    from .lattice import Lattice
+
+    L = lattice if isinstance(lattice, Lattice) else Lattice.load(lattice)
+    n_sl = int(L.sublattice.max()) + 1
+    m = np.zeros((n_sl, 2), dtype=np.uint64)
+    for i, a in enumerate(L.sublattice.tolist()):
+        m[a, i // 64] |= np.uint64(1) << np.uint64(i % 64)
+    return m
+
+
+def partition_basis(lohi: np.ndarray, lattice):
+    """Splits a sorted basis into its sublattice-polarisation sectors on the GPU.
+
+    Returns {sector counts (tuple): sorted (n_s, 2) uint64 states}, the sectors in ascending order of their counts;
+    the dataset name of a sector is sector_name(counts)."""
+    a = np.ascontiguousarray(lohi, dtype=np.uint64)
+    m = np.ascontiguousarray(sublattice_masks(lattice))
+    ns = C.c_int32()
+    call("qsi_partition_basis", ptr(a), len(a), ptr(m), len(m), None, None, None, 0, C.byref(ns))
+    out = np.zeros_like(a)
+    counts = np.zeros((ns.value, len(m)), dtype=np.int32)
+    starts = np.zeros(ns.value + 1, dtype=np.int64)
+    call("qsi_partition_basis", ptr(a), len(a), ptr(m), len(m), ptr(out), ptr(counts), ptr(starts), ns.value,
+         C.byref(ns))
+    return {tuple(int(v) for v in counts[k]): out[starts[k]:starts[k + 1]] for k in range(ns.value)}
+
+
+def sector_name(counts) -> str:
+    """make_sector_string (components/common/include/basis_io_h5.hpp:77-87): basis_s<n0>.<n1>.<n2>.<n3>."""
+    return "basis_s" + ".".join(str(int(c)) for c in counts)
+
+
+def partition_basis_h5(infile, lattice, outfile=None, dataset: str = "basis") -> Path:
+    """The partition_basis tool: INFILE's basis split into one dataset per sector in OUTFILE (default: INFILE with
+    its last extension replaced by .partitioned.h5, partition_basis.cpp:50-56)."""
+    infile = Path(infile)
+    if outfile is None:
+        outfile = infile.with_suffix(".partitioned.h5") if infile.suffix else Path(str(infile) + ".partitioned.h5")
+    m = np.ascontiguousarray(sublattice_masks(lattice))
+    call("qsi_partition_basis_h5", str(infile).encode(), dataset.encode(), str(outfile).encode(), ptr(m), len(m))
+    return Path(outfile)
 
 
 class ZBasis:
@@ -325,7 +370,8 @@ class LazyOpSum:
     cols = rows
 
     def set_kernel(self, kernel: int = 1, use_hash: bool = True, list_cap: int = 0) -> None:
-        """kernel 0: row per thread / warp per row; 1: bit-sliced 32-row tiles (default)."""
+        """kernel 0: row per thread / warp per row; 1: bit-sliced 32-row tiles (default).  use_hash bit 0: hash
+        index lookups; bit 1: FP64 instead of double-float accumulation of FP32 batched applies."""
         call("qsi_op_set_kernel", self._h, int(kernel), int(use_hash), int(list_cap))
 
     def info(self) -> dict:
@@ -385,7 +431,17 @@ class LazyOpSum:
 
     def evaluate_static(self, x, y, accumulate: bool = False) -> None:
         """y (+)= H x for host numpy vectors without any device allocation (bases of at most
-        262,144 states; see qsi_op_apply_static)."""
+        262,144 states; see qsi_op_apply_static).  x and y must be C-contiguous float64 numpy arrays of
+        shape (rows(),): the library copies rows() doubles in and out through raw host pointers."""
+        n = self.rows()
+        for name, a in (("x", x), ("y", y)):
+            if not isinstance(a, np.ndarray):
+                raise ValueError(f"evaluate_static: {name} must be a host numpy array, not {type(a).__name__}")
+            if a.dtype != np.float64 or a.shape != (n,) or not a.flags.c_contiguous:
+                raise ValueError(f"evaluate_static: {name} must be a C-contiguous float64 array of shape ({n},), "
+                                 f"got {a.dtype} {a.shape}{'' if a.flags.c_contiguous else ' (strided)'}")
+        if not y.flags.writeable:
+            raise ValueError("evaluate_static: y is read-only")
         call("qsi_op_apply_static", self._h, ptr(x), ptr(y), int(accumulate))
 
     def __matmul__(self, x):

@@ -177,8 +177,8 @@ __device__ __forceinline__ double term_coeff(const PullTerm& T, const state2 s) 
 }
 
 template <typename XT, typename YT, class LK>
-__global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, const XT* __restrict__ x,
-                                                    YT* __restrict__ y, int accumulate) {
+__global__ void __launch_bounds__(256, LK::kMinBlocks) k_apply_tile(TileParams P, LK lk, const XT* __restrict__ x,
+                                                                 YT* __restrict__ y, int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TileSmem S = stage_terms(P, smem_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256, 3) k_apply_tile(TileParams P, LK lk, cons
         while (true) {
             // up to kNB admitted terms at a time (across rounds): lookups and gathers in flight together,
             // contributions added in term order
-            constexpr int kNB = 4;
+            constexpr int kNB = LK::kNB;
             int tt[kNB];
             uint64_t tl[kNB], th[kNB];
             int64_t J[kNB];
@@ -864,6 +864,15 @@ qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int acc
 }
 
 size_t sector_launch_bytes() { return sizeof(SectorLaunch); }
+
+qsi_status preload_apply_f64_rows();  // operator.cu: the row-per-thread kernel
+
+qsi_status preload_apply_f64() {
+    cudaFuncAttributes a;
+    QSI_CUDA(cudaFuncGetAttributes(&a, k_apply_tile<double, double, LookupHash>));
+    QSI_CUDA(cudaFuncGetAttributes(&a, k_apply_tile<double, double, LookupTable>));
+    return preload_apply_f64_rows();
+}
 
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
                               cudaStream_t st) {

@@ -158,7 +158,7 @@ extern "C" qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_
             for (int d = -4; d <= 4; d += 2) {
                 const int bits = b0 + d;
                 if ((flags & QSI_TUNE_INDEX) || d == 0)
-                    if (bits >= 8 && bits <= std::min(30, b->hb + 1)) codes.push_back(bits);
+                    if (bits >= 8 && bits <= std::min(31, b->hb + 1)) codes.push_back(bits);
             }
             s = T.sweep("index(0=hash,k=table bits)", codes, best_code, best, [&](int code) -> qsi_status {
                 if (code == 0) {

@@ -1,4 +1,4 @@
-// Spin-ice basis enumeration on the GPU (bases without spinon pairs).
+// Spin-ice basis enumeration on the GPU, with or without spinon pairs.
 //
 // The host walks the search tree (same visiting order and admission tests as
 // enumerate.cpp's fast search) down to a prefix depth with enough subtree
@@ -11,6 +11,17 @@
 // Leaves are mapped back to the original spin numbering with byte tables and
 // sorted as 128-bit keys by two stable LSD radix sorts (low word, then high
 // word) with CUB's device radix sort.
+//
+// Bases with spinon pairs follow the reference's forking rule
+// (components/build_basis/src/pyro_tree.cpp:168-189): a value that fails the
+// admission test is still taken while pairs are left, spending one.  The set
+// then depends on exactly which values the test rejects, so that walk uses the
+// reference's own test (pyro_tree.cpp:87-162: every sublattice checked against
+// all N - i unknown spins) rather than the tighter per-sublattice capacity
+// test of the pair-free walk.  The walk keeps no per-level record of pairs
+// spent: coming back to a level, it re-evaluates the test for the value that
+// level took (the state below the level is unchanged), which says whether a
+// pair was spent there.
 #include <algorithm>
 #include <array>
 #include <cstring>
@@ -46,6 +57,7 @@ struct EnumProblem {
     int n_tets;
     int has_sector;
     int d0;
+    int n_pairs;  // spinon pairs allowed (0: the pair-free walk)
 };
 
 // Mask form of one search step for the device walk: the (permuted-space)
@@ -54,13 +66,16 @@ struct EnumProblem {
 struct MaskStep {
     uint64_t tm[4][2];   // tetrahedron masks
     uint64_t sm[2];      // sublattice mask (spins of this step's sublattice)
-    int8_t n_tet, target, rem, pad;
+    int8_t n_tet, target, rem, sl;  // sl: this step's sublattice
     int8_t unk[4], tmin[4], tmax[4];
 };
 
 struct MaskProblem {
     MaskStep step[kMaxSpins];
-    int N, has_sector, d0, pad;
+    int N, has_sector, d0, n_pairs;
+    int n_sl, pad2;
+    uint64_t slm[8][2];  // sublattice masks (permuted space) and targets, for the spinon-pair walk's sector test
+    int8_t target[8];
 };
 
 __device__ __forceinline__ int popc2(uint64_t a0, uint64_t a1, const uint64_t* m) {
@@ -77,6 +92,106 @@ __device__ __forceinline__ bool admit_step(const MaskProblem& P, const MaskStep&
         if (c > st.target || c + st.rem < st.target) return false;
     }
     return true;
+}
+
+// The reference's admission test of value v for the spin at step i (spinon-pair walk).
+__device__ __forceinline__ bool admit_ref(const MaskProblem& P, const MaskStep& st, int v, uint64_t s0, uint64_t s1,
+                                          int i, int sl_i) {
+    for (int k = 0; k < st.n_tet; ++k) {
+        const int q = popc2(s0, s1, st.tm[k]) + v;
+        if (q > st.tmax[k] || q + st.unk[k] < st.tmin[k]) return false;
+    }
+    if (P.has_sector)
+        for (int a = 0; a < P.n_sl; ++a) {
+            const int c = popc2(s0, s1, P.slm[a]) + (a == sl_i ? v : 0);
+            if (c + (P.N - i) < P.target[a] || c > P.target[a]) return false;
+        }
+    return true;
+}
+
+// Walk of one subtree with spinon pairs (see the file comment): pass 0 counts leaves, pass 1 writes them.
+__global__ void __launch_bounds__(128) k_enum_pairs(const MaskProblem* __restrict__ gP, const state2* __restrict__ roots,
+                                                    const int8_t* __restrict__ root_pairs, int64_t n_roots,
+                                                    unsigned long long* __restrict__ counts,
+                                                    const unsigned long long* __restrict__ offsets,
+                                                    state2* __restrict__ out, unsigned long long* cursor) {
+    __shared__ MaskProblem P;
+    for (int k = threadIdx.x; k < (int)(sizeof(MaskProblem) / 8); k += blockDim.x)
+        reinterpret_cast<uint64_t*>(&P)[k] = reinterpret_cast<const uint64_t*>(gP)[k];
+    __syncthreads();
+    for (;;) {
+        const unsigned long long r = atomicAdd(cursor, 1ULL);
+        if (r >= (unsigned long long)n_roots) break;
+        const state2 root = roots[r];
+        uint64_t s0 = root.x, s1 = root.y;
+        int pairs = root_pairs[r];
+        unsigned long long found = 0, steps = 0;
+        const unsigned long long w = offsets ? offsets[r] : 0;
+        int i = P.d0;
+        bool down = true;
+        auto set_bit = [&](int b) {
+            if (b < 64) s0 |= 1ULL << b;
+            else s1 |= 1ULL << (b - 64);
+        };
+        for (;;) {
+            if (++steps > (1ULL << 38)) {
+                atomicOr(cursor + 1, 1ULL);
+                break;
+            }
+            if (down) {
+                if (i == P.N) {
+                    if (out) out[w + found] = make_ulonglong2(s0, s1);
+                    ++found;
+                    down = false;
+                    --i;
+                    if (i < P.d0) break;
+                    continue;
+                }
+                const MaskStep& st = P.step[i];
+                const bool a0 = admit_ref(P, st, 0, s0, s1, i, st.sl);
+                if (a0 || pairs < P.n_pairs) {  // value 0 (bit stays clear)
+                    pairs += !a0;
+                    ++i;
+                    continue;
+                }
+                const bool a1 = admit_ref(P, st, 1, s0, s1, i, st.sl);
+                if (a1 || pairs < P.n_pairs) {
+                    pairs += !a1;
+                    set_bit(i);
+                    ++i;
+                    continue;
+                }
+                down = false;
+                --i;
+                if (i < P.d0) break;
+                continue;
+            }
+            // returning to level i: its bit tells which value was taken; the test for that value says whether
+            // it spent a pair
+            const MaskStep& st = P.step[i];
+            const bool set = (i < 64) ? ((s0 >> i) & 1) : ((s1 >> (i - 64)) & 1);
+            if (set) {
+                if (i < 64) s0 &= ~(1ULL << i);
+                else s1 &= ~(1ULL << (i - 64));
+                pairs -= !admit_ref(P, st, 1, s0, s1, i, st.sl);
+                --i;
+                if (i < P.d0) break;
+                continue;
+            }
+            pairs -= !admit_ref(P, st, 0, s0, s1, i, st.sl);
+            const bool a1 = admit_ref(P, st, 1, s0, s1, i, st.sl);
+            if (a1 || pairs < P.n_pairs) {
+                pairs += !a1;
+                set_bit(i);
+                ++i;
+                down = true;
+                continue;
+            }
+            --i;
+            if (i < P.d0) break;
+        }
+        if (counts) counts[r] = found;
+    }
 }
 
 // Register-only walk of one subtree: descending tries 0 then 1 at each level;
@@ -230,6 +345,40 @@ void host_prefixes(const EnumProblem& P, int d, int i, u128 state, std::vector<i
     }
 }
 
+// Host walk to depth d with spinon pairs (the reference's test and forking rule), collecting (prefix, pairs spent).
+void host_prefixes_pairs(const EnumProblem& P, const std::vector<u128>& slm, int d, int i, u128 state, int pairs,
+                         std::vector<int>& Q, std::vector<int>& cnt, std::vector<u128>& out, std::vector<int8_t>& outp) {
+    if (i == d) {
+        out.push_back(state);
+        outp.push_back((int8_t)pairs);
+        return;
+    }
+    const EnumStep& st = P.step[i];
+    for (int v = 0; v < 2; ++v) {
+        bool ok = true;
+        for (int k = 0; k < st.n_tet; ++k) {
+            int q = Q[st.tet[k]] + v;
+            if (q > st.tmax[k] || q + st.unk[k] < st.tmin[k]) ok = false;
+        }
+        if (P.has_sector)
+            for (size_t a = 0; a < slm.size(); ++a) {
+                int c = cnt[a] + ((int)a == st.sl ? v : 0);
+                if (c + (P.N - i) < P.target[a] || c > P.target[a]) ok = false;
+            }
+        if (!ok && pairs >= P.n_pairs) continue;
+        if (v) {
+            for (int k = 0; k < st.n_tet; ++k) Q[st.tet[k]]++;
+            cnt[st.sl]++;
+        }
+        host_prefixes_pairs(P, slm, d, i + 1, v ? (state | ((u128)1 << i)) : state, pairs + (ok ? 0 : 1), Q, cnt, out,
+                            outp);
+        if (v) {
+            for (int k = 0; k < st.n_tet; ++k) Q[st.tet[k]]--;
+            cnt[st.sl]--;
+        }
+    }
+}
+
 template <typename T>
 struct DBuf {
     T* p = nullptr;
@@ -244,10 +393,11 @@ using namespace qsi;
 
 extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* tetra_spins, int32_t n_tetra,
                                               int32_t tetra_size, const int32_t* sublattice, int32_t n_sublattices,
-                                              const int32_t* sector, uint64_t** out_lohi, int64_t* n_out) {
+                                              const int32_t* sector, int32_t n_spinon_pairs, uint64_t** out_lohi,
+                                              int64_t* n_out) {
     return guarded([&]() -> qsi_status {
         if (n_spins <= 0 || n_spins > kMaxSpins || !tetra_spins || n_tetra <= 0 || n_tetra > kMaxTets ||
-            tetra_size <= 0 || tetra_size > 127 || !out_lohi || !n_out)
+            tetra_size <= 0 || tetra_size > 127 || !out_lohi || !n_out || n_spinon_pairs < 0 || n_spinon_pairs > 64)
             return fail(QSI_INVALID_ARG, "qsi_enumerate_basis_gpu: bad argument");
         if (sector && (!sublattice || n_sublattices <= 0 || n_sublattices > 8))
             return fail(QSI_INVALID_ARG, "qsi_enumerate_basis_gpu: sector needs 1..8 sublattices");
@@ -271,6 +421,7 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
         P.N = N;
         P.n_tets = n_tetra;
         P.has_sector = sector != nullptr;
+        P.n_pairs = n_spinon_pairs;
         for (int i = 0; i < N; ++i) {
             EnumStep& st = P.step[i];
             const int s = order[i];
@@ -292,13 +443,21 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
         }
         if (sector)
             for (int a = 0; a < n_sublattices; ++a) P.target[a] = (int8_t)sector[a];
+        // sublattice masks in the permuted space (the spinon-pair walk tests every sublattice)
+        const int n_sl = sector ? n_sublattices : 0;
+        std::vector<u128> slm(n_sl, 0);
+        for (int j = 0; j < N; ++j)
+            if (sector) slm[sublattice[order[j]]] |= (u128)1 << j;
         // prefix depth: deepen until there are enough roots to fill the GPU
         std::vector<u128> roots;
+        std::vector<int8_t> root_pairs;
         int d0 = std::min(N, 16);
         for (;;) {
             roots.clear();
+            root_pairs.clear();
             std::vector<int> Q(n_tetra, 0), cnt(8, 0);
-            host_prefixes(P, d0, 0, 0, Q, cnt, roots);
+            if (n_spinon_pairs) host_prefixes_pairs(P, slm, d0, 0, 0, 0, Q, cnt, roots, root_pairs);
+            else host_prefixes(P, d0, 0, 0, Q, cnt, roots);
             if (roots.size() >= 2000000 || d0 >= N || d0 >= N - 8) break;
             d0 = std::min(N, d0 + 4);
         }
@@ -308,6 +467,13 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
         M.N = N;
         M.has_sector = sector != nullptr;
         M.d0 = d0;
+        M.n_pairs = n_spinon_pairs;
+        M.n_sl = n_sl;
+        for (int a = 0; a < n_sl; ++a) {
+            M.slm[a][0] = lo64(slm[a]);
+            M.slm[a][1] = hi64(slm[a]);
+            M.target[a] = (int8_t)sector[a];
+        }
         for (int i = 0; i < N; ++i) {
             const int s = order[i];
             MaskStep& ms = M.step[i];
@@ -328,15 +494,21 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
             ms.sm[1] = hi64(sm);
             ms.target = sector ? (int8_t)sector[P.step[i].sl] : 0;
             ms.rem = P.step[i].rem;
+            ms.sl = P.step[i].sl;
         }
         const int64_t n_roots = (int64_t)roots.size();
         std::vector<state2> hroots(n_roots);
         for (int64_t k = 0; k < n_roots; ++k) hroots[k] = make_ulonglong2(lo64(roots[k]), hi64(roots[k]));
         DBuf<MaskProblem> dP;
         DBuf<state2> dRoots;
+        DBuf<int8_t> dRootPairs;
         DBuf<unsigned long long> dCounts, dOffs, dCur;
         QSI_CUDA(dP.alloc(1));
         QSI_CUDA(dRoots.alloc(n_roots));
+        if (n_spinon_pairs) {
+            QSI_CUDA(dRootPairs.alloc(n_roots));
+            QSI_CUDA(cudaMemcpy(dRootPairs.p, root_pairs.data(), (size_t)n_roots, cudaMemcpyHostToDevice));
+        }
         QSI_CUDA(dCounts.alloc(n_roots));
         QSI_CUDA(dOffs.alloc(n_roots + 1));
         QSI_CUDA(dCur.alloc(2));
@@ -346,8 +518,14 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int grid = sms * 16;
+        auto walk = [&](unsigned long long* counts, const unsigned long long* offs, state2* leaves) {
+            if (n_spinon_pairs)
+                k_enum_pairs<<<grid, 128>>>(dP.p, dRoots.p, dRootPairs.p, n_roots, counts, offs, leaves, dCur.p);
+            else
+                k_enum_mask<<<grid, 128>>>(dP.p, dRoots.p, n_roots, counts, offs, leaves, dCur.p);
+        };
         QSI_CUDA(cudaMemset(dCur.p, 0, 16));
-        k_enum_mask<<<grid, 128>>>(dP.p, dRoots.p, n_roots, dCounts.p, nullptr, nullptr, dCur.p);
+        walk(dCounts.p, nullptr, nullptr);
         QSI_CUDA(cudaGetLastError());
         unsigned long long flags[2] = {0, 0};
         QSI_CUDA(cudaMemcpy(flags, dCur.p, 16, cudaMemcpyDeviceToHost));
@@ -366,7 +544,7 @@ extern "C" qsi_status qsi_enumerate_basis_gpu(int32_t n_spins, const int32_t* te
         DBuf<state2> dLeaves;
         QSI_CUDA(dLeaves.alloc(total));
         QSI_CUDA(cudaMemset(dCur.p, 0, 16));
-        k_enum_mask<<<grid, 128>>>(dP.p, dRoots.p, n_roots, nullptr, dOffs.p, dLeaves.p, dCur.p);
+        walk(nullptr, dOffs.p, dLeaves.p);
         QSI_CUDA(cudaGetLastError());
         // byte tables and un-permutation into separate key arrays
         const int nbytes = (N + 7) / 8;

@@ -41,6 +41,22 @@ __global__ void k_fill_buckets(BasisView B, uint32_t* bstart) {
     }
 }
 
+__global__ void k_fill_u32(uint32_t* p, int64_t n, uint32_t v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// Entries of a bucket table of nb buckets: bstart[0 .. nb] rounded up to whole groups of four, plus one group, so
+// that bucket_bounds' 16-byte reads stay inside the allocation.
+size_t bucket_table_entries(uint32_t nb) { return ((size_t)nb + 1 + 3) / 4 * 4 + 4; }
+
+qsi_status build_buckets(qsi_basis* b) {
+    k_fill_buckets<<<grid_for(b->n + 1, 256), 256>>>(b->view(), b->d_bstart);
+    const int64_t pad = (int64_t)bucket_table_entries(b->n_buckets) - ((int64_t)b->n_buckets + 1);
+    k_fill_u32<<<1, 32>>>(b->d_bstart + b->n_buckets + 1, pad, (uint32_t)b->n);
+    QSI_CUDA(cudaGetLastError());
+    return QSI_OK;
+}
+
 __global__ void k_search(BasisView B, const state2* q, int64_t n, int64_t* idx) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     for (; i < n; i += (int64_t)gridDim.x * blockDim.x) idx[i] = basis_find(B, q[i].x, q[i].y);
@@ -323,13 +339,13 @@ extern "C" qsi_status qsi_basis_create(const uint64_t* lohi, int64_t n, int32_t 
             while ((1LL << lg) < n) ++lg;
             bits = std::min(28, std::max(8, lg + 2));
         }
-        bits = std::min(bits, std::min(30, hb + 1));
+        bits = std::min(bits, std::min(31, hb + 1));
         b->bits = bits;
         b->hb = hb;
         b->shift = hb + 1 - bits;
         b->n_buckets = 1u << bits;
         cudaError_t e = cudaMalloc(&b->d_states, (size_t)n * sizeof(state2));
-        if (e == cudaSuccess) e = cudaMalloc(&b->d_bstart, ((size_t)b->n_buckets + 1) * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_bstart, bucket_table_entries(b->n_buckets) * sizeof(uint32_t));
         if (e != cudaSuccess) {
             qsi_basis_destroy(b);
             return fail(e == cudaErrorMemoryAllocation ? QSI_OOM : QSI_CUDA_ERROR, "qsi_basis_create: %s", cudaGetErrorString(e));
@@ -344,9 +360,9 @@ extern "C" qsi_status qsi_basis_create(const uint64_t* lohi, int64_t n, int32_t 
         if (cudaMemcpy(b->d_states, lohi, (size_t)n * 16, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMalloc(&d_bad, sizeof(int)) != cudaSuccess || cudaMemset(d_bad, 0, sizeof(int)) != cudaSuccess)
             return cleanup(fail(QSI_CUDA_ERROR, "qsi_basis_create: copy failed"));
-        BasisView V = b->view();
         k_check_sorted<<<grid_for(n, 256), 256, 0, st>>>(b->d_states, n, d_bad);
-        k_fill_buckets<<<grid_for(n + 1, 256), 256, 0, st>>>(V, b->d_bstart);
+        const qsi_status bs = build_buckets(b);
+        if (bs != QSI_OK) return cleanup(bs);
         int bad = 0;
         if (cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
             return cleanup(fail(QSI_CUDA_ERROR, "qsi_basis_create: %s", cudaGetErrorString(cudaGetLastError())));
@@ -561,6 +577,11 @@ extern "C" qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t
             qsi_op_destroy(op);
             return ds;
         }
+        cudaGetDevice(&op->device);
+        // Device memory that qsi_op_apply_static relies on is reserved here, while allocation is allowed: its
+        // staging arrays and the code of the kernels it launches (both are loaded lazily otherwise, at first use).
+        // A failure leaves that entry point unavailable on this device and the operator usable.
+        if (preload_apply_f64() != QSI_OK || static_stage_prepare() != QSI_OK) cudaGetLastError();
         *out = op;
         return QSI_OK;
     });
@@ -586,6 +607,12 @@ extern "C" qsi_status qsi_op_destroy(qsi_op* op) {
 }
 
 namespace qsi {
+
+qsi_status preload_apply_f64_rows() {
+    cudaFuncAttributes a;
+    QSI_CUDA(cudaFuncGetAttributes(&a, k_apply_rowthread<double, double>));
+    return QSI_OK;
+}
 
 // Enqueues y (+)= H x on `st` for device pointers.
 qsi_status launch_apply(qsi_op* op, const void* x, void* y, int R, int dtype, int accumulate, cudaStream_t st) {
@@ -769,15 +796,16 @@ extern "C" qsi_status qsi_basis_index(qsi_basis* b, int32_t use_hash, int32_t bu
     return guarded([&]() -> qsi_status {
         if (!b) return fail(QSI_INVALID_ARG, "qsi_basis_index: null basis");
         if (bucket_bits > 0 && bucket_bits != b->bits) {
-            int bits = std::min<int>(bucket_bits, std::min(30, b->hb + 1));
+            int bits = std::min<int>(bucket_bits, std::min(31, b->hb + 1));
             uint32_t* nb = nullptr;
-            QSI_CUDA(cudaMalloc(&nb, ((size_t)(1u << bits) + 1) * sizeof(uint32_t)));
+            QSI_CUDA(cudaMalloc(&nb, bucket_table_entries(1u << bits) * sizeof(uint32_t)));
             cudaFree(b->d_bstart);
             b->d_bstart = nb;
             b->bits = bits;
             b->shift = b->hb + 1 - bits;
             b->n_buckets = 1u << bits;
-            k_fill_buckets<<<grid_for(b->n + 1, 256), 256>>>(b->view(), b->d_bstart);
+            qsi_status bs = build_buckets(b);
+            if (bs != QSI_OK) return bs;
             QSI_CUDA(cudaDeviceSynchronize());
         }
         if (use_hash && !b->d_hash) return build_hash(b);
@@ -794,7 +822,8 @@ extern "C" qsi_status qsi_basis_info(const qsi_basis* b, int32_t* bucket_bits, i
     if (bucket_bits) *bucket_bits = b->bits;
     if (has_hash) *has_hash = b->d_hash != nullptr;
     if (index_bytes)
-        *index_bytes = (int64_t)(((size_t)b->n_buckets + 1) * 4 + (b->d_hash ? (b->hash_mask + 1) * sizeof(HashSlot) : 0));
+        *index_bytes = (int64_t)(bucket_table_entries(b->n_buckets) * 4 +
+                                 (b->d_hash ? (b->hash_mask + 1) * sizeof(HashSlot) : 0));
     return QSI_OK;
 }
 

@@ -97,23 +97,44 @@ __device__ __forceinline__ uint64_t bucket_of(const BasisView& B, uint64_t lo, u
     return v;
 }
 
-// Exact index of state (lo, hi) in the basis, or -1.
+// Bounds [a, b) of bucket v: one 16-byte load of the aligned group of four table entries holding bstart[v]
+// (the table is 16-byte aligned and padded to a multiple of four entries plus four), a second load only when v is
+// the last of its group.  The apply kernels are bound by the throughput of their uncoalesced loads, so every load
+// saved per lookup counts.
+__device__ __forceinline__ void bucket_bounds(const BasisView& B, uint64_t v, uint32_t& a, uint32_t& b) {
+    const uint4 q = __ldg(reinterpret_cast<const uint4*>(B.bstart + (v & ~3ULL)));
+    switch ((int)(v & 3)) {
+        case 0: a = q.x, b = q.y; break;
+        case 1: a = q.y, b = q.z; break;
+        case 2: a = q.z, b = q.w; break;
+        default: a = q.w, b = __ldg(B.bstart + v + 1); break;
+    }
+}
+
+// Exact index of state (lo, hi) in the basis, or -1.  Lower-bound bisection over the state's bucket; the state at
+// the final position was loaded by the bisection itself whenever that position lies inside the bucket (the last
+// probe that moved the upper end there), and a search that never moved the upper end ends past the bucket, where
+// the state cannot be: no reload either way.
 __device__ __forceinline__ int64_t basis_find(const BasisView& B, uint64_t lo, uint64_t hi) {
     bool ok;
-    uint64_t v = bucket_of(B, lo, hi, ok);
+    const uint64_t v = bucket_of(B, lo, hi, ok);
     if (!ok) return -1;
-    uint32_t a = __ldg(B.bstart + v), b = __ldg(B.bstart + v + 1);
+    uint32_t a, b;
+    bucket_bounds(B, v, a, b);
+    state2 e = make_ulonglong2(0, 0);
+    bool seen = false;  // e holds states[b]
     while (a < b) {
-        uint32_t m = (a + b) >> 1;
-        state2 e = __ldg(B.states + m);
-        if (less128(e.x, e.y, lo, hi)) a = m + 1;
-        else b = m;
+        const uint32_t m = (a + b) >> 1;
+        const state2 t = __ldg(B.states + m);
+        if (less128(t.x, t.y, lo, hi)) {
+            a = m + 1;
+        } else {
+            b = m;
+            e = t;
+            seen = true;
+        }
     }
-    if (a < (uint32_t)B.n) {
-        state2 e = __ldg(B.states + a);
-        if (e.x == lo && e.y == hi) return (int64_t)a;
-    }
-    return -1;
+    return (seen && e.x == lo && e.y == hi) ? (int64_t)a : -1;
 }
 
 // Exact position of (lo, hi) through the hash index, or -1.  The probe count
@@ -135,6 +156,7 @@ __device__ __forceinline__ int64_t hash_find(const HashView& Hv, uint64_t lo, ui
 // further probes, needed after a collision, follow one by one.
 struct LookupTable {
     BasisView B;
+    static constexpr int kNB = 4, kMinBlocks = 3;  // lookups per batch per lane, resident 256-thread blocks
     __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return basis_find(B, lo, hi); }
     template <int NB>
     __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n) const {
@@ -146,6 +168,7 @@ struct LookupTable {
 
 struct LookupHash {
     HashView H;
+    static constexpr int kNB = 4, kMinBlocks = 3;
     __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return hash_find(H, lo, hi); }
     template <int NB>
     __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n) const {

@@ -48,6 +48,7 @@ struct qsi_op {
     double* d_diag = nullptr;       // per-row diagonal (tile kernels)
     float2* d_diag_ff = nullptr;    // the same as double-float pairs (FP32 batched kernel)
     cudaStream_t stream = nullptr;
+    int device = 0;        // the device current at qsi_op_create (owner of every buffer and of the stream)
     void* d_x = nullptr;   // staging for host-pointer applies
     void* d_y = nullptr;
     size_t staging_bytes = 0;
@@ -61,6 +62,13 @@ qsi_status launch_apply_to_f64(qsi_op* op, const void* x, double* y, int xdtype,
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
                               cudaStream_t st);
 qsi_status build_hash(qsi_basis* b);
+// Bucket table of a basis at its current width (b->bits, b->shift, b->n_buckets), allocated with padding for the
+// 16-byte reads of bucket_bounds.
+qsi_status build_buckets(qsi_basis* b);
+// Loads the single-vector FP64 apply kernels on the current device (CUDA loads device code lazily, on first use).
+qsi_status preload_apply_f64();
+// Looks the static staging arrays of qsi_op_apply_static up on the current device (once per device).
+qsi_status static_stage_prepare();
 qsi_status build_diag(qsi_op* op);
 struct SectorPlan {
     std::vector<unsigned char> records;  // one launch record per sector, to be copied to device memory

@@ -189,6 +189,16 @@ def test_kernel_variants_bit_identical(built, name):
         Y = np.zeros_like(X)
         op.apply_batched(X, Y)
         bouts.append(Y)
+    # narrow and wide bucket tables (buckets of thousands of states, and bucket numbers in every position of the
+    # table's groups of four)
+    bits0 = b.index_info()["bucket_bits"]
+    for bits in (8, 12, 31):
+        b.set_index(use_hash=True, bucket_bits=bits)
+        op.set_kernel(1, 0)
+        y = np.zeros_like(x)
+        op.evaluate(x, y)
+        outs.append(y)
+    b.set_index(use_hash=True, bucket_bits=bits0)
     op.set_kernel(1, 1)
     for y in outs[1:]:
         assert np.array_equal(y, outs[0])
@@ -373,6 +383,11 @@ def test_states_up_to_128_bits():
     op.evaluate(x, y)
     ref = O.apply_port(lohi, specs, x, threads=1)
     np.testing.assert_allclose(y, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    for bits in (12, 31):  # other table widths, bitwise the same
+        b.set_index(use_hash=False, bucket_bits=bits)
+        y2 = np.zeros_like(x)
+        op.evaluate(x, y2)
+        assert np.array_equal(y2, y)
     X = np.random.default_rng(9).standard_normal((len(lohi), 64)).astype(np.float32)
     for vw in (4, 8, 16):
         op.set_tuning(0, 0, which=1, vec_width=vw)

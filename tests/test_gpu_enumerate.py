@@ -22,3 +22,17 @@ def test_gpu_enumeration_matches_reference_bases(name):
 def test_gpu_enumeration_matches_host(lat, sector):
     L = workloads.lattice(lat)
     assert np.array_equal(q.enumerate_basis_gpu(L, sector=sector), q.enumerate_basis(L, sector=sector))
+
+
+@pytest.mark.parametrize("lat,pairs,sector", [("pyro_1x2x1", 1, None), ("pyro_1x2x1", 2, None),
+                                              ("pyro_1x2x1", 1, [4, 4, 4, 4]), ("pyro_1x2x1", 2, [4, 4, 4, 4]),
+                                              ("pyro_1x2x2", 1, None)])
+def test_gpu_enumeration_with_spinon_pairs(lat, pairs, sector):
+    """Spinon-pair bases (the forking rule of the reference's enumerator) from the GPU walk equal the host
+    enumerator's and the oracle's restatement of the reference's."""
+    from oracle import oracle as O
+
+    L = workloads.lattice(lat)
+    b = q.enumerate_basis_gpu(L, sector=sector, n_spinon_pairs=pairs)
+    assert np.array_equal(b, q.enumerate_basis(L, sector=sector, n_spinon_pairs=pairs))
+    assert np.array_equal(b, O.enumerate_basis_oracle(L.data, sector, pairs))

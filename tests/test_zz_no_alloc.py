@@ -3,7 +3,8 @@
 It exists for callers whose process cannot make new device allocations, e.g.
 when another allocator already owns the GPU's memory.  It must give the same
 result as the ordinary host-pointer apply, call after call, since every call
-reuses the same fixed staging arrays.  This file is collected last on purpose.
+reuses the same fixed staging arrays, and a call must leave the device's free
+memory unchanged.  This file is collected last on purpose.
 """
 import numpy as np
 import pytest
@@ -17,6 +18,25 @@ pytestmark = pytest.mark.gpu
 def _op():
     w = workloads.q0_32spin()
     return q.LazyOpSum(q.ZBasis(w.basis_lohi), w.hamiltonian())
+
+
+def test_static_apply_reserves_no_device_memory():
+    """A fresh operator (no ordinary apply before, so no staging buffers of its own): the first static calls and
+    the ones after them leave the device's free memory unchanged."""
+    import torch
+
+    torch.cuda.init()
+    op = _op()
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(op.rows())
+    y = np.zeros_like(x)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        op.evaluate_static(x, y)
+        op.evaluate_static(x, y, accumulate=True)
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"static applies changed free device memory by {free0 - free1} bytes"
 
 
 def test_static_apply_matches_ordinary_apply_twice():
@@ -40,6 +60,17 @@ def test_static_apply_matches_ordinary_apply_twice():
     op.evaluate_add(x, y_ref)
     op.evaluate_static(x, y, accumulate=True)
     np.testing.assert_allclose(y, y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+
+
+def test_static_apply_checks_its_arguments():
+    op = _op()
+    n = op.rows()
+    good = np.zeros(n)
+    for bad in (np.zeros(n, np.float32), np.zeros(n + 1), np.zeros(2 * n)[::2], [0.0] * n):
+        with pytest.raises(ValueError):
+            op.evaluate_static(bad, good)
+        with pytest.raises(ValueError):
+            op.evaluate_static(good, bad)
 
 
 def test_static_apply_rejects_bases_above_the_limit():

@@ -48,10 +48,13 @@ def parse():
     p.add_argument("--no-tune", action="store_true", help="skip the launch autotuner (built-in settings)")
     p.add_argument("--ftlm-steps", type=int, default=30, help="Lanczos steps of the timed FTLM runs")
     p.add_argument("--seed", type=int, default=3)
-    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
+    p.add_argument("--ref-step-seconds", type=float, default=2.5,
+                   help="target length of one reference-arm step (a sample of whole source rows)")
     p.add_argument("--no-extras", action="store_true", help="skip batched / FTLM / e2e / CPU legs")
-    p.add_argument("--legs", default="batched,ftlm,e2e,cpu",
-                   help="extra legs after the FP64 headline (also: lanczos = FP64 vs mixed 10-eigenvalue solves)")
+    p.add_argument("--legs", default="e2e,batched,ftlm,lanczos,ftlm_sectors,cpu",
+                   help="extra legs after the FP64 headline: e2e, batched, ftlm, lanczos (FP64 vs mixed 10-eigenvalue "
+                        "solves), ftlm_sectors (multi-sector FTLM), serve (request loop), cpu (whole oracle apply: "
+                        "CPU baseline and parity)")
     p.add_argument("--nev", type=int, default=10)
     p.add_argument("--serve-n", type=int, default=240)
     p.add_argument("--ftlm-R", type=int, default=0,
@@ -143,28 +146,45 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(args, gpu: bool = False):
-    """The workload's basis is enumerated on the GPU for our arm and on the host for the reference arm."""
+def workload_spec(args):
+    """The workload both arms run, derived from the command line alone (no engine call): lattice file, sector
+    (None: the full Q=0 basis), ring couplings g ~ U[0.2, 1]^4 and field B ~ U[-0.5, 0.5]^3 from
+    numpy default_rng(seed) (the draws of workloads.ring_zeeman_params)."""
+    import numpy as np
+
+    lat = json.load(open(ROOT / "qsi_subspace_ed_gb300" / "lattices" / f"{args.lattice}.json"))
+    rng = np.random.default_rng(args.seed)
+    g = [float(v) for v in rng.uniform(0.2, 1.0, 4)]
+    B = [float(v) for v in rng.uniform(-0.5, 0.5, 3)]
+    n_sl = max(int(a["sl"]) for a in lat["atoms"]) + 1
+    if args.full_basis:
+        sector, name = None, f"{args.lattice}.Q0"
+    else:
+        if args.sector:
+            sector = [int(v) for v in args.sector.split(",")]
+        else:  # equal sublattice polarisation (the zero-winding sector): N/8 up spins per sublattice
+            sector = [len(lat["atoms"]) // n_sl // 2] * n_sl
+        name = f"{args.lattice}.s{'.'.join(map(str, sector))}"
+    return {"name": name, "lattice": lat, "sector": sector, "g": g, "B": B}
+
+
+def workload_config(spec, n: int, n_terms: int) -> dict:
+    """`config` of the JSON line, the same in both arms."""
+    return {"workload": spec["name"], "n_states": int(n), "n_terms": int(n_terms), "vectors_per_apply": 1,
+            "l2": "inputs larger than L2" if n * 24 > 2 * 129 * 2**20 else "L2 flushed between steps"}
+
+
+def make_workload(args):
+    """Our arm: the workload's basis enumerated on the GPU and its Hamiltonian built by the engine."""
+    import qsi_subspace_ed_gb300 as q
     from qsi_subspace_ed_gb300 import workloads
 
-    t0 = time.time()
+    spec = workload_spec(args)
     lat = workloads.lattice(args.lattice)
-    if args.full_basis:
-        import qsi_subspace_ed_gb300 as q
-
-        g, B = workloads.ring_zeeman_params(args.seed, (0.2, 1.0), 0.5)
-        w = workloads.Workload(f"{args.lattice}.Q0", lat, q.enumerate_basis_gpu(lat) if gpu else q.enumerate_basis(lat),
-                               g, B)
-    elif args.sector:
-        import qsi_subspace_ed_gb300 as q
-
-        sec = [int(v) for v in args.sector.split(",")]
-        g, B = workloads.ring_zeeman_params(args.seed, (0.2, 1.0), 0.5)
-        enum = q.enumerate_basis_gpu if gpu else q.enumerate_basis
-        w = workloads.Workload(f"{args.lattice}.s{'.'.join(map(str, sec))}", lat, enum(lat, sector=sec), g, B)
-    else:
-        w = workloads.sector_workload(args.lattice, seed=args.seed, gpu=gpu)
-    return w, time.time() - t0
+    t0 = time.time()
+    basis = q.enumerate_basis_gpu(lat, sector=spec["sector"])
+    w = workloads.Workload(spec["name"], lat, basis, spec["g"], spec["B"])
+    return spec, w, time.time() - t0
 
 
 def measured_traffic(workload: str, kernel: str, n: int):
@@ -178,49 +198,40 @@ def measured_traffic(workload: str, kernel: str, n: int):
     return None
 
 
-def cpu_baseline(w, H, seconds: float):
-    """The reference's push loop (oracle restatement) on all host cores, over a bounded row sample, with the
-    lookups of the basis class diag_DOQSI_ham and bench_apply use (ZBasisInterp: high-word bounds, then a
-    bisection on the low word); the bounds are built once per workload, as the reference builds them on load."""
+def oracle_whole_apply(basis_lohi, specs, x):
+    """One whole y = H x by the reference's push loop (oracle restatement: per-term OpenMP pass over all source
+    rows, atomic scatter, ZBasisInterp lookups) on all host cores; returns (y, seconds, threads, lookups)."""
     import numpy as np
 
     from oracle import oracle as O
 
     threads = O.cpu_threads()
-    terms = O.terms_array(H.specs())
-    n = len(w.basis_lohi)
-    ix = getattr(w, "_interp_index", None)
-    if ix is None:
-        try:
-            ix = O.InterpIndex(w.basis_lohi)
-        except MemoryError:
-            ix = False  # no room for the high-word bounds: whole-basis bisection (ZBasisBST) instead
-        w._interp_index = ix
-
-    def run(rows):
-        if ix:
-            return ix.apply_rows(terms, x, y, 0, rows, threads)
-        O.apply_rows_port(w.basis_lohi, terms, x, y, 0, rows, threads)
-        return 0
-
-    x = np.random.default_rng(0).standard_normal(n)
-    y = np.zeros(n)
-    rows = min(n, 20000)
+    terms = O.terms_array(specs)
+    y = np.zeros(len(basis_lohi))
+    try:
+        ix = O.InterpIndex(basis_lohi)
+    except MemoryError:  # no room for the high-word bounds: whole-basis bisection (ZBasisBST)
+        ix = None
     t0 = time.time()
-    unseen = run(rows)
-    dt = time.time() - t0
-    if dt < seconds / 4 and rows < n:
-        rows = int(min(n, rows * max(1.0, seconds / max(dt, 1e-3))))
-        y[:] = 0
-        t0 = time.time()
-        unseen = run(rows)
-        dt = time.time() - t0
-    lookups = "ZBasisInterp lookups" if ix else "ZBasisBST lookups"
-    out = {"value": rows / dt, "unit": "states/s", "cores": threads, "kind": "port",
-           "sample": f"push-form apply (per-term OpenMP pass, atomic scatter, {lookups}) over source "
-                     f"rows [0,{rows}) of {n} of {w.name}; {dt:.1f}s"}
-    if unseen:
-        out["note"] = f"{unseen} lookups hit an unseen high word (the reference throws there)"
+    if ix is not None:
+        ix.apply_rows(terms, x, y, 0, len(basis_lohi), threads)
+    else:
+        O.apply_rows_port(basis_lohi, terms, x, y, 0, len(basis_lohi), threads)
+    return y, time.time() - t0, threads, "ZBasisInterp" if ix is not None else "ZBasisBST"
+
+
+def sample_blocks(n: int, rows: int, step: int, n_blocks: int = 16):
+    """Source-row blocks of one reference-arm step: n_blocks blocks of rows / n_blocks rows, one in each of
+    n_blocks equal slices of the basis, at an offset inside the slice that moves from step to step."""
+    rows = min(n, rows)
+    nb = max(1, min(n_blocks, rows))
+    size = rows // nb
+    slice_ = n // nb
+    out = []
+    for k in range(nb):
+        room = max(0, slice_ - size)
+        off = (step * 7919 * (k + 1)) % (room + 1)
+        out.append((k * slice_ + off, k * slice_ + off + size))
     return out
 
 
@@ -237,8 +248,8 @@ def ftlm_sectors_leg(args):
     g, B = workloads.ring_zeeman_params(args.seed, (0.2, 1.0), 0.5)
     t0 = time.time()
     secs = [("pyro_1x2x2.n0", l64, q.enumerate_basis_gpu(l64)),
-            ("pyro_1x2x2.n1", l64, q.enumerate_basis(l64, n_spinon_pairs=1)),
-            ("pyro_1x2x1.n2", l32, q.enumerate_basis(l32, n_spinon_pairs=2))]
+            ("pyro_1x2x2.n1", l64, q.enumerate_basis_gpu(l64, n_spinon_pairs=1)),
+            ("pyro_1x2x1.n2", l32, q.enumerate_basis_gpu(l32, n_spinon_pairs=2))]
     t_enum = time.time() - t0
     ops = [q.LazyOpSum(q.ZBasis(b), q.build_ring_zeeman(lat, g, B, Jpm=0.05)) for _, lat, b in secs]
     R, M = args.ftlm_R or 64, args.ftlm_M
@@ -298,33 +309,78 @@ def serve_leg(args):
 
 
 def run_reference(args):
+    """The reference's CPU path on this workload: the oracle's restatement of its push loop (per term, an
+    OpenMP loop over source rows scattering y[J] += c x[i] atomically, ZBasisInterp lookups) on all host cores.
+    Its basis comes from the oracle's restatement of the reference's enumerator and its term list from the
+    oracle's Hamiltonian builder, so nothing of the engine is loaded.  Each step is a bounded sample: whole
+    source rows in 16 blocks spread over the basis (sample_blocks), sized to about --ref-step-seconds."""
+    import numpy as np
+
+    from oracle import oracle as O
+
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    try:  # input preparation only: the GPU enumerator builds the same sorted basis faster
-        import torch
+    spec = workload_spec(args)
+    t0 = time.time()
+    basis = O.enumerate_basis_oracle(spec["lattice"], spec["sector"])
+    t_enum = time.time() - t0
+    specs = O.ring_zeeman_specs(spec["lattice"], spec["g"], spec["B"])
+    terms = O.terms_array(specs)
+    n = len(basis)
+    threads = O.cpu_threads()
+    t0 = time.time()
+    try:
+        ix = O.InterpIndex(basis)
+    except MemoryError:
+        ix = None
+    t_index = time.time() - t0
+    x = np.random.default_rng(0).standard_normal(n)
+    y = np.zeros(n)
 
-        gpu = torch.cuda.is_available()
-    except Exception:
-        gpu = False
-    w, setup_s = make_workload(args, gpu=gpu)
-    H = w.hamiltonian()
-    steps = []
-    base = None
-    for _ in range(max(1, args.warmup)):
-        cpu_baseline(w, H, min(args.cpu_seconds, 5.0))
-    for _ in range(args.steps):
-        base = cpu_baseline(w, H, args.cpu_seconds / max(1, args.steps) * 3)
-        steps.append(base["value"])
-    v = statistics.median(steps)
+    def run(blocks):
+        t = time.time()
+        for a, b in blocks:
+            if ix is not None:
+                ix.apply_rows(terms, x, y, a, b, threads)
+            else:
+                O.apply_rows_port(basis, terms, x, y, a, b, threads)
+        return time.time() - t
+
+    # calibrate the sample to about --ref-step-seconds per step
+    probe = min(n, 200_000)
+    dt = run(sample_blocks(n, probe, 0))
+    rows = int(min(n, max(probe, probe * args.ref_step_seconds / max(dt, 1e-3))))
+    for k in range(max(1, args.warmup)):
+        run(sample_blocks(n, rows, k + 1))
+    per = []
+    for k in range(args.steps):
+        blocks = sample_blocks(n, rows, args.warmup + k + 1)
+        per.append((sum(b - a for a, b in blocks), run(blocks)))
+    total_rows = sum(r for r, _ in per)
+    total_s = sum(t for _, t in per)
+    v = total_rows / total_s
+    sample = (f"per step {per[0][0]} source rows ({per[0][0] / n:.1%} of {n}) in 16 blocks spread over the basis, "
+              f"whole rows: per-term OpenMP pass, atomic scatter, "
+              f"{'ZBasisInterp' if ix is not None else 'ZBasisBST'} lookups")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "states/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * len(w.basis_lohi) / v, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / len(per), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ring/Zeeman parameters)",
-            "config": {"workload": w.name, "n_states": int(len(w.basis_lohi)), "n_terms": len(H),
-                       "parallelism": "host OpenMP"},
-            "cpu_baseline": {**base, "value": v},
+            "config": workload_config(spec, n, len(specs)),
+            "setup": {"enumerate_s": round(t_enum, 2), "index_s": round(t_index, 2), "parallelism": "host OpenMP",
+                      "basis": "oracle restatement of the reference's enumerator"},
+            "cpu_baseline": {"value": v, "unit": "states/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def ftlm_step_bytes(n: int, R: int, h: float, blocks: int, s: int = 4) -> float:
+    """Algorithmic bytes of one FTLM step (one sector, R vectors of s bytes, h off-diagonal hits per row): the
+    apply (16 + R s (h + 2) per row, plus the accumulated previous block read in the two-block recurrence), the
+    column dots <C, W> (2 R s), the update P <- W - alpha C - beta P (reads W, C, P and writes P: 4 R s; two
+    blocks: P - alpha C, 3 R s) and the scale P /= beta (2 R s)."""
+    apply_b = 16 + R * s * (h + 2) + (R * s if blocks == 2 else 0)
+    return n * (apply_b + 2 * R * s + (3 if blocks == 2 else 4) * R * s + 2 * R * s)
 
 
 def run_ours(args):
@@ -339,7 +395,7 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    w, setup_s = make_workload(args, gpu=True)
+    spec, w, setup_s = make_workload(args)
     H = w.hamiltonian()
     n = len(w.basis_lohi)
     t0 = time.time()
@@ -350,7 +406,7 @@ def run_ours(args):
     t_op = time.time() - t0
     tuning = {}
     if not args.no_tune:
-        # launch autotuner (single-vector FP64 applies): lookup structure and table width, blocks per SM
+        # launch autotuner (single-vector FP64 applies): lookup structure, table width and mode, blocks per SM
         t0 = time.time()
         log = op.autotune(R=1, dtype="f64", tune_index=True)
         tuning["single"] = {"seconds": round(time.time() - t0, 2), "trials": len(log.splitlines()) - 2,
@@ -359,7 +415,7 @@ def run_ours(args):
     h = hits / n
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)  # the applies below are launched on this stream too
-    x = torch.randn(n, dtype=torch.float64, device=dev)
+    x = torch.randn(n, dtype=torch.float64, device=dev, generator=torch.Generator(dev).manual_seed(1234 + rank))
     y = torch.zeros_like(x)
     l2_flush = torch.empty(256 * 2**20, dtype=torch.uint8, device=dev)
     inputs_exceed_l2 = (n * 16 + n * 8) > 2 * 129 * 2**20
@@ -399,27 +455,35 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     bytes_per_row = 16 + 8 + 8 * h + 8
     achieved = n * bytes_per_row / (ms * 1e-3) / 1e9
-    lookup = "LookupHash" if op.tuning(0)["use_hash"] and basis.index_info()["hash"] else "LookupTable"
-    kname = f"k_apply_tile<double,double,{lookup}>"
+    st0 = op.tuning(0)
+    if st0["use_hash"] and basis.index_info()["hash"]:
+        kname = "k_apply_tile<double,double,LookupHash>"
+    else:
+        kname = {"bisect": "k_apply_tile<double,double,LookupTable>",
+                 "candidates": "k_apply_tile<double,double,LookupTableGather>",
+                 "subkey": "k_apply_tile<double,double,LookupSubkey>"}[st0["table_mode"]]
     traffic = measured_traffic(w.name, kname, n)
+    # the timed steps' input and result, kept on the host for the whole-size parity check against the oracle
+    x_host = x.cpu().numpy() if rank == 0 else None
+    y_host = y.cpu().numpy() if rank == 0 else None
     line = {"metric": METRIC, "value": value, "unit": "states/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ring/Zeeman parameters, N(0,1) vectors)",
-            "config": {"workload": w.name, "n_states": n, "n_terms": len(H), "offdiag_hits_per_row": round(h, 4),
-                       "misses": misses, "parallelism": f"replicas x{ws}",
-                       "l2": "inputs larger than L2" if inputs_exceed_l2 else "L2 flushed between steps",
-                       "setup_s": {"enumerate": round(setup_s, 2), "basis_index": round(t_basis, 2),
-                                   "operator": round(t_op, 2)},
-                       "index": basis.index_info(), "tuning": tuning},
+            "config": workload_config(spec, n, len(H)),
+            "setup": {"parallelism": f"replicas x{ws}", "offdiag_hits_per_row": round(h, 4), "misses": misses,
+                      "seconds": {"enumerate": round(setup_s, 2), "basis_index": round(t_basis, 2),
+                                  "operator": round(t_op, 2)},
+                      "index": basis.index_info(), "tuning": tuning},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "bytes_per_row": bytes_per_row, "kernel": kname},
             "gpu_launches": args.steps, "clocks": clk.summary(t_start, t_end), "wall_s_timed": t_wall}
     legs = set() if args.no_extras else set(args.legs.split(","))
+    col0 = None  # FP32 batched result column fed with x, for the parity check
     if "e2e" in legs and rank == 0:
         # end to end through the C-ABI with pinned host buffers (copies inside the timed region), measured
         # right after the headline, in the same device state
-        xh = torch.randn(n, dtype=torch.float64).pin_memory()
+        xh = torch.from_numpy(x_host).pin_memory()
         yh = torch.zeros(n, dtype=torch.float64).pin_memory()
         lib = q.load()
         lib.qsi_op_apply(op._h, C.c_void_p(xh.data_ptr()), C.c_void_p(yh.data_ptr()), 0, 0, None)
@@ -430,10 +494,13 @@ def run_ours(args):
             assert st == 0, q._lib.last_error()
         te = (time.time() - t0) / ke
         line["e2e"] = {"value": n / te, "unit": "states/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
-                       "api": "qsi_op_apply(host pointers)"}
+                       "api": "qsi_op_apply(host pointers)",
+                       "bitwise_equal_to_device_apply": bool(np.array_equal(yh.numpy(), y_host))}
+        del xh, yh
     if "batched" in legs and rank == 0:
         # batched mixed precision: R FP32 vectors [row][R], double-float row accumulation.  The first R of --R
-        # is reported as `batched_mixed` and runs last, so that its tuned settings stay for the FTLM leg.
+        # is reported as `batched_mixed` and runs last, so that its tuned settings stay for the FTLM leg.  Its
+        # column 0 holds the headline's x (rounded to FP32) for the parity check.
         Rs = [int(v) for v in str(args.R).split(",") if v]
         for R in Rs[1:] + Rs[:1]:
             tkey = "batched" if R == Rs[0] else f"batched_r{R}"
@@ -446,6 +513,7 @@ def run_ours(args):
                 X = Y = None
                 torch.cuda.empty_cache()
                 continue
+            X[:, 0] = x.float()
             if not args.no_tune:
                 t0 = time.time()
                 log = op.autotune(R=R, dtype="f32", X=X, Y=Y, tune_lookup=True)
@@ -463,6 +531,8 @@ def run_ours(args):
                 b_.record(stream)
             torch.cuda.nvtx.range_pop()
             torch.cuda.synchronize()
+            if R == Rs[0]:
+                col0 = Y[:, 0].double().cpu().numpy()
             bms = sum(a_.elapsed_time(b_) for a_, b_ in ev_b) / kb
             bval = n * R / (bms * 1e-3)
             bbytes = n * (16 + R * 4 * (h + 2))
@@ -514,6 +584,11 @@ def run_ours(args):
             mixed = ftlm_rate(R_ftlm, "mixed")
         free_b, total_b = torch.cuda.mem_get_info()
         mixed["vector_blocks"] = 3 if 3 * n * R_ftlm * 4 + (4 << 30) <= free_b else 2
+        step_b = ftlm_step_bytes(n, R_ftlm, h, mixed["vector_blocks"])
+        fach = step_b / (mixed["ms_per_step"] * 1e-3) / 1e9
+        mixed["roofline"] = {"bound": "hbm", "achieved": fach, "peak": peak, "unit": "GB/s", "frac": fach / peak,
+                             "peak_kind": peak_kind, "bytes_per_step": step_b,
+                             "counted": "apply + column dots, update and scale passes (ftlm_step_bytes)"}
         if note:
             mixed["note"] = note
         torch.cuda.empty_cache()
@@ -521,8 +596,9 @@ def run_ours(args):
         line["ftlm"] = {"value": mixed["vec_steps_per_s"], "unit": "vec-steps/s", "mixed": mixed, "plain_fp64": plain,
                         "speedup_vs_plain_fp64": mixed["vec_steps_per_s"] / plain["vec_steps_per_s"]}
     if "lanczos" in legs and rank == 0:
-        # 96-spin eigen-solves: the nev lowest eigenpairs in plain FP64 and in mixed precision (FP32 Krylov
-        # vectors and gathers, FP64 recurrences, FP64 Rayleigh-Ritz polish), errors of the mixed eigenvalues
+        # 96-spin eigen-solves (the workloads of configs 2 and 3): the nev lowest eigenpairs in plain FP64 and in
+        # mixed precision (FP32 Krylov vectors and gathers, FP64 recurrences, FP64 Rayleigh-Ritz polish), and the
+        # errors of the mixed eigenvalues against the FP64 ones
         del x, y
         torch.cuda.empty_cache()
         out = {"nev": args.nev, "ncv": args.ncv, "tol": 1e-10}
@@ -545,6 +621,7 @@ def run_ours(args):
         out["abs_err_mixed_vs_f64"] = [float(v) for v in err]
         out["max_abs_err"] = float(err.max())
         out["levels_compared"] = int(len(err))
+        out["within_1e-9"] = bool(err.max() <= 1e-9)
         out["speedup_mixed_vs_f64"] = out["f64"]["seconds"] / out["mixed"]["seconds"]
         line["lanczos"] = out
     if "ftlm_sectors" in legs and rank == 0:
@@ -552,7 +629,22 @@ def run_ours(args):
     if "serve" in legs and rank == 0:
         line["serve"] = serve_leg(args)
     if "cpu" in legs and rank == 0:
-        line["cpu_baseline"] = cpu_baseline(w, H, args.cpu_seconds)
+        # One whole apply of the reference's push loop (oracle restatement) on all host cores, on the headline's
+        # x: the CPU baseline (whole apply, no sample) and the full-size parity check of the GPU results.
+        y_ref, dt, threads, lookups = oracle_whole_apply(w.basis_lohi, H.specs(), x_host)
+        line["cpu_baseline"] = {"value": n / dt, "unit": "states/s", "cores": threads, "kind": "port",
+                                "sample": f"one whole apply, all {n} source rows (per-term OpenMP pass, atomic "
+                                          f"scatter, {lookups} lookups), {dt:.1f}s"}
+        scale = float(np.abs(y_ref).max())
+        par = {"reference": "oracle push-loop apply of the same x, whole basis",
+               "apply_fp64": {"max_abs_err": float(np.abs(y_host - y_ref).max()),
+                              "rel_err": float(np.abs(y_host - y_ref).max()) / scale, "tol_rel": 1e-12}}
+        par["apply_fp64"]["pass"] = par["apply_fp64"]["rel_err"] <= 1e-12
+        if col0 is not None:
+            e = float(np.abs(col0 - y_ref).max()) / scale
+            par["apply_fp32_batched_col0"] = {"rel_err": e, "tol_rel": 4e-6, "pass": e <= 4e-6,
+                                              "note": "x rounded to FP32, double-float row accumulation"}
+        line["parity"] = par
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -179,8 +179,9 @@ def test_reference_side_adaptor_compiles_against_the_reference_headers(tmp_path)
 
     from oracle import oracle as O
 
-    ref = Path(O.REFERENCE_ROOT)
-    if not shutil.which("g++") or not (ref / "components" / "operator" / "src" / "operator.cpp").exists():
+    root = O.reference_root()
+    ref = Path(root) if root else None
+    if not shutil.which("g++") or ref is None or not (ref / "components" / "operator" / "src" / "operator.cpp").exists():
         pytest.skip("needs g++ and the reference checkout")
     main = """#include "gb300_lazy_op.hpp"
 int main(int argc, char**) {
@@ -208,22 +209,54 @@ int main(int argc, char**) {
 
 
 def test_reference_arm_runs_on_the_host():
-    """`bench.py --impl reference` (the restated push loop on the host cores) prints one contract line."""
+    """`bench.py --impl reference` (the restated push loop on the host cores) prints one contract line, builds its
+    basis and terms with the oracle alone (the engine's library is never loaded) and reports the same config as
+    the GPU arm would for that workload."""
     import json
     import subprocess
     import sys
 
-    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--lattice", "pyro_1x2x1",
-                        "--full-basis", "--steps", "1", "--warmup", "1", "--cpu-seconds", "0.5"],
-                       capture_output=True, text=True, timeout=600)
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--lattice', 'pyro_1x2x1', "
+            "'--full-basis', '--steps', '2', '--warmup', '1', '--ref-step-seconds', '0.2']; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "print('LOADED_ENGINE', 'libqsi_ed' in open('/proc/self/maps').read())")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=str(ROOT))
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
     assert len(lines) == 1
+    assert "LOADED_ENGINE False" in r.stdout
     d = lines[0]
     assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "states/s"
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["ms_per_step"] > 0 and d["steps"] == 2
+    # the GPU arm's config for this workload: same keys and values
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class A:
+        lattice, full_basis, sector, seed = "pyro_1x2x1", True, "", 3
+
+    spec = bench.workload_spec(A)
+    w = workloads.q0_32spin()
+    g, B = workloads.ring_zeeman_params(3, (0.2, 1.0), 0.5)
+    assert spec["g"] == [float(v) for v in g] and spec["B"] == [float(v) for v in B]
+    H = q.build_ring_zeeman(workloads.lattice("pyro_1x2x1"), spec["g"], spec["B"])
+    assert d["config"] == bench.workload_config(spec, len(w.basis_lohi), len(H))
     assert d["config"]["workload"] == "pyro_1x2x1.Q0" and d["config"]["n_states"] == 3618
+
+
+def test_reference_arm_samples_cover_the_basis():
+    import bench
+
+    n = 1_000_003
+    for step in range(5):
+        blocks = bench.sample_blocks(n, 100_000, step)
+        assert len(blocks) == 16
+        assert all(0 <= a < b <= n for a, b in blocks)
+        assert all(blocks[k][1] <= blocks[k + 1][0] for k in range(15))  # disjoint, in order
+        assert blocks[0][0] < n // 16 and blocks[-1][0] >= 15 * (n // 16)  # spread over the whole basis
+    assert bench.sample_blocks(100, 1000, 0)[-1][1] <= 100
 
 
 def test_device_path_fails_loudly_without_a_gpu():

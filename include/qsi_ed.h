@@ -281,6 +281,10 @@ typedef struct qsi_lanczos_cfg {
                              >= 2 rounds the FP32 Krylov phase stops at max(tol, 1e-7) and the
                              FP64 rounds (the 2nd on [X, HX - X theta]) refine the pairs */
     int32_t want_vectors; /* write eigenvectors */
+    int32_t block;        /* QSI_F32 only: 16 = block Lanczos on FP32 blocks of 16 vectors through the
+                             batched apply (nev <= 13), 1 = single-vector, 0 = block for bases of at
+                             least 65536 states when nev <= 13, else single-vector */
+    int32_t reserved;
 } qsi_lanczos_cfg;
 
 typedef struct qsi_report {

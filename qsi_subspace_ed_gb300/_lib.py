@@ -52,6 +52,8 @@ class LanczosCfg(C.Structure):
         ("seed", C.c_uint64),
         ("polish_steps", C.c_int32),
         ("want_vectors", C.c_int32),
+        ("block", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

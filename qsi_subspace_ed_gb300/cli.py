@@ -4,10 +4,11 @@
   python -m qsi_subspace_ed_gb300.cli ftlm_DOQSI_ham LATTICE.json [flags]     -> <out>/<params>.ftlm.h5
   python -m qsi_subspace_ed_gb300.cli eval_observables FILE.eigs.h5 [flags]   -> FILE.eigs.out.h5
   python -m qsi_subspace_ed_gb300.cli build_hamiltonian LATTICE.json [flags]  -> <out>/<params>.mat.mtx
+  python -m qsi_subspace_ed_gb300.cli partition_basis STEM.N.basis.h5         -> STEM.N.basis.partitioned.h5
 
 Flags, defaults, basis-file naming and output layouts follow src/diag_DOQSI_ham.cpp:14-173,
 include/lanczos_cli.hpp:5-40, include/basis_format_bits.hpp:8-48, src/ftlm_DOQSI_ham.cpp:14-72,
-src/eval_observables.cpp:44-130 and src/build_hamiltonian.cpp.  Every algorithm choice runs on the GPU:
+src/eval_observables.cpp:44-130, src/build_hamiltonian.cpp and components/build_basis/partition_basis.cpp.  Every algorithm choice runs on the GPU:
 mfeig0 is the reference's plain Lanczos (qsi_eigval0); dense, sparse and mfsparse use the thick-restart
 Lanczos solver on the matrix-free apply (qsi_lanczos_solve).
 """
@@ -226,8 +227,34 @@ def build_main(argv=None) -> Path:
     return out
 
 
+def lattice_of_basis_file(basis_file) -> Path:
+    """replace_filename of partition_basis.cpp:235-256: STEM.N.basis.h5 -> STEM.json."""
+    name = str(basis_file)
+    k = name.rfind(".basis.h5")
+    j = k
+    while j > 0 and name[j - 1].isdigit():
+        j -= 1
+    if k < 0 or j == k or j == 0 or name[j - 1] != ".":
+        raise SystemExit("Mangled basis name: expects .n.basis.h5 for some int n")
+    return Path(name[: j - 1] + ".json")
+
+
+def partition_main(argv=None) -> Path:
+    """partition_basis STEM.N.basis.h5 (components/build_basis/partition_basis.cpp:258-269): the basis split into
+    one dataset per sublattice-polarisation sector in STEM.N.basis.partitioned.h5, the sublattice masks read from
+    STEM.json."""
+    p = argparse.ArgumentParser(prog="partition_basis")
+    p.add_argument("basis_file", help="<latfile_stem>.N.basis.h5")
+    a = p.parse_args(argv)
+    from .core import partition_basis_h5
+
+    out = partition_basis_h5(a.basis_file, Lattice.load(lattice_of_basis_file(a.basis_file)))
+    print(f"Wrote {out}")
+    return out
+
+
 COMMANDS = {"diag_DOQSI_ham": diag_main, "ftlm_DOQSI_ham": ftlm_main, "eval_observables": eval_main,
-            "build_hamiltonian": build_main}
+            "build_hamiltonian": build_main, "partition_basis": partition_main}
 
 
 def main(argv=None) -> None:

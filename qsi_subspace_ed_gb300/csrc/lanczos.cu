@@ -468,6 +468,84 @@ __global__ void k_residual(const double* __restrict__ HX, const double* __restri
         for (int i = 0; i < k; ++i) R[(size_t)i * n + r] = HX[(size_t)i * n + r] - th[i] * X[(size_t)i * n + r];
 }
 
+// FP64 polish of the Ritz block X (nev FP64 vectors, vector-major, Ritz values th): Rayleigh-Ritz on X, then
+// `rounds - 1` Rayleigh-Ritz steps on [X, HX - X theta]; then the residual report and the solver's outputs.
+static qsi_status finish_solve(qsi_op* op, const qsi_lanczos_cfg& cfg, Vecs& vx, DevBuf<double>& X, DevBuf<double>& HX,
+                               std::vector<double>& th, int nev, int rounds, int64_t applies, int nconv, int restarts,
+                               bool exhausted, std::chrono::steady_clock::time_point t0, double* evals, double* evecs,
+                               qsi_report* rep) {
+    const int64_t n = op->basis->n;
+    cudaStream_t st = op->stream;
+    qsi_status s = QSI_OK;
+    std::vector<double> h;
+    // FP64 polish: Rayleigh-Ritz on the Ritz block, then optional residual-augmented rounds
+    DevBuf<double> S, HS, dth;
+    if (rounds > 0) {
+        QSI_CUDA(S.alloc((size_t)2 * nev * n, st));
+        QSI_CUDA(HS.alloc((size_t)2 * nev * n, st));
+        QSI_CUDA(dth.alloc((size_t)nev, st));
+        QSI_CUDA(cudaMemcpyAsync(S.p, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, st));
+        s = orthonormalise(vx, S.p, nev, n);
+        if (s) return s;
+        for (int i = 0; i < nev; ++i) {
+            s = launch_apply(op, S.p + (size_t)i * n, HS.p + (size_t)i * n, 1, QSI_F64, 0, st);
+            if (s) return s;
+            ++applies;
+        }
+        s = rayleigh_ritz(vx, S.p, HS.p, nev, nev, n, X.p, HX.p, th, st);
+        if (s) return s;
+        for (int round = 1; round < rounds; ++round) {
+            // S = [X, R], R = HX - X theta
+            QSI_CUDA(cudaMemcpyAsync(S.p, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, st));
+            QSI_CUDA(cudaMemcpyAsync(dth.p, th.data(), (size_t)nev * 8, cudaMemcpyHostToDevice, st));
+            k_residual<<<grid_for(n, 256), 256, 0, st>>>(HX.p, X.p, dth.p, nev, n, S.p + (size_t)nev * n);
+            s = orthonormalise(vx, S.p, 2 * nev, n);
+            if (s) return s;
+            for (int i = 0; i < 2 * nev; ++i) {
+                s = launch_apply(op, S.p + (size_t)i * n, HS.p + (size_t)i * n, 1, QSI_F64, 0, st);
+                if (s) return s;
+                ++applies;
+            }
+            s = rayleigh_ritz(vx, S.p, HS.p, 2 * nev, nev, n, X.p, HX.p, th, st);
+            if (s) return s;
+        }
+    } else {
+        for (int i = 0; i < nev; ++i) {
+            s = launch_apply(op, X.p + (size_t)i * n, HX.p + (size_t)i * n, 1, QSI_F64, 0, st);
+            if (s) return s;
+            ++applies;
+        }
+    }
+    // residual norms ||H x - theta x|| / ||x||
+    if (rep) {
+        DevBuf<double> R, d2;
+        QSI_CUDA(R.alloc((size_t)nev * n, st));
+        QSI_CUDA(d2.alloc((size_t)nev, st));
+        QSI_CUDA(cudaMemcpyAsync(d2.p, th.data(), (size_t)nev * 8, cudaMemcpyHostToDevice, st));
+        k_residual<<<grid_for(n, 256), 256, 0, st>>>(HX.p, X.p, d2.p, nev, n, R.p);
+        for (int i = 0; i < nev && i < 64; ++i) {
+            s = vx.dots<double>(X.p + (size_t)i * n, n, 1, R.p + (size_t)i * n, h);
+            if (s) return s;
+            std::vector<double> hx;
+            s = vx.dots<double>(X.p, n, 0, X.p + (size_t)i * n, hx);
+            if (s) return s;
+            rep->residual[i] = std::sqrt(h[1] / std::max(hx[0], 1e-300));
+        }
+        rep->converged = nconv;
+        rep->restarts = restarts;
+        rep->applies = applies;
+        rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    for (int i = 0; i < nev; ++i) evals[i] = th[i];
+    if (evecs && cfg.want_vectors) {
+        QSI_CUDA(cudaMemcpyAsync(evecs, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+    }
+    if (nconv < nev && !exhausted) return fail(QSI_NOT_CONVERGED, "lanczos: %d of %d eigenpairs converged after %d restarts", nconv, nev, restarts);
+    return QSI_OK;
+}
+
+
 // Thick-restart Lanczos (Wu & Simon) for the nev smallest eigenpairs.
 template <typename VT>
 static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, double* evecs, qsi_report* rep) {
@@ -601,72 +679,392 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     std::vector<double> th(Tw.begin(), Tw.begin() + nev);
     // free the Krylov basis before polishing
     V.release();
-    // FP64 polish: Rayleigh-Ritz on the Ritz block, then optional residual-augmented rounds
-    int rounds = std::max(cfg.polish_steps, sizeof(VT) == 4 ? 1 : 0);
-    DevBuf<double> S, HS, dth;
-    if (rounds > 0) {
-        QSI_CUDA(S.alloc((size_t)2 * nev * n, st));
-        QSI_CUDA(HS.alloc((size_t)2 * nev * n, st));
-        QSI_CUDA(dth.alloc((size_t)nev, st));
-        QSI_CUDA(cudaMemcpyAsync(S.p, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, st));
-        s = orthonormalise(vx, S.p, nev, n);
-        if (s) return s;
-        for (int i = 0; i < nev; ++i) {
-            s = launch_apply(op, S.p + (size_t)i * n, HS.p + (size_t)i * n, 1, QSI_F64, 0, st);
-            if (s) return s;
-            ++applies;
-        }
-        s = rayleigh_ritz(vx, S.p, HS.p, nev, nev, n, X.p, HX.p, th, st);
-        if (s) return s;
-        for (int round = 1; round < rounds; ++round) {
-            // S = [X, R], R = HX - X theta
-            QSI_CUDA(cudaMemcpyAsync(S.p, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToDevice, st));
-            QSI_CUDA(cudaMemcpyAsync(dth.p, th.data(), (size_t)nev * 8, cudaMemcpyHostToDevice, st));
-            k_residual<<<grid_for(n, 256), 256, 0, st>>>(HX.p, X.p, dth.p, nev, n, S.p + (size_t)nev * n);
-            s = orthonormalise(vx, S.p, 2 * nev, n);
-            if (s) return s;
-            for (int i = 0; i < 2 * nev; ++i) {
-                s = launch_apply(op, S.p + (size_t)i * n, HS.p + (size_t)i * n, 1, QSI_F64, 0, st);
-                if (s) return s;
-                ++applies;
+    return finish_solve(op, cfg, vx, X, HX, th, nev, std::max(cfg.polish_steps, sizeof(VT) == 4 ? 1 : 0), applies,
+                        nconv, restarts, m >= n, t0, evals, evecs, rep);
+}
+
+// ------------------------------------------------------------------ block thick-restart Lanczos (FP32 blocks)
+// The mixed-precision solve for large bases.  A single FP32 vector costs an apply as much as an FP64 one (a random
+// 4-byte gather moves the same memory sector as an 8-byte one), but the batched apply moves 16 FP32 vectors for
+// little more than the price of one, so the Krylov space grows a block of kBlk vectors per apply: block Lanczos
+// with full reorthogonalisation (two classical Gram-Schmidt passes per block) and thick restarts that keep whole
+// blocks of Ritz vectors.  Blocks are stored [row][16] in FP32, the batched apply's layout.  Projections are
+// FP32 products summed per 32-row tile and carried into double-float totals, reduced in FP64 in a fixed order
+// (deterministic, and none of it on GB300's slow FP64 pipe); the block QR is Cholesky QR done twice.  The phase
+// stops at the FP32 resolution (1e-7 relative residual) and the FP64 polish of finish_solve finishes the pairs.
+constexpr int kBlk = 16;      // vectors per Krylov block
+constexpr int kMaxBlk = 8;    // blocks per projection (128 vectors)
+constexpr int kProjRows = 32; // rows per shared-memory tile
+constexpr int kProjGrid = 1216;
+
+struct BlockPtrs {
+    const float* p[kMaxBlk];
+};
+
+// partial[blockIdx.x][r*16 + kq][c] = sum over this CTA's rows of Q_r[i][kq] * W[i][c], r < nq.
+__global__ void __launch_bounds__(256) k_block_project(BlockPtrs qs, int nq, const float* __restrict__ W, int64_t n,
+                                                       double* __restrict__ partial) {
+    __shared__ __align__(16) float tq[kMaxBlk + 1][kProjRows][kBlk];
+    const int t = threadIdx.x, kq = t >> 4, c = t & 15;
+    float hi[kMaxBlk], lo[kMaxBlk];
+#pragma unroll
+    for (int r = 0; r < kMaxBlk; ++r) hi[r] = lo[r] = 0.f;
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+    for (int64_t r0 = a; r0 < b; r0 += kProjRows) {
+        const int rows = (int)min((int64_t)kProjRows, b - r0);
+        __syncthreads();
+        for (int idx = t; idx < (nq + 1) * kProjRows * 4; idx += blockDim.x) {
+            const int blk = idx / (kProjRows * 4), e = idx % (kProjRows * 4), row = e >> 2, q4 = e & 3;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (row < rows) {
+                const float* src = (blk < nq) ? qs.p[blk] : W;
+                v = *reinterpret_cast<const float4*>(src + (r0 + row) * kBlk + q4 * 4);
             }
-            s = rayleigh_ritz(vx, S.p, HS.p, 2 * nev, nev, n, X.p, HX.p, th, st);
-            if (s) return s;
+            *reinterpret_cast<float4*>(&tq[blk == nq ? kMaxBlk : blk][row][q4 * 4]) = v;
         }
-    } else {
-        for (int i = 0; i < nev; ++i) {
-            s = launch_apply(op, X.p + (size_t)i * n, HX.p + (size_t)i * n, 1, QSI_F64, 0, st);
-            if (s) return s;
-            ++applies;
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kMaxBlk; ++r) {
+            if (r >= nq) break;
+            float s = 0.f;
+            for (int row = 0; row < rows; ++row) s = fmaf(tq[r][row][kq], tq[kMaxBlk][row][c], s);
+            const float sum = hi[r] + s, bb = sum - hi[r];
+            lo[r] += (hi[r] - (sum - bb)) + (s - bb);
+            hi[r] = sum;
         }
     }
-    // residual norms ||H x - theta x|| / ||x||
-    if (rep) {
-        DevBuf<double> R, d2;
-        QSI_CUDA(R.alloc((size_t)nev * n, st));
-        QSI_CUDA(d2.alloc((size_t)nev, st));
-        QSI_CUDA(cudaMemcpyAsync(d2.p, th.data(), (size_t)nev * 8, cudaMemcpyHostToDevice, st));
-        k_residual<<<grid_for(n, 256), 256, 0, st>>>(HX.p, X.p, d2.p, nev, n, R.p);
-        for (int i = 0; i < nev && i < 64; ++i) {
-            s = vx.dots<double>(X.p + (size_t)i * n, n, 1, R.p + (size_t)i * n, h);
-            if (s) return s;
-            std::vector<double> hx;
-            s = vx.dots<double>(X.p, n, 0, X.p + (size_t)i * n, hx);
-            if (s) return s;
-            rep->residual[i] = std::sqrt(h[1] / std::max(hx[0], 1e-300));
-        }
-        rep->converged = nconv;
-        rep->restarts = restarts;
-        rep->applies = applies;
-        rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (int r = 0; r < nq; ++r)
+        partial[((int64_t)blockIdx.x * nq * kBlk + r * kBlk + kq) * kBlk + c] = (double)hi[r] + (double)lo[r];
+}
+
+// out[e] = sum over blocks of partial[b][e] (e < count), fixed order.
+__global__ void k_sum_partials(const double* __restrict__ partial, int nblocks, int count, double* __restrict__ out) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nblocks; ++b) s += partial[(int64_t)b * count + e];
+        out[e] = s;
     }
-    for (int i = 0; i < nev; ++i) evals[i] = th[i];
-    if (evecs && cfg.want_vectors) {
-        QSI_CUDA(cudaMemcpyAsync(evecs, X.p, (size_t)nev * n * 8, cudaMemcpyDeviceToHost, st));
+}
+
+// out_o[i][c'] = sum_k Q[i][k] Y[k][o*16 + c'] for the nout output blocks (sub: out_o[i][c'] -= that sum), with
+// Y given as (hi, lo) float pairs ([16 nq][16 nout] row-major).  FP64 output: the first n64 of those vectors into
+// out64 (vector-major, vector v at out64 + v * n) instead of FP32 blocks.
+__global__ void __launch_bounds__(256) k_block_combine(BlockPtrs qs, int nq, const float2* __restrict__ Y, int nout,
+                                                       float* const* __restrict__ outs, int sub, double* __restrict__ out64,
+                                                       int n64, int64_t n) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* ys = reinterpret_cast<float2*>(smem);                                   // [16 nq][16 nout]
+    float* tq = reinterpret_cast<float*>(ys + (size_t)nq * kBlk * nout * kBlk);  // [nq][16 rows][16]
+    const int ncol = nout * kBlk;
+    for (int e = threadIdx.x; e < nq * kBlk * ncol; e += blockDim.x) ys[e] = Y[e];
+    const int rowl = threadIdx.x >> 4, c = threadIdx.x & 15;
+    for (int64_t r0 = (int64_t)blockIdx.x * 16; r0 < n; r0 += (int64_t)gridDim.x * 16) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nq * 16 * 4; idx += blockDim.x) {
+            const int blk = idx >> 6, e = idx & 63, row = e >> 2, q4 = e & 3;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r0 + row < n) v = *reinterpret_cast<const float4*>(qs.p[blk] + (r0 + row) * kBlk + q4 * 4);
+            *reinterpret_cast<float4*>(tq + (blk * 16 + row) * kBlk + q4 * 4) = v;
+        }
+        __syncthreads();
+        const int64_t i = r0 + rowl;
+        if (i >= n) continue;
+        for (int o = 0; o < nout; ++o) {
+            float sh = 0.f, sl = 0.f;
+            for (int r = 0; r < nq; ++r)
+#pragma unroll
+                for (int k = 0; k < kBlk; ++k) {
+                    const float q = tq[(r * 16 + rowl) * kBlk + k];
+                    const float2 y = ys[(size_t)(r * kBlk + k) * ncol + o * kBlk + c];
+                    sh = fmaf(q, y.x, sh);
+                    sl = fmaf(q, y.y, sl);
+                }
+            if (out64) {
+                if (o * kBlk + c < n64) out64[(int64_t)(o * kBlk + c) * n + i] = (double)sh + (double)sl;
+            } else {
+                float* dst = outs[o] + i * kBlk + c;
+                *dst = sub ? *dst - (sh + sl) : sh + sl;
+            }
+        }
+    }
+}
+
+// Deterministic N(0,1) entries of an FP32 block (count = rows * 16).
+__global__ void k_randn_f32(float* __restrict__ w, int64_t count, uint64_t seed) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < count; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = splitmix64(seed * 0x632be59bd9b4e019ULL + 2 * (uint64_t)r);
+        const uint64_t b = splitmix64(seed * 0x632be59bd9b4e019ULL + 2 * (uint64_t)r + 1);
+        const double u1 = ((a >> 11) + 1) * (1.0 / 9007199254740993.0), u2 = (b >> 11) * (1.0 / 9007199254740992.0);
+        w[r] = (float)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+    }
+}
+
+struct BlockSolver {
+    qsi_op* op;
+    int64_t n;
+    cudaStream_t st;
+    DevBuf<double> partial, red;
+    DevBuf<float2> ymat;
+    DevBuf<float*> outp;
+    qsi_status init() {
+        n = op->basis->n;
+        st = op->stream;
+        QSI_CUDA(partial.alloc((size_t)kProjGrid * kMaxBlk * kBlk * kBlk, st));
+        QSI_CUDA(red.alloc((size_t)kMaxBlk * kBlk * kBlk, st));
+        QSI_CUDA(ymat.alloc((size_t)kMaxBlk * kBlk * kMaxBlk * kBlk, st));
+        QSI_CUDA(outp.alloc(kMaxBlk, st));
+        return QSI_OK;
+    }
+    // C (16 nq x 16, row-major, host) = [Q_0 .. Q_{nq-1}]^T W
+    qsi_status project(float* const* Q, int nq, const float* W, std::vector<double>& C) {
+        BlockPtrs bp{};
+        for (int r = 0; r < nq; ++r) bp.p[r] = Q[r];
+        k_block_project<<<kProjGrid, 256, 0, st>>>(bp, nq, W, n, partial.p);
+        const int count = nq * kBlk * kBlk;
+        k_sum_partials<<<(count + 255) / 256, 256, 0, st>>>(partial.p, kProjGrid, count, red.p);
+        C.resize(count);
+        QSI_CUDA(cudaMemcpyAsync(C.data(), red.p, (size_t)count * 8, cudaMemcpyDeviceToHost, st));
         QSI_CUDA(cudaStreamSynchronize(st));
+        return QSI_OK;
     }
-    if (nconv < nev && !(m >= n)) return fail(QSI_NOT_CONVERGED, "lanczos: %d of %d eigenpairs converged after %d restarts", nconv, nev, restarts);
-    return QSI_OK;
+    // outs (nout blocks) = or -= Q Y, Y (16 nq x 16 nout, row-major FP64); or FP64 vector-major into out64
+    qsi_status combine(float* const* Q, int nq, const std::vector<double>& Y, int nout, float* const* outs, int sub,
+                       double* out64 = nullptr, int n64 = 0) {
+        BlockPtrs bp{};
+        for (int r = 0; r < nq; ++r) bp.p[r] = Q[r];
+        std::vector<float2> yf(Y.size());
+        for (size_t e = 0; e < Y.size(); ++e) {
+            const float h = (float)Y[e];
+            yf[e] = make_float2(h, (float)(Y[e] - (double)h));
+        }
+        QSI_CUDA(cudaMemcpyAsync(ymat.p, yf.data(), yf.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+        if (!out64) QSI_CUDA(cudaMemcpyAsync(outp.p, outs, (size_t)nout * sizeof(float*), cudaMemcpyHostToDevice, st));
+        const size_t smem = yf.size() * sizeof(float2) + (size_t)nq * 16 * kBlk * sizeof(float);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_block_combine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = (int)std::min<int64_t>((n + 15) / 16, (int64_t)sms * 4);
+        k_block_combine<<<grid, 256, smem, st>>>(bp, nq, ymat.p, nout, outp.p, sub, out64, n64, n);
+        QSI_CUDA(cudaGetLastError());
+        QSI_CUDA(cudaStreamSynchronize(st));  // the host-side Y / pointer copies are reused by the next call
+        return QSI_OK;
+    }
+    // W <- W - Q C twice (classical Gram-Schmidt, repeated); C accumulates both passes' coefficients
+    qsi_status orthogonalise(float* const* Q, int nq, float* W, std::vector<double>& C) {
+        std::vector<double> C2;
+        qsi_status s = project(Q, nq, W, C);
+        if (s) return s;
+        s = combine(Q, nq, C, 1, &W, 1);
+        if (s) return s;
+        s = project(Q, nq, W, C2);
+        if (s) return s;
+        s = combine(Q, nq, C2, 1, &W, 1);
+        if (s) return s;
+        for (size_t e = 0; e < C.size(); ++e) C[e] += C2[e];
+        return QSI_OK;
+    }
+    // Cholesky QR of W (twice): Qout = W R^{-1} with R upper triangular (16 x 16, row-major, returned).  ok =
+    // false when W is numerically rank deficient.
+    qsi_status cholqr(float* W, float* Qout, std::vector<double>& R, bool& ok) {
+        R.assign(kBlk * kBlk, 0.0);
+        for (int e = 0; e < kBlk; ++e) R[e * kBlk + e] = 1.0;
+        float* src = W;
+        for (int pass = 0; pass < 2; ++pass) {
+            std::vector<double> G;
+            qsi_status s = project(&src, 1, src, G);
+            if (s) return s;
+            // G = L L^T (lower), R_pass = L^T; R_pass^{-1}
+            std::vector<double> L(kBlk * kBlk, 0.0);
+            double gmax = 0.0;
+            for (int e = 0; e < kBlk; ++e) gmax = std::max(gmax, G[e * kBlk + e]);
+            ok = gmax > 0.0;
+            for (int j = 0; j < kBlk && ok; ++j) {
+                double d = G[j * kBlk + j];
+                for (int k = 0; k < j; ++k) d -= L[j * kBlk + k] * L[j * kBlk + k];
+                if (!(d > 1e-24 * gmax)) {
+                    ok = false;
+                    break;
+                }
+                L[j * kBlk + j] = std::sqrt(d);
+                for (int i = j + 1; i < kBlk; ++i) {
+                    double v = G[i * kBlk + j];
+                    for (int k = 0; k < j; ++k) v -= L[i * kBlk + k] * L[j * kBlk + k];
+                    L[i * kBlk + j] = v / L[j * kBlk + j];
+                }
+            }
+            if (!ok) return QSI_OK;
+            // Rinv = (L^T)^{-1} (upper triangular): solve L^T X = I column by column
+            std::vector<double> Rinv(kBlk * kBlk, 0.0), Rp(kBlk * kBlk, 0.0);
+            for (int i = 0; i < kBlk; ++i)
+                for (int j = 0; j < kBlk; ++j) Rp[i * kBlk + j] = L[j * kBlk + i];
+            for (int c = 0; c < kBlk; ++c)
+                for (int i = kBlk - 1; i >= 0; --i) {
+                    double v = (i == c) ? 1.0 : 0.0;
+                    for (int k = i + 1; k < kBlk; ++k) v -= Rp[i * kBlk + k] * Rinv[k * kBlk + c];
+                    Rinv[i * kBlk + c] = v / Rp[i * kBlk + i];
+                }
+            s = combine(&src, 1, Rinv, 1, &Qout, 0);
+            if (s) return s;
+            // R <- Rp R
+            std::vector<double> Rn(kBlk * kBlk, 0.0);
+            for (int i = 0; i < kBlk; ++i)
+                for (int j = 0; j < kBlk; ++j) {
+                    double v = 0.0;
+                    for (int k = 0; k < kBlk; ++k) v += Rp[i * kBlk + k] * R[k * kBlk + j];
+                    Rn[i * kBlk + j] = v;
+                }
+            R = Rn;
+            if (pass == 0) {  // second pass in place on Qout: copy into W's buffer first
+                QSI_CUDA(cudaMemcpyAsync(W, Qout, (size_t)n * kBlk * sizeof(float), cudaMemcpyDeviceToDevice, st));
+                src = W;
+            }
+        }
+        return QSI_OK;
+    }
+};
+
+// Block thick-restart Lanczos, FP32 Krylov blocks of kBlk vectors (see above), then the FP64 polish.
+static qsi_status btrlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, double* evecs, qsi_report* rep) {
+    auto t0 = std::chrono::steady_clock::now();
+    BlockSolver B{op};
+    qsi_status s = B.init();
+    if (s) return s;
+    const int64_t n = B.n;
+    cudaStream_t st = B.st;
+    const int nev = std::max(1, cfg.nev);
+    const int keep = ((nev + std::max(nev, 6) + kBlk - 1) / kBlk) * kBlk;  // kept Ritz vectors, whole blocks
+    const int kb = keep / kBlk;
+    int nblk = std::max(kb + 4, (cfg.ncv + kBlk - 1) / kBlk);  // at least four new blocks per restart cycle
+    nblk = std::min(nblk, kMaxBlk - 1);
+    if (kb + 2 > nblk || nev > keep || (int64_t)(nblk + 1) * kBlk > n)
+        return fail(QSI_INVALID_ARG, "block lanczos: nev %d needs more Krylov blocks than fit (dim %lld)", nev, (long long)n);
+    const int m = nblk * kBlk;
+    const double tol = std::max(cfg.tol > 0 ? cfg.tol : 1e-10, cfg.polish_steps >= 2 ? 1e-7 : 0.0);
+    const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
+    // nblk + 1 Krylov blocks, W and one spare block (the Cholesky QR output; also half of the restart scratch)
+    std::vector<DevBuf<float>> store(nblk + 3);
+    for (auto& b : store) QSI_CUDA(b.alloc((size_t)n * kBlk, st));
+    std::vector<float*> Q(nblk + 1);
+    for (int j = 0; j <= nblk; ++j) Q[j] = store[j].p;
+    float* W = store[nblk + 1].p;
+    float* spare = store[nblk + 2].p;
+    // start block: N(0,1), orthonormalised
+    std::vector<double> R, C;
+    bool ok = false;
+    for (int attempt = 0; attempt < 4 && !ok; ++attempt) {
+        k_randn_f32<<<grid_for(n * kBlk, 256), 256, 0, st>>>(W, n * kBlk, cfg.seed + 1000003ULL * attempt);
+        s = B.cholqr(W, Q[0], R, ok);
+        if (s) return s;
+    }
+    if (!ok) return fail(QSI_NOT_CONVERGED, "block lanczos: no independent start block");
+    std::vector<double> T((size_t)m * m, 0.0), Tw, TY, Blast(kBlk * kBlk, 0.0);
+    int k0 = 0;  // blocks kept from the previous cycle
+    int64_t applies = 0;
+    int restarts = 0, nconv = 0;
+    uint64_t breakdowns = 0;
+    for (;;) {
+        for (int j = k0; j < nblk; ++j) {
+            s = launch_apply(op, Q[j], W, kBlk, QSI_F32, 0, st);
+            if (s) return s;
+            applies += kBlk;
+            s = B.orthogonalise(Q.data(), j + 1, W, C);
+            if (s) return s;
+            // projected matrix column block j: T[0 .. 16(j+1), 16j .. 16j+16) = C, mirrored; its diagonal block
+            // symmetrised
+            for (int r = 0; r < (j + 1) * kBlk; ++r)
+                for (int c = 0; c < kBlk; ++c) {
+                    const int cc = j * kBlk + c;
+                    double v = C[(size_t)r * kBlk + c];
+                    if (r >= j * kBlk) v = 0.5 * (v + C[(size_t)(j * kBlk + c) * kBlk + (r - j * kBlk)]);
+                    T[(size_t)r * m + cc] = T[(size_t)cc * m + r] = v;
+                }
+            s = B.cholqr(W, Q[j + 1], R, ok);
+            if (s) return s;
+            if (!ok) {  // the Krylov space became invariant: continue from random directions orthogonal to it
+                ++breakdowns;
+                for (int attempt = 0; attempt < 4 && !ok; ++attempt) {
+                    k_randn_f32<<<grid_for(n * kBlk, 256), 256, 0, st>>>(W, n * kBlk, cfg.seed + 7919ULL * (breakdowns * 16 + attempt));
+                    s = B.orthogonalise(Q.data(), j + 1, W, C);
+                    if (s) return s;
+                    s = B.cholqr(W, Q[j + 1], R, ok);
+                    if (s) return s;
+                }
+                if (!ok) return fail(QSI_NOT_CONVERGED, "block lanczos: breakdown");
+                std::fill(R.begin(), R.end(), 0.0);
+            }
+            if (j + 1 < nblk) {
+                for (int a = 0; a < kBlk; ++a)
+                    for (int c = 0; c < kBlk; ++c)
+                        T[(size_t)((j + 1) * kBlk + a) * m + j * kBlk + c] = T[(size_t)(j * kBlk + c) * m + (j + 1) * kBlk + a] =
+                            R[(size_t)a * kBlk + c];
+            } else {
+                Blast = R;
+            }
+        }
+        s = jacobi_eigh(T, m, 1, Tw, TY, st);
+        if (s) return s;
+        // residual of Ritz pair i: || Blast y_last,i ||, y_last,i = the last block's components
+        std::vector<double> res(m, 0.0);
+        for (int i = 0; i < m; ++i) {
+            double acc = 0.0;
+            for (int a = 0; a < kBlk; ++a) {
+                double v = 0.0;
+                for (int c = 0; c < kBlk; ++c) v += Blast[(size_t)a * kBlk + c] * TY[(size_t)(m - kBlk + c) * m + i];
+                acc += v * v;
+            }
+            res[i] = std::sqrt(acc);
+        }
+        nconv = 0;
+        for (int i = 0; i < nev; ++i)
+            if (res[i] < tol * std::max(eps23, std::fabs(Tw[i]))) ++nconv;
+        if (nconv >= nev || restarts >= cfg.max_iter) break;
+        ++restarts;
+        // thick restart: the lowest `keep` Ritz vectors Q Y[:, :keep] into W and spare (kb <= 2 blocks), then
+        // the residual block continues the space
+        std::vector<double> Yk((size_t)m * keep);
+        for (int r = 0; r < m; ++r)
+            for (int c = 0; c < keep; ++c) Yk[(size_t)r * keep + c] = TY[(size_t)r * m + c];
+        if (kb > 2) return fail(QSI_INVALID_ARG, "block lanczos: more than two kept blocks");
+        float* outs[2] = {W, spare};
+        s = B.combine(Q.data(), nblk, Yk, kb, outs, 0);
+        if (s) return s;
+        // new basis: the Ritz blocks, then the residual block; every other buffer returns to the pool
+        float* res_blk = Q[nblk];
+        std::vector<float*> pool;
+        for (int j = 0; j < nblk; ++j) pool.push_back(Q[j]);
+        if (kb == 1) pool.push_back(spare);
+        Q[0] = W;
+        if (kb > 1) Q[1] = spare;
+        Q[kb] = res_blk;
+        size_t f = 0;
+        for (int j = kb + 1; j <= nblk; ++j) Q[j] = pool[f++];
+        W = pool[f++];
+        spare = pool[f++];
+        std::fill(T.begin(), T.end(), 0.0);
+        for (int i = 0; i < keep; ++i) T[(size_t)i * m + i] = Tw[i];
+        k0 = kb;
+    }
+    // FP64 Ritz vectors (vector-major) for the polish
+    DevBuf<double> X, HX;
+    QSI_CUDA(X.alloc((size_t)nev * n, st));
+    QSI_CUDA(HX.alloc((size_t)nev * n, st));
+    {
+        const int nout = (nev + kBlk - 1) / kBlk;
+        std::vector<double> Yn((size_t)m * nout * kBlk, 0.0);
+        for (int r = 0; r < m; ++r)
+            for (int c = 0; c < nev; ++c) Yn[(size_t)r * nout * kBlk + c] = TY[(size_t)r * m + c];
+        s = B.combine(Q.data(), nblk, Yn, nout, nullptr, 0, X.p, nev);
+        if (s) return s;
+    }
+    std::vector<double> th(Tw.begin(), Tw.begin() + nev);
+    for (auto& b : store) b.release();
+    Vecs vx;
+    s = vx.init(n, st);
+    if (s) return s;
+    return finish_solve(op, cfg, vx, X, HX, th, nev, std::max(cfg.polish_steps, 1), applies, nconv, restarts, false, t0,
+                        evals, evecs, rep);
 }
 
 // ------------------------------------------------------------------ eigval0 (mfeig0)
@@ -815,7 +1213,14 @@ extern "C" qsi_status qsi_lanczos_solve(qsi_op* op, const qsi_lanczos_cfg* cfg, 
     return guarded([&]() -> qsi_status {
         if (!op || !cfg || !evals) return fail(QSI_INVALID_ARG, "qsi_lanczos_solve: null argument");
         if (report) std::memset(report, 0, sizeof(*report));
-        if (cfg->precision == QSI_F32) return trlan<float>(op, *cfg, evals, evecs, report);
+        if (cfg->precision == QSI_F32) {
+            // FP32 Krylov blocks through the batched apply (btrlan) when asked (block == 16), or by default for
+            // bases large enough that the apply dominates and nev fits two kept blocks
+            const bool block = cfg->block == kBlk || (cfg->block == 0 && op->basis->n >= (1 << 16) && cfg->nev <= 13);
+            if (block) return btrlan(op, *cfg, evals, evecs, report);
+            if (cfg->block != 0 && cfg->block != 1) return fail(QSI_INVALID_ARG, "qsi_lanczos_solve: block must be 0, 1 or 16");
+            return trlan<float>(op, *cfg, evals, evecs, report);
+        }
         return trlan<double>(op, *cfg, evals, evecs, report);
     });
 }

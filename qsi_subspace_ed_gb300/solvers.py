@@ -26,12 +26,14 @@ class SolveReport:
 
 
 def diagonalise(op: LazyOpSum, nev: int = 1, ncv: int = 15, tol: float = 1e-10, max_iter: int = 1000,
-                seed: int = 0, precision: str = "f64", polish_steps: int = 0, want_vectors: bool = True):
+                seed: int = 0, precision: str = "f64", polish_steps: int = 0, want_vectors: bool = True,
+                block: int = 0):
     """nev smallest eigenpairs by thick-restart Lanczos with full reorthogonalisation.
 
     ncv is clamped to the dimension and nev to ncv-1 (matrix_diag_bits.hpp:64-66).
-    precision 'mixed' stores Krylov vectors in FP32 (FP64 coefficients and
-    projected problem) and polishes with FP64 Rayleigh-Ritz.
+    precision 'mixed' stores Krylov vectors in FP32 and polishes with FP64 Rayleigh-Ritz; block (mixed only):
+    16 = block Lanczos on FP32 blocks of 16 vectors through the batched apply, 1 = single-vector (FP64
+    coefficients), 0 = block for large bases when nev <= 13.
     Returns (evals, evecs (dim x nev) or None, SolveReport).
     """
     n = op.rows()
@@ -39,7 +41,7 @@ def diagonalise(op: LazyOpSum, nev: int = 1, ncv: int = 15, tol: float = 1e-10, 
     nev_e = min(nev, max(1, ncv_e - 1))
     cfg = LanczosCfg(nev=nev_e, ncv=ncv_e, max_iter=max_iter,
                      precision=_lib.QSI_F32 if precision == "mixed" else _lib.QSI_F64,
-                     tol=tol, seed=seed, polish_steps=polish_steps, want_vectors=int(want_vectors))
+                     tol=tol, seed=seed, polish_steps=polish_steps, want_vectors=int(want_vectors), block=int(block))
     evals = np.zeros(nev_e)
     evecs = np.zeros((nev_e, n)) if want_vectors else None
     rep = Report()

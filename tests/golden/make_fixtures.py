@@ -18,8 +18,10 @@ writes small files next to this script:
   observables48.npz        ring, ring_ring, partial_vol_sl0..3 of the reference's stored .eigs.out.h5
   wide128.json, apply_wide128.npy   connectivity digest and y = H x from the reference code for the 32-spin
                            Q=0 case with spin i at bit 4i+3 (states up to 128 bits)
+  adaptor_terms_q0_32.bin  the qsi_term array include/gb300_lazy_op.hpp builds from the reference's own operator
+                           objects for the 32-spin Q=0 Hamiltonian (tests/adaptor_main.cpp)
 
-`python tests/golden/make_fixtures.py REFERENCE_ROOT observables` (or `wide`) writes only those files.
+`python tests/golden/make_fixtures.py REFERENCE_ROOT observables` (or `wide`, `adaptor`) writes only those files.
 """
 from __future__ import annotations
 
@@ -171,12 +173,32 @@ def wide():
     print("wide128 fixtures written to", HERE)
 
 
+def adaptor():
+    """The qsi_term array the reference-side adaptor (include/gb300_lazy_op.hpp) hands to the library for the
+    32-spin Q=0 ring/Zeeman Hamiltonian, produced by tests/adaptor_main.cpp from the reference's own
+    SymbolicPMROperator objects (the GPU test makes the adaptor's C-ABI calls with it)."""
+    import tempfile
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    from helpers import run_adaptor
+
+    w = workloads.q0_32spin()
+    x, _ = np.load(HERE / "apply_q0_32.npy")
+    with tempfile.TemporaryDirectory() as d:
+        terms, _ = run_adaptor(d, w.basis_lohi, w.hamiltonian().specs(), x, str(REF))
+    (HERE / "adaptor_terms_q0_32.bin").write_bytes(terms)
+    print("adaptor_terms_q0_32.bin written to", HERE)
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[2] == "observables":
         observables()
     elif len(sys.argv) > 2 and sys.argv[2] == "wide":
         wide()
+    elif len(sys.argv) > 2 and sys.argv[2] == "adaptor":
+        adaptor()
     else:
         main()
         observables()
         wide()
+        adaptor()

@@ -58,3 +58,39 @@ def wide_case():
     for c, ops, ids in specs:
         H.add_term(c, q.SymbolicPMROperator(ops, ids))
     return lohi, H, specs
+
+
+def run_adaptor(workdir, basis_lohi, specs, x, reference_root):
+    """Builds tests/adaptor_main.cpp against the reference checkout's operator code and the engine's library, runs
+    it on (basis, term specs, x) and returns (the qsi_term bytes the adaptor hands to the library, y = H x and
+    y += H x as a (2, n) array, or the library's error text when its device path cannot run)."""
+    import subprocess
+
+    from qsi_subspace_ed_gb300 import _lib
+
+    workdir = Path(workdir)
+    ref = Path(reference_root)
+    root = Path(__file__).resolve().parent.parent
+    lib = Path(_lib.LIB_PATH)
+    exe = workdir / "adaptor_main"
+    cmd = ["g++", "-std=c++17", "-O1", "-fopenmp", f"-I{root / 'oracle' / 'ref_shim'}",
+           f"-I{ref / 'components' / 'operator' / 'include'}", f"-I{ref / 'components' / 'common' / 'include'}",
+           f"-I{root / 'include'}", str(root / "tests" / "adaptor_main.cpp"),
+           str(ref / "components" / "operator" / "src" / "operator.cpp"),
+           f"-L{lib.parent}", "-lqsi_ed", f"-Wl,-rpath,{lib.parent}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr[-3000:])
+    with open(workdir / "basis.csv", "w") as f:  # basis_io::write_line (components/common/include/basis_io.hpp:16-18)
+        f.writelines("0x%016x%016x\n" % (int(hi), int(lo)) for lo, hi in basis_lohi)
+    with open(workdir / "terms.txt", "w") as f:
+        f.writelines("%.17g %s %s\n" % (c, ops, " ".join(map(str, ids))) for c, ops, ids in specs)
+    np.ascontiguousarray(x, dtype=np.float64).tofile(workdir / "x.bin")
+    r = subprocess.run([str(exe), str(workdir / "basis.csv"), str(workdir / "terms.txt"), str(workdir / "x.bin"),
+                        str(workdir / "terms_out.bin"), str(workdir / "y_out.bin")], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"adaptor_main exited {r.returncode}: {r.stderr[-2000:]}")
+    terms = (workdir / "terms_out.bin").read_bytes()
+    if r.stdout.startswith("library error:"):
+        return terms, r.stdout.strip()
+    return terms, np.fromfile(workdir / "y_out.bin", dtype=np.float64).reshape(2, -1)

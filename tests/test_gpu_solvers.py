@@ -172,3 +172,38 @@ def test_eigval0_checkpoint_resume_is_bitwise(tmp_path):
     # a checkpoint of another seed is refused
     with pytest.raises(q.QsiError):
         q.eigval0(op, checkpoint=path, **{**kw, "seed": 6})
+
+
+@pytest.mark.parametrize("nev", [5, 10])
+def test_block_mixed_solver_matches_dense_oracle(nev):
+    """Block Lanczos on FP32 blocks of 16 vectors through the batched apply (kept Ritz blocks 1 and 2), then the
+    FP64 polish: the lowest eigenvalues of the 32-spin Q=0 basis within 1e-9 of the dense FP64 oracle."""
+    basis, H = cases()["q0_32"]
+    ref = golden_json("eigs_q0_32.json")["evals"]
+    op = q.LazyOpSum(q.ZBasis(basis), H)
+    w, V, rep = q.diagonalise(op, nev=nev, ncv=24, tol=1e-10, seed=3, precision="mixed", polish_steps=2, block=16)
+    np.testing.assert_allclose(w, ref[:nev], atol=1e-9)
+    assert np.all(rep.residual[:nev] < 1e-6)
+    for k in range(nev):
+        y = np.zeros(len(basis))
+        op.evaluate(np.ascontiguousarray(V[:, k]), y)
+        assert np.linalg.norm(y - w[k] * V[:, k]) < 1e-6 * np.linalg.norm(V[:, k])
+
+
+def test_block_mixed_solver_matches_fp64_on_a_larger_sector():
+    """The 64-spin 8.8.8.8 sector (221,628 states, the default block choice): ten lowest eigenvalues of the
+    block FP32 solve with FP64 polish against the plain FP64 thick-restart solve, within 1e-9; a second run is
+    bitwise the same (fixed reduction orders)."""
+    from qsi_subspace_ed_gb300 import workloads
+
+    w_ = workloads.sector_workload("pyro_1x2x2", seed=3, gpu=True)
+    op = q.LazyOpSum(q.ZBasis(w_.basis_lohi), w_.hamiltonian())
+    e64, _, _ = q.diagonalise(op, nev=10, ncv=24, tol=1e-10, seed=1, precision="f64", want_vectors=False)
+    eb, _, rep = q.diagonalise(op, nev=10, ncv=24, tol=1e-10, seed=1, precision="mixed", polish_steps=2,
+                               want_vectors=False)
+    top = min(eb.max(), e64.max())
+    err = [np.abs(e64 - v).min() for v in eb if v <= top + 1e-8]
+    assert len(err) >= 8 and max(err) <= 1e-9, err
+    eb2, _, _ = q.diagonalise(op, nev=10, ncv=24, tol=1e-10, seed=1, precision="mixed", polish_steps=2,
+                              want_vectors=False)
+    assert np.array_equal(eb, eb2)

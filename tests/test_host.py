@@ -159,6 +159,10 @@ def test_cli_names_and_flags():
         cli.diag_parser().parse_args(["L.json", "--g", "1", "1", "1", "1", "--B", "0", "0", "0", "-o", "o"])
     f = cli.ftlm_parser().parse_args(["L.json", "--g", "1", "2", "3", "4", "-o", "o", "--T_min", "0.1", "--T_max", "2"])
     assert (f.n_randvecs, f.n_temps, f.ncv) == (20, 100, 15)
+    # partition_basis: STEM.N.basis.h5 -> lattice STEM.json (replace_filename, partition_basis.cpp:235-256)
+    assert str(cli.lattice_of_basis_file("a/pyro_1x2x1.12.basis.h5")) == "a/pyro_1x2x1.json"
+    with pytest.raises(SystemExit):
+        cli.lattice_of_basis_file("a/x.basis.h5")
 
 
 def test_h5_string_round_trip(tmp_path):
@@ -171,41 +175,33 @@ def test_h5_string_round_trip(tmp_path):
     assert _read_string_h5(p, "dset_name") == "basis"
 
 
-def test_reference_side_adaptor_compiles_against_the_reference_headers(tmp_path):
-    """include/gb300_lazy_op.hpp (GB300LazyOpSum over SymbolicOpSum / ZBasisBST) compiles against the reference's
-    own operator.hpp and operator.cpp and links against libqsi_ed.so (no GPU call is made)."""
+def test_reference_side_adaptor_runs_with_the_reference_operator_code(tmp_path):
+    """include/gb300_lazy_op.hpp driven by the reference's own code (tests/adaptor_main.cpp, built against the
+    reference's operator.hpp/operator.cpp): the 32-spin Q=0 basis loaded into ZBasisBST from CSV, the Hamiltonian
+    built with SymbolicPMROperator, then GB300LazyOpSum::evaluate and evaluate_add.  The terms it hands to the
+    library equal the engine's own term compiler's bytes; on a machine without a GPU the adaptor surfaces the
+    library's error as an exception (no host fallback), and with one its results equal the reference's stored
+    apply.  tests/golden/adaptor_terms_q0_32.bin holds those terms for the GPU test of the same calls."""
     import shutil
-    import subprocess
 
+    from helpers import run_adaptor
     from oracle import oracle as O
 
     root = O.reference_root()
-    ref = Path(root) if root else None
-    if not shutil.which("g++") or ref is None or not (ref / "components" / "operator" / "src" / "operator.cpp").exists():
+    if not shutil.which("g++") or root is None:
         pytest.skip("needs g++ and the reference checkout")
-    main = """#include "gb300_lazy_op.hpp"
-int main(int argc, char**) {
-    if (argc < 0) {
-        ZBasisBST basis;
-        SymbolicOpSum<double> H;
-        GB300LazyOpSum<ZBasisBST> op(basis, H);
-        std::vector<double> x(op.rows()), y(op.rows());
-        op.evaluate(x.data(), y.data());
-        op.evaluate_add(x.data(), y.data());
-    }
-    return 0;
-}
-"""
-    src = tmp_path / "binding.cpp"
-    src.write_text(main)
-    lib = Path(_lib.LIB_PATH)
-    cmd = ["g++", "-std=c++17", "-fopenmp", f"-I{ROOT / 'oracle' / 'ref_shim'}",
-           f"-I{ref / 'components' / 'operator' / 'include'}", f"-I{ref / 'components' / 'common' / 'include'}",
-           f"-I{ROOT / 'include'}", str(src), str(ref / "components" / "operator" / "src" / "operator.cpp"),
-           f"-L{lib.parent}", "-lqsi_ed", f"-Wl,-rpath,{lib.parent}", "-o", str(tmp_path / "binding")]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-2000:]
-    assert subprocess.run([str(tmp_path / "binding")]).returncode == 0
+    w = workloads.q0_32spin()
+    H = w.hamiltonian()
+    x, y_ref = np.load(GOLDEN / "apply_q0_32.npy")
+    terms, y = run_adaptor(tmp_path, w.basis_lohi, H.specs(), x, root)
+    arr, nt = H.to_terms()
+    assert terms == bytes(arr)[: nt * 80]
+    assert terms == (GOLDEN / "adaptor_terms_q0_32.bin").read_bytes()
+    if isinstance(y, str):
+        assert "QSI_CUDA_ERROR" in y or "CUDA" in y, y
+    else:
+        np.testing.assert_allclose(y[0], y_ref, rtol=0, atol=1e-12 * np.abs(y_ref).max())
+        np.testing.assert_allclose(y[1], 2 * y_ref, rtol=0, atol=2e-12 * np.abs(y_ref).max())
 
 
 def test_reference_arm_runs_on_the_host():

@@ -51,12 +51,12 @@ def parse():
     p.add_argument("--ref-step-seconds", type=float, default=2.5,
                    help="target length of one reference-arm step (a sample of whole source rows)")
     p.add_argument("--no-extras", action="store_true", help="skip batched / FTLM / e2e / CPU legs")
-    p.add_argument("--legs", default="e2e,batched,ftlm,lanczos,ftlm_sectors,cpu",
+    p.add_argument("--legs", default="e2e,batched,ftlm,lanczos,ftlm_sectors,serve,cpu",
                    help="extra legs after the FP64 headline: e2e, batched, ftlm, lanczos (FP64 vs mixed 10-eigenvalue "
                         "solves), ftlm_sectors (multi-sector FTLM), serve (request loop), cpu (whole oracle apply: "
                         "CPU baseline and parity)")
     p.add_argument("--nev", type=int, default=10)
-    p.add_argument("--serve-n", type=int, default=240)
+    p.add_argument("--serve-n", type=int, default=200)
     p.add_argument("--ftlm-R", type=int, default=0,
                    help="FTLM vectors per sector (0: the first of --R; the ftlm_sectors leg: 64)")
     p.add_argument("--ftlm-M", type=int, default=100)
@@ -284,8 +284,10 @@ def torch_sync():
 
 
 def serve_leg(args):
-    """Request loop: Poisson phase-diagram points over three resident sectors, served with
-    `slots` concurrent solves, against the same requests solved one after another."""
+    """Request loop (config 5 scaled to the bench's time): Poisson phase-diagram points over three resident sectors,
+    served with `slots` concurrent solves and same-sector continuous batching (operator families: concurrent
+    requests' applies run as columns of one batched apply), against the same requests solved one after another
+    without batching (plain FP64 GPU solves)."""
     import qsi_subspace_ed_gb300 as q
     from qsi_subspace_ed_gb300 import serve, workloads
 
@@ -296,12 +298,15 @@ def serve_leg(args):
     weights = {"pyro_1x2x1.Q0": 0.5, "pyro_1x2x2.s8.8.8.8": 0.35, "pyro_1x2x2.Q0": 0.15}
     out = {"requests": args.serve_n, "rate_per_s": args.serve_rate, "nev": 5, "tol": 1e-9, "slots": args.serve_slots,
            "sectors": {k: v.dim for k, v in sectors.items()}, "weights": weights,
-           "note": "the 96-spin sector of the request mix is replaced by the 64-spin Q=0 basis"}
-    for name, slots in (("serial", 1), ("continuous", args.serve_slots)):
-        loop = serve.RequestLoop(sectors, slots=slots)
+           "note": "the 96-spin sector of the request mix is replaced by the 64-spin Q=0 basis: one 96-spin solve "
+                   "takes tens of seconds, and the mix's share of them would run for hours"}
+    for name, slots, batching in (("serial", 1, False), ("continuous", args.serve_slots, True)):
+        loop = serve.RequestLoop(sectors, slots=slots, batching=batching)
         try:
             arr = serve.poisson_requests(args.serve_n, args.serve_rate if slots > 1 else 1e9, weights, seed=7)
             out[name] = serve.run_arrivals(loop, arr)
+            if batching:
+                out[name]["batching"] = loop.family_stats()
         finally:
             loop.close()
     out["throughput_ratio"] = out["continuous"]["solves_per_s"] / out["serial"]["solves_per_s"]
@@ -455,13 +460,8 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     bytes_per_row = 16 + 8 + 8 * h + 8
     achieved = n * bytes_per_row / (ms * 1e-3) / 1e9
-    st0 = op.tuning(0)
-    if st0["use_hash"] and basis.index_info()["hash"]:
-        kname = "k_apply_tile<double,double,LookupHash>"
-    else:
-        kname = {"bisect": "k_apply_tile<double,double,LookupTable>",
-                 "candidates": "k_apply_tile<double,double,LookupTableGather>",
-                 "subkey": "k_apply_tile<double,double,LookupSubkey>"}[st0["table_mode"]]
+    lookup = "LookupHash" if op.tuning(0)["use_hash"] and basis.index_info()["hash"] else "LookupTable"
+    kname = f"k_apply_tile<double,double,{lookup}>"
     traffic = measured_traffic(w.name, kname, n)
     # the timed steps' input and result, kept on the host for the whole-size parity check against the oracle
     x_host = x.cpu().numpy() if rank == 0 else None

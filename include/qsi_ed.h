@@ -60,6 +60,7 @@ typedef struct qsi_term {
 
 typedef struct qsi_basis qsi_basis; /* device-resident sorted basis + bucket table */
 typedef struct qsi_op qsi_op;       /* operator bound to a basis */
+typedef struct qsi_family qsi_family; /* operators H(p) = sum_t p[class(t)] term_t over one basis */
 
 /* ---------------------------------------------------------------- errors */
 const char* qsi_version(void);
@@ -185,6 +186,23 @@ qsi_status qsi_basis_search(qsi_basis* b, const uint64_t* states_lohi, int64_t n
 qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t n_terms,
                          qsi_op** out);
 qsi_status qsi_op_destroy(qsi_op* op);
+/* Operator families for serving many parameter points of one sector at once (the request loop that replaces
+ * the reference's static phase-diagram plans, driver/ed_phasedia_plan.sh:21-25 with
+ * driver/execute_asynchronous.sh:1-38; no counterpart in the operator code): the terms of qsi_op_create with a
+ * class per term (term_class[t] < n_classes <= 16; diagonal terms must be single-site z), H(p) has coefficient
+ * p[class(t)] on term t (the terms' own coefficients are ignored).  qsi_family_member returns H(p) as an
+ * ordinary operator (every entry point takes it; release with qsi_op_destroy); its FP64 single-vector applies
+ * are queued with the family and the applies of all members waiting at the same time run as one batched apply,
+ * one column per member (at most max_cols <= 32), so concurrent solves share every lookup.  A member's results
+ * are bitwise the same whether its applies ran alone or batched.  Members may be used from several host
+ * threads at once (one thread per member). */
+qsi_status qsi_family_create(qsi_basis* b, const qsi_term* terms, int32_t n_terms,
+                             const int32_t* term_class, int32_t n_classes, int32_t max_cols,
+                             qsi_family** out);
+qsi_status qsi_family_destroy(qsi_family* f);
+qsi_status qsi_family_member(qsi_family* f, const double* p, qsi_op** out);
+/* Batches run and member applies they served (applies / batches = mean columns per batch). */
+qsi_status qsi_family_stats(const qsi_family* f, int64_t* batches, int64_t* applies);
 /* accumulate = 0: y = H x   (LazyOpSumProd::perform_op / LazyOpSum::evaluate,
  *                            operator_matrix.hpp:32-36,129-131)
  * accumulate = 1: y += H x  (LazyOpSum::evaluate_add, operator_matrix.cpp:108-112;

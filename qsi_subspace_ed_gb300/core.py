@@ -364,6 +364,16 @@ class LazyOpSum:
         self._h = C.c_void_p()
         call("qsi_op_create", basis._h, C.cast(self._terms, C.c_void_p), n, C.byref(self._h))
 
+    @classmethod
+    def _from_handle(cls, basis: ZBasis, handle: C.c_void_p) -> "LazyOpSum":
+        """An operator the library created (a family member)."""
+        op = cls.__new__(cls)
+        op.basis = basis
+        op.ops = None
+        op._terms = None
+        op._h = handle
+        return op
+
     def rows(self):
         return self.basis.dim()
 
@@ -494,6 +504,51 @@ class LazyOpSum:
     def close(self):
         if self._h:
             _lib.load().qsi_op_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OperatorFamily:
+    """H(p) = sum_t p[class(t)] term_t over one basis: the terms of `ops` with a class per term (in to_terms()
+    order); members H(p) are LazyOpSum operators whose FP64 single-vector applies run batched with those of the
+    family's other members waiting at the same time (qsi_family_create / qsi_family_member)."""
+
+    def __init__(self, basis: ZBasis, ops: SymbolicOpSum, term_class: Sequence[int], n_classes: int,
+                 max_cols: int = 8):
+        self.basis = basis
+        self.n_classes = int(n_classes)
+        self._terms, n = ops.to_terms()
+        cls = np.ascontiguousarray(term_class, dtype=np.int32)
+        if len(cls) != n:
+            raise ValueError(f"{len(cls)} classes for {n} terms")
+        self._h = C.c_void_p()
+        call("qsi_family_create", basis._h, C.cast(self._terms, C.c_void_p), n, ptr(cls), self.n_classes,
+             int(max_cols), C.byref(self._h))
+
+    def member(self, p) -> "LazyOpSum":
+        """The operator H(p) (p: one coefficient per class)."""
+        pa = np.ascontiguousarray(p, dtype=np.float64)
+        if pa.shape != (self.n_classes,):
+            raise ValueError(f"need {self.n_classes} class coefficients")
+        h = C.c_void_p()
+        call("qsi_family_member", self._h, ptr(pa), C.byref(h))
+        op = LazyOpSum._from_handle(self.basis, h)
+        op._family = self  # the family outlives its members
+        return op
+
+    def stats(self) -> dict:
+        b, a = C.c_int64(), C.c_int64()
+        call("qsi_family_stats", self._h, C.byref(b), C.byref(a))
+        return {"batches": b.value, "applies": a.value, "mean_columns": a.value / max(1, b.value)}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.load().qsi_family_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -34,7 +34,31 @@ struct TileParams {
     const float2* diag_ff;  // the same as (hi, lo) float pairs
     int n_off, n_lits, nwords;
     int vchunk;             // vectors per pass of the 16-byte batched kernel (16, 32, 64 or 128; 0 = 128)
+    // operator families (family mode kernels only): the terms' coefficients encode their class as +-(class + 1)
+    // and fcoef[class * fR + column] is the coefficient of that class in each column's operator
+    const double* fcoef = nullptr;
+    int fR = 1;
 };
+
+// Family mode: the coefficient of a hit whose term's coefficient encodes +-(class + 1), for column col.
+__device__ __forceinline__ double fam_coef(const TileParams& P, double enc, int col) {
+    const double c = P.fcoef[((int)(fabs(enc) + 0.5) - 1) * P.fR + col];
+    return enc < 0 ? -c : c;
+}
+// Family mode: the diagonal of state s for column col, sum over the single-site z groups of the template's
+// diagonal (weight +-(class + 1) each) of coefficient(class) * sign * (2 popcount(s & M) - |M|), in group order.
+__device__ __forceinline__ double fam_diag(const TileParams& P, uint64_t s0, uint64_t s1, int col) {
+    double d = 0.0;
+    for (int k = 0; k < P.D.n_cls; ++k) {
+        const double w = 0.5 * P.D.w2[k];
+        const int cls = (int)(fabs(w) + 0.5) - 1;
+        const int cnt = __popcll(P.D.m0[k]) + __popcll(P.D.m1[k]);
+        const int v = 2 * (__popcll(s0 & P.D.m0[k]) + __popcll(s1 & P.D.m1[k])) - cnt;
+        const double c = P.fcoef[cls * P.fR + col];
+        d += (w < 0 ? -c : c) * (double)v;
+    }
+    return d;
+}
 
 // |x| > 1e-15 (APPLY_TOL, operator_matrix.hpp:113) as integer compares on the
 // bit pattern: magnitude above the threshold and not a NaN.  For FP32 x the
@@ -176,7 +200,7 @@ __device__ __forceinline__ double term_coeff(const PullTerm& T, const state2 s) 
     return cs;
 }
 
-template <typename XT, typename YT, class LK>
+template <typename XT, typename YT, class LK, bool kFam = false>
 __global__ void __launch_bounds__(256, LK::kMinBlocks) k_apply_tile(TileParams P, LK lk, const XT* __restrict__ x,
                                                                  YT* __restrict__ y, int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -193,7 +217,7 @@ __global__ void __launch_bounds__(256, LK::kMinBlocks) k_apply_tile(TileParams P
         const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
         tile_spin_words(s, P.nwords, lane, spinw);
         for (int r = 0; r < n_rounds; ++r) adm[r * 32 + lane] = tile_admitted(S, P.n_off, r * 32, lane, vmask, spinw);
-        double acc = valid ? P.diag[row] * (double)x[row] : 0.0;
+        double acc = valid ? (kFam ? fam_diag(P, s.x, s.y, 0) : P.diag[row]) * (double)x[row] : 0.0;
         int r = 0;
         uint32_t a = adm[lane];
         while (true) {
@@ -225,7 +249,10 @@ __global__ void __launch_bounds__(256, LK::kMinBlocks) k_apply_tile(TileParams P
             for (int u = 0; u < kNB; ++u) xv[u] = (u < nh && J[u] >= 0) ? x[J[u]] : (XT)0;
 #pragma unroll
             for (int u = 0; u < kNB; ++u)
-                if (u < nh && J[u] >= 0 && above_tol(xv[u])) acc += term_coeff(S.terms[tt[u]], s) * (double)xv[u];
+                if (u < nh && J[u] >= 0 && above_tol(xv[u])) {
+                    const double cs = term_coeff(S.terms[tt[u]], s);
+                    acc += (kFam ? fam_coef(P, cs, 0) : cs) * (double)xv[u];
+                }
         }
         if (valid) {
             if (accumulate) acc += (double)y[row];
@@ -255,7 +282,7 @@ inline bool vec16_ok(int64_t n, int R, const void* x, const void* y) {
 }
 
 // Body of the batched tile kernel for one block (block_id of n_blocks working on this operator).
-template <typename XT, class LK, bool kFF, int KM>
+template <typename XT, class LK, bool kFF, int KM, bool kFam = false>
 __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, const XT* __restrict__ x,
                                              XT* __restrict__ y, int R, int accumulate, int cap, int64_t block_id,
                                              int64_t n_blocks, unsigned char* smem_raw,
@@ -530,6 +557,7 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                 const int b0 = __shfl_sync(0xffffffffu, base, l);
                 const int nl = __shfl_sync(0xffffffffu, cnt, l);
                 const double dl = __shfl_sync(0xffffffffu, d, l);
+                const uint64_t sl0 = __shfl_sync(0xffffffffu, s.x, l), sl1 = __shfl_sync(0xffffffffu, s.y, l);
                 const int64_t rl = tile * 32 + l;
                 if (rl >= P.B.n) break;
                 for (int r0 = 0; r0 < R; r0 += 32 * KM) {
@@ -538,7 +566,7 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
 #pragma unroll
                         for (int m = 0; m < KM; ++m) {
                             const int rr = r0 + lane + 32 * m;
-                            acc[m] = (rr < R) ? dl * (double)x[rl * R + rr] : 0.0;
+                            acc[m] = (rr < R) ? (kFam ? fam_diag(P, sl0, sl1, rr) : dl) * (double)x[rl * R + rr] : 0.0;
                         }
                         for (int k = b0; k < b0 + nl; k += 4) {
                             XT xv[4][KM];
@@ -557,7 +585,8 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                             for (int u = 0; u < 4; ++u)
 #pragma unroll
                                 for (int m = 0; m < KM; ++m)
-                                    if (above_tol(xv[u][m])) acc[m] += ck[u] * (double)xv[u][m];
+                                    if (above_tol(xv[u][m]))
+                                        acc[m] += (kFam ? fam_coef(P, ck[u], r0 + lane + 32 * m) : ck[u]) * (double)xv[u][m];
                         }
 #pragma unroll
                         for (int m = 0; m < KM; ++m) {
@@ -578,11 +607,11 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
     }
 }
 
-template <typename XT, class LK, bool kFF, int KM>
+template <typename XT, class LK, bool kFF, int KM, bool kFam = false>
 __global__ void __launch_bounds__(256, KM <= kVec4 ? 2 : 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
                                                             XT* __restrict__ y, int R, int accumulate, int cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    batched_body<XT, LK, kFF, KM>(P, lk, x, y, R, accumulate, cap, blockIdx.x, gridDim.x, smem_raw);
+    batched_body<XT, LK, kFF, KM, kFam>(P, lk, x, y, R, accumulate, cap, blockIdx.x, gridDim.x, smem_raw);
 }
 
 // Several operators (sectors) in one launch: the grid is partitioned into
@@ -872,6 +901,55 @@ qsi_status preload_apply_f64() {
     QSI_CUDA(cudaFuncGetAttributes(&a, k_apply_tile<double, double, LookupHash>));
     QSI_CUDA(cudaFuncGetAttributes(&a, k_apply_tile<double, double, LookupTable>));
     return preload_apply_f64_rows();
+}
+
+// Family mode applies of the template operator tmpl: y = H(p_c) x per column c (FP64, [row][R]), fcoef
+// [classes][R] on the device.  One column runs the single-vector tile kernel, several the batched one; both sum a
+// row in the same order, so a column's result does not depend on R.
+template <class LK>
+static qsi_status launch_family_lk(qsi_op* tmpl, LK lk, const double* x, double* y, int R, const double* fcoef,
+                                   int accumulate, cudaStream_t st) {
+    const qsi_tuning& T = tmpl->tune[0];
+    TileParams P{tmpl->basis->view(), tmpl->d_pull, tmpl->d_lit_off, tmpl->d_lits, tmpl->d_diag_generic, tmpl->diag,
+                 tmpl->d_diag, tmpl->d_diag_ff, tmpl->n_pull, tmpl->n_lits, tmpl->nwords, 0, fcoef, R};
+    const int block = 256, nw = block / 32;
+    const int64_t ntiles = (P.B.n + 31) / 32;
+    if (R == 1) {
+        const size_t smem = term_smem(tmpl) + (size_t)nw * (512 + (size_t)(tmpl->n_pull + 31) / 32 * 128);
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = (int)std::max<int64_t>(
+            1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * (T.grid_bps > 0 ? T.grid_bps : 8)));
+        auto k = k_apply_tile<double, double, LK, true>;
+        set_smem(k, smem);
+        k<<<grid, block, smem, st>>>(P, lk, x, y, accumulate);
+    } else {
+        const int cap = (std::max(tmpl->tune[1].list_cap, tmpl->n_pull + 1) + 7) & ~7;
+        const int n_rounds = (tmpl->n_pull + 31) / 32;
+        const size_t smem = term_smem(tmpl) + (size_t)nw * (512 + (size_t)n_rounds * 128 + (size_t)cap * 12);
+        if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "family apply: %zu bytes of shared memory needed", smem);
+        auto go = [&](auto km) {
+            constexpr int KM = decltype(km)::value;
+            auto k = k_apply_tile_batched<double, LK, false, KM, true>;
+            set_smem(k, smem);
+            k<<<one_wave(k, block, smem, ntiles, tmpl->tune[1].grid_bps), block, smem, st>>>(P, lk, x, y, R, accumulate,
+                                                                                             cap);
+        };
+        if (R <= 32) go(std::integral_constant<int, 1>{});
+        else if (R <= 64) go(std::integral_constant<int, 2>{});
+        else go(std::integral_constant<int, 4>{});
+    }
+    QSI_CUDA(cudaGetLastError());
+    return QSI_OK;
+}
+
+qsi_status launch_family(qsi_op* tmpl, const double* x, double* y, int R, const double* fcoef, int accumulate,
+                         cudaStream_t st) {
+    if (R < 1 || R > 128) return fail(QSI_INVALID_ARG, "family apply: %d columns (1..128)", R);
+    if (tmpl->basis->d_hash && tmpl->tune[R > 1].use_hash)
+        return launch_family_lk(tmpl, LookupHash{tmpl->basis->hview()}, x, y, R, fcoef, accumulate, st);
+    return launch_family_lk(tmpl, LookupTable{tmpl->basis->view()}, x, y, R, fcoef, accumulate, st);
 }
 
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,

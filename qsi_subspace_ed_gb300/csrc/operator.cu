@@ -590,6 +590,8 @@ extern "C" qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t
 extern "C" qsi_status qsi_op_destroy(qsi_op* op) {
     if (!op) return QSI_OK;
     if (op->stream) cudaStreamSynchronize(op->stream);
+    if (op->family) family_release_member(op);
+    if (op->d_fcoef) cudaFree(op->d_fcoef);
     cudaFree(op->d_pull);
     cudaFree(op->d_push_off);
     cudaFree(op->d_push_diag);
@@ -616,6 +618,8 @@ qsi_status preload_apply_f64_rows() {
 
 // Enqueues y (+)= H x on `st` for device pointers.
 qsi_status launch_apply(qsi_op* op, const void* x, void* y, int R, int dtype, int accumulate, cudaStream_t st) {
+    if (op->family && R == 1 && dtype == QSI_F64)
+        return family_apply(op, (const double*)x, (double*)y, accumulate, st);
     if (op->kernel == 1) return launch_apply_tiles(op, x, y, R, dtype, dtype, accumulate, st);
     BasisView V = op->basis->view();
     const int block = 256;

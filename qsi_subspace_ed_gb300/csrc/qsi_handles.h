@@ -27,8 +27,13 @@ struct qsi_tuning {
     int vec_width = 0;   // FP32 vectors per lane of the 16-byte batched kernel: 4 (0), 8 or 16
 };
 
+struct qsi_family;
+
 struct qsi_op {
     qsi_basis* basis = nullptr;
+    qsi_family* family = nullptr;  // member of an operator family: FP64 single-vector applies join its batches
+    double* d_fcoef = nullptr;     // the member's class coefficients on the device (family mode, one column)
+    std::vector<double> fcoef;     // ... and on the host
     qsi::PullTerm* d_pull = nullptr;        // transposed off-diagonal terms (apply)
     qsi::PushTerm* d_push_off = nullptr;    // off-diagonal terms as given (export)
     qsi::PushTerm* d_push_diag = nullptr;   // diagonal terms as given (export)
@@ -61,6 +66,13 @@ qsi_status launch_apply(qsi_op* op, const void* x, void* y, int R, int dtype, in
 qsi_status launch_apply_to_f64(qsi_op* op, const void* x, double* y, int xdtype, cudaStream_t st);
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
                               cudaStream_t st);
+// Family mode apply of a family's template operator: y = H(p_c) x per column c of [row][R] FP64 blocks.
+qsi_status launch_family(qsi_op* tmpl, const double* x, double* y, int R, const double* fcoef, int accumulate,
+                         cudaStream_t st);
+// A member's single-vector FP64 apply, run in a batch with the family's other waiting members.
+qsi_status family_apply(qsi_op* op, const double* x, double* y, int accumulate, cudaStream_t st);
+// Called by qsi_op_destroy for a family member.
+void family_release_member(qsi_op* op);
 qsi_status build_hash(qsi_basis* b);
 // Bucket table of a basis at its current width (b->bits, b->shift, b->n_buckets), allocated with padding for the
 // 16-byte reads of bucket_bounds.

@@ -128,3 +128,29 @@ def build_ring_zeeman(lat: Lattice, g, B, Jpm: float = 0.0, kappa: float = KAPPA
         h = _dot3(B, lz[int(a["sl"])])
         H.add_term(-h * kappa, SymbolicPMROperator("z", [i]))
     return H
+
+
+def ring_zeeman_classes(lat: Lattice, Jpm: float = 0.0):
+    """Class of every term of build_ring_zeeman (in its to_terms() order) for an operator family: the ring terms
+    of hexagon type sl are class sl (0..3), the Zeeman term of a spin on sublattice a is class 4 + a, bond hopping
+    (Jpm != 0) is class 8.  Returns (classes, n_classes)."""
+    off, diag = [], []
+    for ring in lat.rings:
+        if len(ring["member_spin_idx"]) != 6:
+            continue
+        off += [int(ring["sl"])] * 2
+    if Jpm:
+        off += [8] * (2 * len(lat.bonds))
+    diag = [4 + int(a["sl"]) for a in lat.data["atoms"]]
+    return off + diag, 9 if Jpm else 8
+
+
+def ring_zeeman_class_coefficients(g, B, Jpm: float = 0.0, kappa: float = KAPPA):
+    """Class coefficients p of H(g, B) for ring_zeeman_classes: -g[sl] for the rings, -(B . z_a) kappa for the
+    Zeeman terms (the same arithmetic as build_ring_zeeman, so a family member equals build_ring_zeeman's
+    operator term by term), -Jpm for the hopping."""
+    lz = get_loc_z()
+    p = [-float(g[k]) for k in range(4)] + [-_dot3(B, lz[a]) * kappa for a in range(4)]
+    if Jpm:
+        p.append(-float(Jpm))
+    return p

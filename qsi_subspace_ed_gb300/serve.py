@@ -1,12 +1,20 @@
 """Request loop for phase-diagram points: resident bases, HBM admission, continuous batching.
 
 A request is one ground-state-manifold solve (the nev lowest eigenvalues) of the ring/Zeeman Hamiltonian
-H(g, B) on one named sector.  The loop keeps every sector's basis and lookup index resident on the device
-once loaded, and runs up to `slots` solves at a time, each on its own operator (own CUDA stream), so
-solves that arrive while others run are admitted as soon as a slot and enough device memory are free and
-their kernels overlap on the GPU.  Among waiting requests, one whose sector is already resident and has
-a solve running is preferred (same-sector batching keeps that basis hot in L2/HBM); otherwise the oldest.
-Every solve is deterministic, so a result is identical whether the request ran alone or in the mix.
+H(g, B) on one named sector; it replaces the reference's static phase-diagram plans run by a process pool
+(driver/ed_phasedia_plan.sh:21-25, driver/execute_asynchronous.sh:1-38).  The loop keeps every sector's basis
+and lookup index resident on the device once loaded, and runs up to `slots` solves at a time, each on its own
+worker thread and operator stream; a request that arrives while others run is admitted as soon as a slot and
+enough device memory are free.  Among waiting requests, one whose sector already has a solve running is
+preferred, then the oldest.
+
+With batching (the default) every sector is an operator family (OperatorFamily: H(p) with per-class
+coefficients p = ring couplings by hexagon type and Zeeman field by sublattice) and each request's operator
+is a member of it: the single-vector applies of all same-sector solves that wait at the same moment run as one
+batched apply, one column per request, so concurrent requests share every basis read and lookup while each
+runs its own Lanczos (restarts, convergence) at its own pace; requests join at their first apply and leave
+when their solve ends.  Every solve is deterministic and a member's results do not depend on the batch it ran
+in, so a result is identical whether the request ran alone or in the mix.
 
 Latency is completion minus arrival; the loop reports p50/p99 and completed solves per second.
 """
@@ -20,8 +28,8 @@ from typing import Callable
 
 import numpy as np
 
-from .core import LazyOpSum, ZBasis
-from .hamiltonian import build_ring_zeeman
+from .core import LazyOpSum, OperatorFamily, ZBasis
+from .hamiltonian import build_ring_zeeman, ring_zeeman_class_coefficients, ring_zeeman_classes
 from .lattice import Lattice
 from .solvers import diagonalise
 
@@ -64,9 +72,10 @@ def solve_footprint(dim: int, nev: int, ncv: int) -> int:
     return 8 * dim * (ncv + 1 + 2 * nev + 4) + (64 << 20)
 
 
-def basis_footprint(dim: int) -> int:
-    """Resident bytes of a basis: states, bucket table (~4 B/state at the automatic size), hash index (<= 64 B/state)."""
-    return dim * (16 + 4 + 64)
+def basis_footprint(dim: int, batch_cols: int = 0) -> int:
+    """Resident bytes of a basis: states, bucket table (~4 B/state at the automatic size), hash index (<= 64 B/state),
+    and with batching the family's two [dim][batch_cols] FP64 batch blocks."""
+    return dim * (16 + 4 + 64 + 16 * batch_cols)
 
 
 class RequestLoop:
@@ -74,12 +83,14 @@ class RequestLoop:
     default to the device solve and ZBasis (both replaceable, e.g. by host-side fakes)."""
 
     def __init__(self, sectors: dict[str, Sector], slots: int = 4, hbm_budget: int = 200 << 30,
-                 solve: Callable | None = None, make_basis: Callable | None = None):
+                 solve: Callable | None = None, make_basis: Callable | None = None, batching: bool = True):
         self.sectors = sectors
         self.slots = slots
         self.budget = hbm_budget
+        self.batching = batching and solve is None
         self._solve = solve or self._solve_default
         self._make_basis = make_basis or ZBasis
+        self._families: dict[str, OperatorFamily] = {}
         self._lock = threading.Condition()
         self._waiting: deque[Request] = deque()
         self._running: dict[int, Request] = {}
@@ -134,7 +145,7 @@ class RequestLoop:
         sec = self.sectors[req.sector]
         need = solve_footprint(sec.dim, req.nev, req.ncv)
         if req.sector not in self._bases:
-            need += basis_footprint(sec.dim)
+            need += basis_footprint(sec.dim, self.slots if self.batching else 0)
         return need
 
     def _pick(self) -> Request | None:
@@ -168,10 +179,19 @@ class RequestLoop:
                     sec = self.sectors[req.sector]
                     basis = self._make_basis(sec.basis_lohi)
                     self._bases[req.sector] = basis
-                    self._in_use += basis_footprint(sec.dim)  # stays resident and accounted for
+                    if self.batching:
+                        cls, n_cls = ring_zeeman_classes(sec.lattice)
+                        self._families[req.sector] = OperatorFamily(
+                            basis, build_ring_zeeman(sec.lattice, [1.0] * 4, [0.0] * 3), cls, n_cls, self.slots)
+                    # stays resident and accounted for
+                    self._in_use += basis_footprint(sec.dim, self.slots if self.batching else 0)
+                family = self._families.get(req.sector)
             req.start = time.perf_counter()
             try:
-                req.evals = self._solve(req, basis, self.sectors[req.sector])
+                if family is not None:
+                    req.evals = self._solve_member(req, family)
+                else:
+                    req.evals = self._solve(req, basis, self.sectors[req.sector])
             except Exception as e:  # a failed solve is reported with its request, the loop carries on
                 req.error = f"{type(e).__name__}: {e}"
             req.done = time.perf_counter()
@@ -181,6 +201,19 @@ class RequestLoop:
                 self.completed.append(req)
                 req.event.set()
                 self._lock.notify_all()
+
+    def family_stats(self) -> dict:
+        """Per sector: batches run, member applies served and mean columns per batch."""
+        return {k: f.stats() for k, f in self._families.items()}
+
+    @staticmethod
+    def _solve_member(req: Request, family: OperatorFamily) -> np.ndarray:
+        op = family.member(ring_zeeman_class_coefficients(req.g, req.B))
+        try:
+            ev, _, _ = diagonalise(op, nev=req.nev, ncv=req.ncv, tol=req.tol, seed=req.rid + 1, want_vectors=False)
+        finally:
+            op.close()
+        return ev
 
     @staticmethod
     def _solve_default(req: Request, basis: ZBasis, sec: Sector) -> np.ndarray:

@@ -24,6 +24,54 @@ def _requests(n=14):
     return [r for _, r in arr]
 
 
+def test_family_members_batch_bitwise_and_match_their_operators():
+    """Operator-family members H(p): a member's apply equals the plain operator of the same H to rounding, and
+    its results are bitwise the same whether its applies ran alone or batched with other members' (several host
+    threads applying at once)."""
+    import threading
+
+    from qsi_subspace_ed_gb300.hamiltonian import ring_zeeman_class_coefficients, ring_zeeman_classes
+
+    lat = workloads.lattice("pyro_1x2x1")
+    lohi = q.enumerate_basis(lat)
+    b = q.ZBasis(lohi)
+    cls, ncls = ring_zeeman_classes(lat)
+    fam = q.OperatorFamily(b, q.build_ring_zeeman(lat, [1.0] * 4, [0.0] * 3), cls, ncls, max_cols=4)
+    rng = np.random.default_rng(5)
+    params = [(list(rng.uniform(0, 1, 4)), list(rng.uniform(-1, 1, 3))) for _ in range(4)]
+    members = [fam.member(ring_zeeman_class_coefficients(g, B)) for g, B in params]
+    x = rng.standard_normal(len(lohi))
+    alone = []
+    for (g, B), m in zip(params, members):
+        y = np.zeros_like(x)
+        m.evaluate(x, y)
+        alone.append(y)
+        ref = np.zeros_like(x)
+        q.LazyOpSum(b, q.build_ring_zeeman(lat, g, B)).evaluate(x, ref)
+        np.testing.assert_allclose(y, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    assert fam.stats()["mean_columns"] == 1.0
+    out = [[None] * 20 for _ in members]
+    gate = threading.Barrier(len(members))
+
+    def run(k):
+        gate.wait()
+        for rep in range(20):
+            y = np.zeros_like(x)
+            members[k].evaluate(x, y)
+            out[k][rep] = y
+
+    ts = [threading.Thread(target=run, args=(k,)) for k in range(len(members))]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    for k in range(len(members)):
+        for y in out[k]:
+            assert np.array_equal(y, alone[k])
+    st = fam.stats()
+    assert st["mean_columns"] > 1.0, st  # concurrent applies ran as batched columns
+
+
 def test_results_identical_alone_and_in_the_mix():
     sectors = _sectors()
     alone = {}
@@ -41,12 +89,34 @@ def test_results_identical_alone_and_in_the_mix():
         reqs = [mix.submit(r) for r in _requests()]
         mix.drain(timeout=300)
         st = mix.stats()
+        fam = mix.family_stats()
     finally:
         mix.close()
     assert st["completed"] == len(reqs) and st["failed"] == 0
     for r in reqs:
         assert np.array_equal(r.evals, alone[r.rid]), r.rid
     assert st["p99_s"] >= st["p50_s"] > 0
+    # same-sector requests shared batched applies (continuous batching, not a queue alone)
+    assert max(f["mean_columns"] for f in fam.values()) > 1.0, fam
+
+
+def test_batched_results_match_unbatched_solves():
+    """A request served through its sector's operator family gives the eigenvalues of a plain solve of the same
+    H(g, B) to 1e-9."""
+    sectors = _sectors()
+    reqs = _requests(6)
+    loop = serve.RequestLoop(sectors, slots=3)
+    try:
+        for r in reqs:
+            loop.submit(r)
+        loop.drain(timeout=300)
+    finally:
+        loop.close()
+    for r in reqs:
+        sec = sectors[r.sector]
+        op = q.LazyOpSum(q.ZBasis(sec.basis_lohi), q.build_ring_zeeman(sec.lattice, r.g, r.B))
+        ev, _, _ = q.diagonalise(op, nev=r.nev, ncv=r.ncv, tol=r.tol, seed=r.rid + 1, want_vectors=False)
+        np.testing.assert_allclose(r.evals, ev, atol=1e-9)
 
 
 def test_admission_respects_the_memory_budget():

@@ -9,6 +9,7 @@
 // The writer emits the same structures with fixed-length strings (the
 // reference writes variable-length strings for latfile_json / dset_name).
 #include <algorithm>
+#include <cassert>
 #include <cerrno>
 #include <cstring>
 #include <fstream>
@@ -29,13 +30,13 @@ struct Reader {
     int so = 8, sl = 8;  // sizes of offsets and lengths
 
     uint64_t rd(uint64_t pos, int n) const {
-        if (pos + n > buf.size()) throw std::runtime_error("HDF5: read past end of file");
+        if (pos > buf.size() || n > buf.size() - pos) throw std::runtime_error("HDF5: read past end of file");
         uint64_t v = 0;
         for (int i = 0; i < n; ++i) v |= (uint64_t)buf[pos + i] << (8 * i);
         return v;
     }
     const uint8_t* at(uint64_t pos, uint64_t n) const {
-        if (pos + n > buf.size()) throw std::runtime_error("HDF5: read past end of file");
+        if (pos > buf.size() || n > buf.size() - pos) throw std::runtime_error("HDF5: read past end of file");
         return buf.data() + pos;
     }
 };
@@ -179,6 +180,7 @@ static uint64_t superblock(Reader& R) {
     if (ver > 1) throw std::runtime_error("HDF5: superblock version >1 is not supported");
     R.so = (int)R.rd(off + 13, 1);
     R.sl = (int)R.rd(off + 14, 1);
+    if (R.so < 1 || R.so > 8 || R.sl < 1 || R.sl > 8) throw std::runtime_error("HDF5: unsupported offset/length size");
     uint64_t p = off + 24 + (ver == 1 ? 4 : 0);
     R.base = R.rd(p, R.so);
     p += 4 * R.so;  // base, free-space, eof, driver
@@ -250,10 +252,12 @@ static const uint8_t* dataset_bytes(const Reader& R, const Dataset& d, uint64_t 
 // ------------------------------------------------------------------ writer
 struct Writer {
     std::vector<uint8_t> out;
-    void put(uint64_t v, int n) {
+    void put(uint64_t v, int n) {  // n <= 8: a shift by 64 bits or more is undefined
+        assert(n <= 8);
         for (int i = 0; i < n; ++i) out.push_back((uint8_t)(v >> (8 * i)));
     }
     void put_at(uint64_t pos, uint64_t v, int n) {
+        assert(n <= 8);
         for (int i = 0; i < n; ++i) out[pos + i] = (uint8_t)(v >> (8 * i));
     }
     void align8() {
@@ -376,7 +380,8 @@ static void write_file(const char* path, std::vector<OutDataset> ds) {
             }
             W.put(0, 4);
             W.put(0, 4);
-            W.put(0, 16);
+            W.put(0, 8);  // 16-byte scratch pad, written as two 8-byte words (put takes at most 8)
+            W.put(0, 8);
         }
         if (ds.empty()) break;
     }

@@ -380,12 +380,15 @@ def run_reference(args):
 
 
 def ftlm_step_bytes(n: int, R: int, h: float, blocks: int, s: int = 4) -> float:
-    """Algorithmic bytes of one FTLM step (one sector, R vectors of s bytes, h off-diagonal hits per row): the
-    apply (16 + R s (h + 2) per row, plus the accumulated previous block read in the two-block recurrence), the
-    column dots <C, W> (2 R s), the update P <- W - alpha C - beta P (reads W, C, P and writes P: 4 R s; two
-    blocks: P - alpha C, 3 R s) and the scale P /= beta (2 R s)."""
-    apply_b = 16 + R * s * (h + 2) + (R * s if blocks == 2 else 0)
-    return n * (apply_b + 2 * R * s + (3 if blocks == 2 else 4) * R * s + 2 * R * s)
+    """Algorithmic bytes of one FTLM step (one sector, R vectors of s bytes, h off-diagonal hits per row).
+    Two blocks (the one-launch FP32 form): the apply P <- H C - beta P (16 + R s (h + 2) per row, plus the read of
+    P it accumulates into), one pass of dots over C and P (2 R s) and P <- (P - alpha C) / beta (reads C, P and
+    writes P: 3 R s).  Three blocks: the apply W = H C, the dots <C, W> (2 R s), the update P <- W - alpha C -
+    beta P (4 R s) and the scale P /= beta (2 R s)."""
+    apply_b = 16 + R * s * (h + 2)
+    if blocks == 2:
+        return n * (apply_b + R * s + 2 * R * s + 3 * R * s)
+    return n * (apply_b + 2 * R * s + 4 * R * s + 2 * R * s)
 
 
 def run_ours(args):
@@ -552,20 +555,20 @@ def run_ours(args):
             torch.cuda.empty_cache()
     if "ftlm" in legs and rank == 0:
         # FTLM vector-steps/s on the same operator: batched mixed precision (ftlm-R FP32 vectors, one apply
-        # launch per step, the run captured in one CUDA graph; two vector blocks instead of three when three do
-        # not fit, as at R = 128 on the 96-spin sector) against plain FP64 single-vector Lanczos.
+        # launch per step, the run captured in one CUDA graph, the in-place two-block recurrence) against plain
+        # FP64 single-vector Lanczos.
         # Per-step rates come from the difference of an M and an M/3 step run (setup, capture and readout
         # cancel); the rates including setup are given beside them.
         M1 = max(3, args.ftlm_steps)
         M0 = max(1, M1 // 3)
 
-        def ftlm_rate(R, prec):
-            q.ftlm([op], [R], M=2, seed=1, precision=prec)  # warm-up (allocations, graph paths)
+        def ftlm_rate(R, prec, blocks=0):
+            q.ftlm([op], [R], M=2, seed=1, precision=prec, blocks=blocks)  # warm-up (allocations, graph paths)
             t = {}
             for M in (M0, M1):
                 torch.cuda.synchronize()
                 t0 = time.time()
-                q.ftlm([op], [R], M=M, seed=1, precision=prec)
+                q.ftlm([op], [R], M=M, seed=1, precision=prec, blocks=blocks)
                 t[M] = time.time() - t0
             per = (t[M1] - t[M0]) / (M1 - M0)
             return {"R": R, "precision": prec, "ms_per_step": per * 1e3, "vec_steps_per_s": R / per,
@@ -574,21 +577,20 @@ def run_ours(args):
         R_ftlm = args.ftlm_R or int(str(args.R).split(",")[0])
         note = None
         try:
-            mixed = ftlm_rate(R_ftlm, "mixed")  # the batched settings tuned for R = first of --R
+            mixed = ftlm_rate(R_ftlm, "mixed", 2)  # the batched settings tuned for R = first of --R
         except q.QsiError as e:  # device memory taken by others: half the vectors
             if R_ftlm <= 16:
                 raise
             note = f"R={R_ftlm} failed ({str(e)[:120]}); R={R_ftlm // 2} instead"
             R_ftlm //= 2
             torch.cuda.empty_cache()
-            mixed = ftlm_rate(R_ftlm, "mixed")
-        free_b, total_b = torch.cuda.mem_get_info()
-        mixed["vector_blocks"] = 3 if 3 * n * R_ftlm * 4 + (4 << 30) <= free_b else 2
+            mixed = ftlm_rate(R_ftlm, "mixed", 2)
+        mixed["vector_blocks"] = 2
         step_b = ftlm_step_bytes(n, R_ftlm, h, mixed["vector_blocks"])
         fach = step_b / (mixed["ms_per_step"] * 1e-3) / 1e9
         mixed["roofline"] = {"bound": "hbm", "achieved": fach, "peak": peak, "unit": "GB/s", "frac": fach / peak,
                              "peak_kind": peak_kind, "bytes_per_step": step_b,
-                             "counted": "apply + column dots, update and scale passes (ftlm_step_bytes)"}
+                             "counted": "apply (with the read of the block it accumulates into) + one dots pass + one update pass (ftlm_step_bytes)"}
         if note:
             mixed["note"] = note
         torch.cuda.empty_cache()

@@ -203,6 +203,10 @@ qsi_status qsi_family_destroy(qsi_family* f);
 qsi_status qsi_family_member(qsi_family* f, const double* p, qsi_op** out);
 /* Batches run and member applies they served (applies / batches = mean columns per batch). */
 qsi_status qsi_family_stats(const qsi_family* f, int64_t* batches, int64_t* applies);
+/* Bases with fewer than min_rows states are not batched (default 131072): their applies take about a kernel
+ * launch, less than queueing for partners costs, so each member's apply runs at once on its own stream (same
+ * kernel and sums; a batch of one).  0 batches every basis. */
+qsi_status qsi_family_set_min_rows(qsi_family* f, int64_t min_rows);
 /* accumulate = 0: y = H x   (LazyOpSumProd::perform_op / LazyOpSum::evaluate,
  *                            operator_matrix.hpp:32-36,129-131)
  * accumulate = 1: y += H x  (LazyOpSum::evaluate_add, operator_matrix.cpp:108-112;
@@ -361,8 +365,10 @@ qsi_status qsi_ftlm_run(qsi_op** ops, int32_t n_sectors, const int32_t* R,
 /* qsi_ftlm_run with the number of R-vector blocks kept per sector: 3 (H q in
  * its own block), 2 (in-place recurrence: H q accumulated into the previous
  * vector block, so R can double at the same device-memory footprint), or 0 =
- * three when they fit in free device memory, else two (what qsi_ftlm_run
- * does).  Both layouts give the same recurrences up to rounding. */
+ * what qsi_ftlm_run does: two when every sector takes the one-launch FP32
+ * sector apply (whose two-block step moves fewer bytes), else three when they
+ * fit in free device memory, else two.  Both layouts give the same
+ * recurrences up to rounding. */
 qsi_status qsi_ftlm_run_blocks(qsi_op** ops, int32_t n_sectors, const int32_t* R,
                                int32_t M, uint64_t seed, int32_t precision,
                                int32_t blocks, double* alphas, double* betas);

@@ -541,6 +541,10 @@ class OperatorFamily:
         op._family = self  # the family outlives its members
         return op
 
+    def set_min_rows(self, min_rows: int) -> None:
+        """Bases below min_rows states run each member's apply at once instead of batching (0: always batch)."""
+        call("qsi_family_set_min_rows", self._h, int(min_rows))
+
     def stats(self) -> dict:
         b, a = C.c_int64(), C.c_int64()
         call("qsi_family_stats", self._h, C.byref(b), C.byref(a))

@@ -682,44 +682,50 @@ __global__ void k_hash_clear(HashSlot* slots, uint64_t n_slots) {
     }
 }
 
-__global__ void k_hash_insert(const state2* __restrict__ states, int64_t n, HashSlot* slots, uint64_t mask,
+__global__ void k_hash_insert(const state2* __restrict__ states, int64_t n, HashView H, HashSlot* slots,
                               int* overflow) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const state2 s = states[i];
-        uint64_t p = state_mix(s.x, s.y) & mask;
+        const HashSlot* creg;
+        const uint64_t cap = hash_region(H, s.x, s.y, creg);
+        HashSlot* reg = slots + (creg - H.slots);
+        uint64_t off = cap ? region_first(s.x, s.y, cap) : 0;
         bool done = false;
-        for (uint64_t probe = 0; probe <= mask; ++probe) {
-            if (atomicCAS(&slots[p].idx, kEmpty, (uint32_t)i) == kEmpty) {
-                slots[p].lo = s.x;
-                slots[p].hi = (uint32_t)s.y;
+        for (uint64_t probe = 0; probe < cap; ++probe) {
+            if (atomicCAS(&reg[off].idx, kEmpty, (uint32_t)i) == kEmpty) {
+                reg[off].lo = s.x;
+                reg[off].hi = (uint32_t)s.y;
                 done = true;
                 break;
             }
-            p = (p + 1) & mask;
+            off = (off + 1 == cap) ? 0 : off + 1;
         }
         if (!done) atomicOr(overflow, 1);
     }
 }
 
+// The regional hash index over the basis's current bucket table (built again whenever the table is): 2n slots.
 qsi_status build_hash(qsi_basis* b) {
     if (b->hb >= 96) return fail(QSI_INVALID_ARG, "hash index needs states of at most 96 bits");
-    uint64_t cap = 1;
-    while (cap < (uint64_t)b->n * 2) cap <<= 1;
-    if (cap < 1024) cap = 1024;
-    if (b->d_hash) cudaFree(b->d_hash);
-    b->d_hash = nullptr;
-    QSI_CUDA(cudaMalloc(&b->d_hash, cap * sizeof(HashSlot)));
-    b->hash_mask = cap - 1;
+    if (b->n >= ((int64_t)1 << 31)) return fail(QSI_INVALID_ARG, "hash index needs fewer than 2^31 states");
+    const uint64_t n_slots = 2 * (uint64_t)b->n;
+    if (!b->d_hash || b->hash_slots != n_slots) {
+        if (b->d_hash) cudaFree(b->d_hash);
+        b->d_hash = nullptr;
+        b->hash_slots = 0;
+        QSI_CUDA(cudaMalloc(&b->d_hash, n_slots * sizeof(HashSlot)));
+        b->hash_slots = n_slots;
+    }
     int* d_over = nullptr;
     QSI_CUDA(cudaMalloc(&d_over, sizeof(int)));
     QSI_CUDA(cudaMemset(d_over, 0, sizeof(int)));
-    k_hash_clear<<<grid_for((int64_t)cap, 256), 256>>>(b->d_hash, cap);
-    k_hash_insert<<<grid_for(b->n, 256), 256>>>(b->d_states, b->n, b->d_hash, b->hash_mask, d_over);
+    k_hash_clear<<<grid_for((int64_t)n_slots, 256), 256>>>(b->d_hash, n_slots);
+    k_hash_insert<<<grid_for(b->n, 256), 256>>>(b->d_states, b->n, b->hview(), b->d_hash, d_over);
     int over = 0;
     cudaError_t e = cudaMemcpy(&over, d_over, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(d_over);
     if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "hash build: %s", cudaGetErrorString(e));
-    if (over) return fail(QSI_CUDA_ERROR, "hash build: table overflow");
+    if (over) return fail(QSI_CUDA_ERROR, "hash build: a state found no slot in its region");
     return QSI_OK;
 }
 

@@ -145,30 +145,26 @@ extern "C" qsi_status qsi_op_autotune(qsi_op* op, const void* x, void* y, int32_
                           cfg.use_hash, cfg.grid_bps, cfg.vec_chunk, cfg.list_cap, best);
             T.log += line;
         }
-        // lookup: hash, or the bucket table (QSI_TUNE_INDEX: at widths around the current one; QSI_TUNE_LOOKUP:
-        // at the current width, leaving the basis as it is)
+        // lookup: bisection over the bucket table or the regional hash, whose regions are the table's buckets
+        // (QSI_TUNE_INDEX: both at widths around the current one; QSI_TUNE_LOOKUP: at the current width, leaving
+        // the basis as it is).  code = 2 * bits + (1 for the hash).
         if (s == QSI_OK && (flags & (QSI_TUNE_INDEX | QSI_TUNE_LOOKUP))) {
             qsi_basis* b = op->basis;
             const int b0 = b->bits;
-            const int hash0 = cfg.use_hash && b->d_hash ? 1 : 0;
-            // code: 0 = hash, k > 0 = table of k bits
-            int best_code = hash0 ? 0 : b0;
+            const bool can_hash = b->d_hash != nullptr;
+            const int hash0 = cfg.use_hash && can_hash ? 1 : 0;
+            int best_code = 2 * b0 + hash0;
             std::vector<int> codes;
-            if (b->d_hash) codes.push_back(0);
             for (int d = -4; d <= 4; d += 2) {
                 const int bits = b0 + d;
-                if ((flags & QSI_TUNE_INDEX) || d == 0)
-                    if (bits >= 8 && bits <= std::min(31, b->hb + 1)) codes.push_back(bits);
+                if (!((flags & QSI_TUNE_INDEX) || d == 0) || bits < 8 || bits > std::min(31, b->hb + 1)) continue;
+                codes.push_back(2 * bits);
+                if (can_hash) codes.push_back(2 * bits + 1);
             }
-            s = T.sweep("index(0=hash,k=table bits)", codes, best_code, best, [&](int code) -> qsi_status {
-                if (code == 0) {
-                    cfg.use_hash = 1;
-                    return QSI_OK;
-                }
-                cfg.use_hash = 0;
-                return qsi_basis_index(b, b->d_hash ? 1 : 0, code);
+            s = T.sweep("index(2*bits+hash)", codes, best_code, best, [&](int code) -> qsi_status {
+                cfg.use_hash = code & 1;
+                return qsi_basis_index(b, can_hash ? 1 : 0, code >> 1);
             });
-            if (s == QSI_OK && best_code == 0 && b->bits != b0) s = qsi_basis_index(b, 1, b0);  // table as found
         }
         const bool v4 = dtype == QSI_F32 && R > 1 && op->ff_accumulate && R >= 16 && (R & 3) == 0 &&
                         (R <= 128 ? (R & (R - 1)) == 0 : (R & 127) == 0);

@@ -11,6 +11,8 @@
 //
 // The queue is ready when it holds an apply of every live member (up to max_cols), or when its oldest entry has
 // waited a quarter of the last batch's duration (members spend the time between applies in their dot products).
+// Bases below kFamilyDirectRows states are not batched: their applies take about a kernel launch, less than the
+// queueing would cost, and each member's column runs at once on its own stream.
 // One column runs the single-vector family kernel and several the batched one; both sum a row in the same order
 // with the same coefficients and diagonal, so a request's results are bitwise the same alone and in any mix.
 //
@@ -35,6 +37,7 @@ struct qsi_family {
     std::vector<int32_t> cls;      // class of every term
     int n_cls = 0;
     int max_cols = 8;
+    int64_t min_rows = 0;          // bases below this many states run members' applies directly
     // batcher
     std::mutex mu;
     std::condition_variable cv;
@@ -67,6 +70,7 @@ namespace qsi {
 namespace {
 
 constexpr int kMaxFamilyClasses = 16;
+constexpr int64_t kFamilyDirectRows = 1 << 17;  // default: bases below this many states are not batched
 
 // X[i][c] = x_c[i] for the batch's columns
 __global__ void k_gather_columns(const double* const* __restrict__ xs, int R, int64_t n, double* __restrict__ X) {
@@ -138,6 +142,16 @@ qsi_status run_batch(qsi_family* f, const std::vector<qsi_family::Req*>& batch) 
 
 qsi_status family_apply(qsi_op* op, const double* x, double* y, int accumulate, cudaStream_t st) {
     qsi_family* f = op->family;
+    if (f->basis->n < f->min_rows) {
+        // a small basis: an apply takes about a launch, so waiting for partners would cost more than the
+        // lookups a batch shares; the member's own column runs at once on its stream (same kernel, same sums)
+        qsi_status s = launch_family(f->tmpl, x, y, 1, op->d_fcoef, accumulate, st);
+        if (s != QSI_OK) return s;
+        std::lock_guard<std::mutex> lk(f->mu);
+        ++f->batches;
+        ++f->served;
+        return QSI_OK;
+    }
     QSI_CUDA(cudaStreamSynchronize(st));  // x (and y when accumulating) are ready
     qsi_family::Req r{op, x, y, accumulate};
     r.arrival = std::chrono::steady_clock::now();
@@ -168,7 +182,7 @@ qsi_status family_apply(qsi_op* op, const double* x, double* y, int accumulate, 
             const auto dt = std::chrono::steady_clock::now() - t0;
             lk.lock();
             f->window = std::min<std::chrono::steady_clock::duration>(
-                std::max<std::chrono::steady_clock::duration>(dt / 4, std::chrono::microseconds(50)),
+                std::max<std::chrono::steady_clock::duration>(dt / 4, std::chrono::microseconds(5)),
                 std::chrono::milliseconds(20));
             ++f->batches;
             f->served += (int64_t)batch.size();
@@ -179,8 +193,10 @@ qsi_status family_apply(qsi_op* op, const double* x, double* y, int accumulate, 
             }
             f->running = false;
             f->cv.notify_all();
+        } else if (!f->running && !f->pending.empty()) {
+            f->cv.wait_until(lk, f->pending.front()->arrival + f->window);  // until the oldest entry's window ends
         } else {
-            f->cv.wait_for(lk, std::chrono::microseconds(50));
+            f->cv.wait_for(lk, std::chrono::milliseconds(5));  // a batch runs, or this entry was taken: notified
         }
     }
     if (r.status != QSI_OK) return fail(r.status, "family batch: %s", r.error.c_str());
@@ -211,6 +227,7 @@ extern "C" qsi_status qsi_family_create(qsi_basis* b, const qsi_term* terms, int
         f->cls.assign(term_class, term_class + n_terms);
         f->n_cls = n_classes;
         f->max_cols = max_cols;
+        f->min_rows = kFamilyDirectRows;
         std::vector<qsi_term> tt(f->terms);
         for (int t = 0; t < n_terms; ++t) {
             if (f->cls[t] < 0 || f->cls[t] >= n_classes) {
@@ -242,6 +259,13 @@ extern "C" qsi_status qsi_family_create(qsi_basis* b, const qsi_term* terms, int
         *out = f;
         return QSI_OK;
     });
+}
+
+extern "C" qsi_status qsi_family_set_min_rows(qsi_family* f, int64_t min_rows) {
+    if (!f || min_rows < 0) return fail(QSI_INVALID_ARG, "qsi_family_set_min_rows: bad argument");
+    std::lock_guard<std::mutex> lk(f->mu);
+    f->min_rows = min_rows;
+    return QSI_OK;
 }
 
 extern "C" qsi_status qsi_family_destroy(qsi_family* f) {

@@ -11,8 +11,12 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <random>
+#include <string>
 #include <vector>
 
 #include "h5lite.h"
@@ -468,6 +472,31 @@ __global__ void k_residual(const double* __restrict__ HX, const double* __restri
         for (int i = 0; i < k; ++i) R[(size_t)i * n + r] = HX[(size_t)i * n + r] - th[i] * X[(size_t)i * n + r];
 }
 
+// Wall time per phase of a solver, printed to stderr at the end when the environment sets QSI_TRACE (each mark
+// then synchronises the stream, so a traced run is slower; without QSI_TRACE a mark does nothing).
+struct PhaseClock {
+    cudaStream_t st;
+    const char* name;
+    bool on = std::getenv("QSI_TRACE") != nullptr;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    std::map<std::string, std::pair<double, int>> acc;
+    void mark(const char* phase) {
+        if (!on) return;
+        cudaStreamSynchronize(st);
+        const auto now = std::chrono::steady_clock::now();
+        auto& a = acc[phase];
+        a.first += std::chrono::duration<double>(now - t).count();
+        a.second += 1;
+        t = now;
+    }
+    ~PhaseClock() {
+        if (!on) return;
+        for (auto& kv : acc)
+            std::fprintf(stderr, "[qsi trace] %s %-14s %9.3f s %6d marks\n", name, kv.first.c_str(), kv.second.first,
+                         kv.second.second);
+    }
+};
+
 // FP64 polish of the Ritz block X (nev FP64 vectors, vector-major, Ritz values th): Rayleigh-Ritz on X, then
 // `rounds - 1` Rayleigh-Ritz steps on [X, HX - X theta]; then the residual report and the solver's outputs.
 static qsi_status finish_solve(qsi_op* op, const qsi_lanczos_cfg& cfg, Vecs& vx, DevBuf<double>& X, DevBuf<double>& HX,
@@ -583,11 +612,14 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     int64_t applies = 0;
     int restarts = 0, nconv = 0;
     std::vector<double> Tw, TY;
+    PhaseClock clk{st, sizeof(VT) == 4 ? "trlan-f32" : "trlan-f64"};
     for (;;) {
         for (int j = k; j < m; ++j) {
+            clk.mark("setup/host");
             s = apply_to_w<VT>(op, vec(j), w.p, st);
             if (s) return s;
             ++applies;
+            clk.mark("apply");
             // full reorthogonalisation: classical Gram-Schmidt against v_0..v_j, repeated once
             // when the norm drops by more than 1/sqrt(2) (DGKS criterion)
             s = vx.dots<VT>(V.p, n, j + 1, w.p, h);
@@ -623,6 +655,7 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
             beta[j] = b;
             QSI_CUDA(cudaMemcpyAsync(vx.red, &nrm2, 8, cudaMemcpyHostToDevice, st));
             k_scale_store<VT><<<grid_for(n, 256), 256, 0, st>>>(w.p, vx.red, vec(j + 1), n);
+            clk.mark("orthogonalise");
         }
         // projected matrix: arrowhead (kept Ritz values + couplings) then tridiagonal
         std::vector<double> T((size_t)m * m, 0.0);
@@ -634,8 +667,10 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
             T[(size_t)j * m + j] = alpha[j];
             if (j + 1 < m) T[(size_t)j * m + j + 1] = T[(size_t)(j + 1) * m + j] = beta[j];
         }
+        clk.mark("setup/host");
         s = jacobi_eigh(T, m, 1, Tw, TY, st);
         if (s) return s;
+        clk.mark("ritz");
         const double bl = beta[m - 1];
         nconv = 0;
         for (int i = 0; i < nev; ++i) {
@@ -661,6 +696,7 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
         for (int i = 0; i < knew; ++i) coup[i] = bl * TY[(size_t)(m - 1) * m + i];
         k = knew;
         QSI_CUDA(cudaGetLastError());
+        clk.mark("restart");
     }
     // Ritz vectors in FP64
     DevBuf<double> X, HX;
@@ -679,8 +715,11 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     std::vector<double> th(Tw.begin(), Tw.begin() + nev);
     // free the Krylov basis before polishing
     V.release();
-    return finish_solve(op, cfg, vx, X, HX, th, nev, std::max(cfg.polish_steps, sizeof(VT) == 4 ? 1 : 0), applies,
-                        nconv, restarts, m >= n, t0, evals, evecs, rep);
+    clk.mark("ritz vectors");
+    s = finish_solve(op, cfg, vx, X, HX, th, nev, std::max(cfg.polish_steps, sizeof(VT) == 4 ? 1 : 0), applies, nconv,
+                     restarts, m >= n, t0, evals, evecs, rep);
+    clk.mark("polish");
+    return s;
 }
 
 // ------------------------------------------------------------------ block thick-restart Lanczos (FP32 blocks)
@@ -933,6 +972,7 @@ static qsi_status btrlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, 
     if (s) return s;
     const int64_t n = B.n;
     cudaStream_t st = B.st;
+    PhaseClock clk{st, "btrlan"};
     const int nev = std::max(1, cfg.nev);
     const int keep = ((nev + std::max(nev, 6) + kBlk - 1) / kBlk) * kBlk;  // kept Ritz vectors, whole blocks
     const int kb = keep / kBlk;
@@ -966,11 +1006,14 @@ static qsi_status btrlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, 
     uint64_t breakdowns = 0;
     for (;;) {
         for (int j = k0; j < nblk; ++j) {
+            clk.mark("setup/host");
             s = launch_apply(op, Q[j], W, kBlk, QSI_F32, 0, st);
             if (s) return s;
             applies += kBlk;
+            clk.mark("apply");
             s = B.orthogonalise(Q.data(), j + 1, W, C);
             if (s) return s;
+            clk.mark("orthogonalise");
             // projected matrix column block j: T[0 .. 16(j+1), 16j .. 16j+16) = C, mirrored; its diagonal block
             // symmetrised
             for (int r = 0; r < (j + 1) * kBlk; ++r)
@@ -982,6 +1025,7 @@ static qsi_status btrlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, 
                 }
             s = B.cholqr(W, Q[j + 1], R, ok);
             if (s) return s;
+            clk.mark("cholqr");
             if (!ok) {  // the Krylov space became invariant: continue from random directions orthogonal to it
                 ++breakdowns;
                 for (int attempt = 0; attempt < 4 && !ok; ++attempt) {
@@ -1003,8 +1047,10 @@ static qsi_status btrlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, 
                 Blast = R;
             }
         }
+        clk.mark("setup/host");
         s = jacobi_eigh(T, m, 1, Tw, TY, st);
         if (s) return s;
+        clk.mark("ritz");
         // residual of Ritz pair i: || Blast y_last,i ||, y_last,i = the last block's components
         std::vector<double> res(m, 0.0);
         for (int i = 0; i < m; ++i) {
@@ -1030,6 +1076,7 @@ static qsi_status btrlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, 
         float* outs[2] = {W, spare};
         s = B.combine(Q.data(), nblk, Yk, kb, outs, 0);
         if (s) return s;
+        clk.mark("restart");
         // new basis: the Ritz blocks, then the residual block; every other buffer returns to the pool
         float* res_blk = Q[nblk];
         std::vector<float*> pool;
@@ -1063,8 +1110,11 @@ static qsi_status btrlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, 
     Vecs vx;
     s = vx.init(n, st);
     if (s) return s;
-    return finish_solve(op, cfg, vx, X, HX, th, nev, std::max(cfg.polish_steps, 1), applies, nconv, restarts, false, t0,
-                        evals, evecs, rep);
+    clk.mark("ritz vectors");
+    s = finish_solve(op, cfg, vx, X, HX, th, nev, std::max(cfg.polish_steps, 1), applies, nconv, restarts, false, t0,
+                     evals, evecs, rep);
+    clk.mark("polish");
+    return s;
 }
 
 // ------------------------------------------------------------------ eigval0 (mfeig0)
@@ -1838,6 +1888,124 @@ __global__ void k_col_scale(VT* __restrict__ v, const double* __restrict__ inv, 
     }
 }
 
+// The two-block recurrence's column work in two passes instead of three (FP32 storage, sector launch).  One
+// read of C and P gives <C, P>, |P|^2 and |C|^2 per column; with alpha = <C, P> the norm of P - alpha C follows
+// without another pass, |P - alpha C|^2 = |P|^2 - 2 alpha <C, P> + alpha^2 |C|^2, and a second pass writes
+// (P - alpha C) / beta.  The subtraction in that formula loses (alpha / beta)^2 times the sums' relative rounding
+// (double-float, about 2^-46), far below the FP32 storage of the vectors.
+template <int VW>
+__global__ void __launch_bounds__(256) k_col_dots3(const float* __restrict__ c, const float* __restrict__ p, int64_t n,
+                                                   int R, double* __restrict__ partial) {
+    __shared__ double sh[256 * VW];
+    const ColLayout L = ColLayout::make<VW>(n, R);
+    F2 cp[VW], pp[VW], cc[VW];
+#pragma unroll
+    for (int k = 0; k < VW; ++k) cp[k] = pp[k] = cc[k] = F2{0.f, 0.f};
+    for (int64_t i = L.i0 + L.sub; i < L.i1; i += (int64_t)L.rpp * kColUnroll) {
+        float cv[kColUnroll][VW], pv[kColUnroll][VW];
+#pragma unroll
+        for (int u = 0; u < kColUnroll; ++u) {
+            const int64_t ii = i + (int64_t)u * L.rpp;
+            if (ii < L.i1) {
+                load_vec<float, VW>(c + ii * R + L.c0, cv[u]);
+                load_vec<float, VW>(p + ii * R + L.c0, pv[u]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < VW; ++k) cv[u][k] = pv[u][k] = 0.f;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kColUnroll; ++u)
+#pragma unroll
+            for (int k = 0; k < VW; ++k) {
+                f2_fma(cp[k], cv[u][k], 0.f, pv[u][k]);
+                f2_fma(pp[k], pv[u][k], 0.f, pv[u][k]);
+                f2_fma(cc[k], cv[u][k], 0.f, cv[u][k]);
+            }
+    }
+    const int64_t stride = (int64_t)gridDim.x * R;
+    double res[VW];
+#pragma unroll
+    for (int k = 0; k < VW; ++k) res[k] = f2_value(cp[k]);
+    col_block_sum<VW>(L, res, R, sh, partial);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < VW; ++k) res[k] = f2_value(pp[k]);
+    col_block_sum<VW>(L, res, R, sh, partial + stride);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < VW; ++k) res[k] = f2_value(cc[k]);
+    col_block_sum<VW>(L, res, R, sh, partial + 2 * stride);
+}
+
+// alpha = <C, P>, beta = |P - alpha C| from k_col_dots3's partial sums (summed over blocks in block order), with
+// 1/beta as FP64 and as a (hi, lo) float pair, and -beta as a float pair (the next step's accumulate coefficient).
+__global__ void k_ftlm_coef3(const double* __restrict__ partial, int nblocks, int R, double* __restrict__ alpha,
+                             double* __restrict__ beta, double* __restrict__ inv, float2* __restrict__ inv_ff,
+                             float2* __restrict__ neg_ff) {
+    const int64_t stride = (int64_t)nblocks * R;
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        double cp = 0.0, pp = 0.0, cc = 0.0;
+        for (int b = 0; b < nblocks; ++b) {
+            cp += partial[(int64_t)b * R + r];
+            pp += partial[stride + (int64_t)b * R + r];
+            cc += partial[2 * stride + (int64_t)b * R + r];
+        }
+        const double a = cp;
+        const double b2 = pp - 2.0 * a * cp + a * a * cc;
+        const double b = b2 > 0.0 ? sqrt(b2) : 0.0;
+        alpha[r] = a;
+        beta[r] = b;
+        const double v = b > 0 ? 1.0 / b : 1.0;
+        const float h = (float)v;
+        inv[r] = v;
+        inv_ff[r] = make_float2(h, (float)(v - (double)h));
+        const float nh = (float)(-b);
+        neg_ff[r] = make_float2(nh, (float)(-b - (double)nh));
+    }
+}
+
+// prev <- (prev - alpha cur) / beta per column, in double-float, rounded to FP32 once.
+template <int VW>
+__global__ void __launch_bounds__(256) k_ftlm_update_scaled(float* __restrict__ prev, const float* __restrict__ cur,
+                                                            const double* __restrict__ alpha,
+                                                            const float2* __restrict__ inv_ff, int64_t n, int R) {
+    const ColLayout L = ColLayout::make<VW>(n, R);
+    float ah[VW], al[VW], ih[VW], il[VW];
+#pragma unroll
+    for (int k = 0; k < VW; ++k) {
+        const double a = alpha[L.c0 + k];
+        ah[k] = (float)(-a), al[k] = (float)(-a - (double)ah[k]);
+        ih[k] = inv_ff[L.c0 + k].x, il[k] = inv_ff[L.c0 + k].y;
+    }
+    for (int64_t i = L.i0 + L.sub; i < L.i1; i += (int64_t)L.rpp * kColUnroll) {
+        float cv[kColUnroll][VW], pv[kColUnroll][VW];
+#pragma unroll
+        for (int u = 0; u < kColUnroll; ++u) {
+            const int64_t ii = i + (int64_t)u * L.rpp;
+            if (ii < L.i1) {
+                load_vec<float, VW>(cur + ii * R + L.c0, cv[u]);
+                load_vec<float, VW>(prev + ii * R + L.c0, pv[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kColUnroll; ++u) {
+            const int64_t ii = i + (int64_t)u * L.rpp;
+            if (ii >= L.i1) continue;
+            float out[VW];
+#pragma unroll
+            for (int k = 0; k < VW; ++k) {
+                F2 v{pv[u][k], 0.f};
+                f2_fma(v, ah[k], al[k], cv[u][k]);  // v = prev - alpha cur
+                const float w = v.hi * ih[k];
+                const float e = fmaf(v.hi, ih[k], -w) + (v.hi * il[k] + v.lo * ih[k]);
+                out[k] = w + e;
+            }
+            store_vec<float, VW>(prev + ii * R + L.c0, out);
+        }
+    }
+}
+
 constexpr int kColGrid = 1024;
 
 template <typename VT>
@@ -1859,9 +2027,11 @@ struct FtlmSector {
 // Two blocks (blocks == 2, or blocks == 0 when three do not fit in free device memory), the in-place
 // recurrence with P holding q_prev at the start of a step:
 //   P <- H C - beta_prev P;  alpha = <C, P>;  P <- P - alpha C;  beta = |P|;  P /= beta;  swap(P, C).
-// The one-launch sector apply takes -beta_prev per column as its accumulate coefficient (double-float); the
-// per-sector launches instead have the column pass also scale C by -beta for the next step.  R can double at
-// the same footprint; the in-launch form moves as many blocks per step as the three-block one.
+// The one-launch sector apply takes -beta_prev per column as its accumulate coefficient (double-float), and its
+// column work is two passes (k_col_dots3: <C, P>, |P|^2 and |C|^2 in one read; k_ftlm_update_scaled:
+// P <- (P - alpha C) / beta), so a step moves 6 blocks beyond the apply's gathers against 9 for three blocks: the
+// one-launch form always takes two blocks unless three are asked for.  The per-sector launches instead have the
+// column pass also scale C by -beta for the next step, and take three blocks when they fit.
 template <typename VT>
 static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint64_t seed, double* alphas,
                            double* betas, int blocks) {
@@ -1874,11 +2044,12 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
         if (R <= 0 || R > 256 || (R & (R - 1))) return fail(QSI_INVALID_ARG, "ftlm: R must be a power of two in [1,256]");
         if (ops[s]->basis->n < 1) return fail(QSI_INVALID_ARG, "ftlm: empty sector");
         block_bytes += (size_t)ops[s]->basis->n * R * sizeof(VT);
+        one_launch = one_launch && ops[s]->kernel == 1 && ops[s]->ff_accumulate;
     }
-    if (blocks == 0) {  // three blocks when they fit with 4 GiB to spare, else two
+    if (blocks == 0) {  // one launch: two blocks; else three blocks when they fit with 4 GiB to spare, else two
         size_t free_b = 0, total_b = 0;
         QSI_CUDA(cudaMemGetInfo(&free_b, &total_b));
-        blocks = (3 * block_bytes + ((size_t)4 << 30) <= free_b) ? 3 : 2;
+        blocks = (!one_launch && 3 * block_bytes + ((size_t)4 << 30) <= free_b) ? 3 : 2;
     }
     if (blocks != 2 && blocks != 3) return fail(QSI_INVALID_ARG, "ftlm: blocks must be 0, 2 or 3");
     const bool two = (blocks == 2);
@@ -1890,14 +2061,12 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
         QSI_CUDA(S[s].P.alloc((size_t)S[s].n * R, st));
         QSI_CUDA(S[s].C.alloc((size_t)S[s].n * R, st));
         if (!two) QSI_CUDA(S[s].W.alloc((size_t)S[s].n * R, st));
-        QSI_CUDA(S[s].partial.alloc((size_t)kColGrid * R, st));
+        QSI_CUDA(S[s].partial.alloc((size_t)3 * kColGrid * R, st));  // three dots per column (k_col_dots3)
         QSI_CUDA(S[s].ab.alloc((size_t)2 * M * R, st));
         QSI_CUDA(S[s].inv.alloc((size_t)R, st));
         QSI_CUDA(S[s].inv_ff.alloc((size_t)R, st));
         QSI_CUDA(S[s].nbeta_ff.alloc((size_t)R, st));
         QSI_CUDA(cudaMemsetAsync(S[s].nbeta_ff.p, 0, (size_t)R * sizeof(float2), st));
-        one_launch = one_launch && ops[s]->kernel == 1 &&
-                     ops[s]->ff_accumulate;
         k_ftlm_init<VT><<<grid_for(S[s].n * R, 256), 256, 0, st>>>(S[s].C.p, S[s].P.p, S[s].n, R, seed + (uint64_t)s);
     }
     std::vector<VT*> prev(ns), cur(ns);
@@ -1975,6 +2144,18 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
             double* beta = dB + (size_t)j * F.R;
             auto col_step = [&](auto vw) {
                 constexpr int VW = decltype(vw)::value;
+                if constexpr (sizeof(VT) == 4) {
+                    if (one_launch && two) {  // two passes: three dots, then (P - alpha C) / beta
+                        const float* c = reinterpret_cast<const float*>(cur[s]);
+                        float* p = reinterpret_cast<float*>(prev[s]);
+                        k_col_dots3<VW><<<kColGrid, blk, 0, st>>>(c, p, F.n, F.R, F.partial.p);
+                        k_ftlm_coef3<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dA + (size_t)j * F.R, beta,
+                                                        F.inv.p, F.inv_ff.p, F.nbeta_ff.p);
+                        k_ftlm_update_scaled<VW><<<kColGrid, blk, 0, st>>>(p, c, dA + (size_t)j * F.R, F.inv_ff.p,
+                                                                           F.n, F.R);
+                        return;
+                    }
+                }
                 k_col_dots<VT, VW><<<kColGrid, blk, 0, st>>>(cur[s], two ? prev[s] : F.W.p, F.n, F.R, F.partial.p);
                 k_col_reduce<<<1, 256, 0, st>>>(F.partial.p, kColGrid, F.R, dA + (size_t)j * F.R, 0);
                 if (two)

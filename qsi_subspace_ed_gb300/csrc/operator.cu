@@ -372,6 +372,7 @@ extern "C" qsi_status qsi_basis_create(const uint64_t* lohi, int64_t n, int32_t 
             if (build_hash(b) != QSI_OK) {
                 if (b->d_hash) cudaFree(b->d_hash);
                 b->d_hash = nullptr;
+                b->hash_slots = 0;
                 cudaGetLastError();
             }
         }
@@ -811,11 +812,21 @@ extern "C" qsi_status qsi_basis_index(qsi_basis* b, int32_t use_hash, int32_t bu
             qsi_status bs = build_buckets(b);
             if (bs != QSI_OK) return bs;
             QSI_CUDA(cudaDeviceSynchronize());
+            if (b->d_hash) {  // the hash's regions are the table's buckets
+                if (!use_hash) {
+                    cudaFree(b->d_hash);
+                    b->d_hash = nullptr;
+                    b->hash_slots = 0;
+                    return QSI_OK;
+                }
+                return build_hash(b);
+            }
         }
         if (use_hash && !b->d_hash) return build_hash(b);
         if (!use_hash && b->d_hash) {
             cudaFree(b->d_hash);
             b->d_hash = nullptr;
+            b->hash_slots = 0;
         }
         return QSI_OK;
     });
@@ -827,7 +838,7 @@ extern "C" qsi_status qsi_basis_info(const qsi_basis* b, int32_t* bucket_bits, i
     if (has_hash) *has_hash = b->d_hash != nullptr;
     if (index_bytes)
         *index_bytes = (int64_t)(bucket_table_entries(b->n_buckets) * 4 +
-                                 (b->d_hash ? (b->hash_mask + 1) * sizeof(HashSlot) : 0));
+                                 (b->d_hash ? b->hash_slots * sizeof(HashSlot) : 0));
     return QSI_OK;
 }
 

@@ -55,9 +55,8 @@ struct BasisView {
     uint32_t n_buckets;
 };
 
-// Open-addressing index of the basis (states of at most 96 bits): slot =
-// {low word, high 32 bits, position in the sorted basis}; idx == kEmpty marks a
-// free slot.  Linear probing from mix(state); built once per basis.
+// Slot of the basis hash index (states of at most 96 bits): {low word, high 32 bits, position in the sorted
+// basis}; idx == kEmpty marks a free slot.
 struct HashSlot {
     uint64_t lo;
     uint32_t hi;
@@ -73,10 +72,6 @@ __host__ __device__ __forceinline__ uint64_t state_mix(uint64_t lo, uint64_t hi)
     return h;
 }
 
-struct HashView {
-    const HashSlot* slots;
-    uint64_t mask;
-};
 
 __device__ __forceinline__ bool less128(uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi) {
     return ahi < bhi || (ahi == bhi && alo < blo);
@@ -137,16 +132,53 @@ __device__ __forceinline__ int64_t basis_find(const BasisView& B, uint64_t lo, u
     return (seen && e.x == lo && e.y == hi) ? (int64_t)a : -1;
 }
 
-// Exact position of (lo, hi) through the hash index, or -1.  The probe count
-// is bounded by the table size (the table always has free slots).
+// Regional hash index of the basis: bucket v of the top-bits table owns the slots [2 bstart[v], 2 bstart[v+1])
+// of a table of 2n slots.  A state's probe starts at a hash of the state scaled to its bucket's slots and
+// continues linearly, wrapping inside them.  The regions keep the locality of the sorted basis (the columns of
+// neighbouring rows fall in the same few regions, whose slots stay in L2), and at the fixed load factor of 1/2 a
+// lookup takes about 1.5 probes whatever its bucket's size, where a bisection takes log2 of it (the buckets of
+// spin-ice bases are very uneven: on the 96-spin 12.12.12.12 sector a state's 30-bit bucket holds 18.7 states on
+// average).  One 16-byte load of the table gives the region, as for the bisection.
+struct HashView {
+    const HashSlot* slots;
+    BasisView B;
+};
+
+// First probe of (lo, hi) in a region of cap slots.
+__device__ __forceinline__ uint32_t region_first(uint64_t lo, uint64_t hi, uint64_t cap) {
+    return (uint32_t)(((state_mix(lo, hi) >> 32) * cap) >> 32);
+}
+
+// Region of (lo, hi): its first slot and size (0: the state's bucket is empty or out of range, or the state has
+// more than 96 bits, so it is not in the basis).
+__device__ __forceinline__ uint64_t hash_region(const HashView& Hv, uint64_t lo, uint64_t hi, const HashSlot*& reg) {
+    reg = Hv.slots;
+    if (hi >> 32) return 0;
+    bool ok;
+    const uint64_t v = bucket_of(Hv.B, lo, hi, ok);
+    if (!ok) return 0;
+    uint32_t a, b;
+    bucket_bounds(Hv.B, v, a, b);
+    reg = Hv.slots + 2 * (uint64_t)a;
+    return 2 * (uint64_t)(b - a);
+}
+
+__device__ __forceinline__ bool slot_holds(const uint4& e, uint64_t lo, uint64_t hi) {
+    return e.x == (uint32_t)lo && e.y == (uint32_t)(lo >> 32) && e.z == (uint32_t)hi;
+}
+
+// Exact position of (lo, hi) through the hash index, or -1.  A region is never full (load 1/2), so the probes
+// end at a free slot at the latest.
 __device__ __forceinline__ int64_t hash_find(const HashView& Hv, uint64_t lo, uint64_t hi) {
-    if (hi >> 32) return -1;
-    uint64_t s = state_mix(lo, hi) & Hv.mask;
-    for (uint64_t probe = 0; probe <= Hv.mask; ++probe) {
-        const uint4 e = __ldg(reinterpret_cast<const uint4*>(Hv.slots + s));
+    const HashSlot* reg;
+    const uint64_t cap = hash_region(Hv, lo, hi, reg);
+    if (!cap) return -1;
+    uint64_t off = region_first(lo, hi, cap);
+    for (uint64_t probe = 0; probe < cap; ++probe) {
+        const uint4 e = __ldg(reinterpret_cast<const uint4*>(reg + off));
         if (e.w == kEmpty) return -1;
-        if (e.x == (uint32_t)lo && e.y == (uint32_t)(lo >> 32) && e.z == (uint32_t)hi) return (int64_t)e.w;
-        s = (s + 1) & Hv.mask;
+        if (slot_holds(e, lo, hi)) return (int64_t)e.w;
+        off = (off + 1 == cap) ? 0 : off + 1;
     }
     return -1;
 }
@@ -170,36 +202,41 @@ struct LookupHash {
     HashView H;
     static constexpr int kNB = 4, kMinBlocks = 3;
     __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return hash_find(H, lo, hi); }
+    // every state's region (one table load each), then every first probe, before resolving any
     template <int NB>
     __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n) const {
-        uint64_t slot[NB];
+        const HashSlot* reg[NB];
+        uint32_t cap[NB], off[NB];
         uint4 e[NB];
 #pragma unroll
         for (int u = 0; u < NB; ++u) {
-            slot[u] = 0;
-            if (u < n) {
-                slot[u] = state_mix(lo[u], hi[u]) & H.mask;
-                e[u] = __ldg(reinterpret_cast<const uint4*>(H.slots + slot[u]));
+            cap[u] = 0;
+            reg[u] = H.slots;
+            if (u < n) cap[u] = (uint32_t)hash_region(H, lo[u], hi[u], reg[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            off[u] = 0;
+            e[u] = make_uint4(0, 0, 0, kEmpty);
+            if (cap[u]) {
+                off[u] = region_first(lo[u], hi[u], cap[u]);
+                e[u] = __ldg(reinterpret_cast<const uint4*>(reg[u] + off[u]));
             }
         }
 #pragma unroll
         for (int u = 0; u < NB; ++u) {
             if (u >= n) continue;
-            if (hi[u] >> 32) {
-                J[u] = -1;
-                continue;
-            }
-            uint64_t sl = slot[u];
-            uint4 v = e[u];
             int64_t r = -1;
-            for (uint64_t probe = 0; probe <= H.mask; ++probe) {
+            uint32_t o = off[u];
+            uint4 v = e[u];
+            for (uint32_t probe = 0; probe < cap[u]; ++probe) {
                 if (v.w == kEmpty) break;
-                if (v.x == (uint32_t)lo[u] && v.y == (uint32_t)(lo[u] >> 32) && v.z == (uint32_t)hi[u]) {
+                if (slot_holds(v, lo[u], hi[u])) {
                     r = (int64_t)v.w;
                     break;
                 }
-                sl = (sl + 1) & H.mask;
-                v = __ldg(reinterpret_cast<const uint4*>(H.slots + sl));
+                o = (o + 1 == cap[u]) ? 0 : o + 1;
+                v = __ldg(reinterpret_cast<const uint4*>(reg[u] + o));
             }
             J[u] = r;
         }

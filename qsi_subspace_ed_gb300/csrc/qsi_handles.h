@@ -12,10 +12,10 @@ struct qsi_basis {
     qsi::state2* d_states = nullptr;
     uint32_t* d_bstart = nullptr;
     int hb = 0;                        // highest bit used by any state
-    qsi::HashSlot* d_hash = nullptr;   // optional hash index (states <= 96 bits)
-    uint64_t hash_mask = 0;
+    qsi::HashSlot* d_hash = nullptr;   // optional regional hash index over the bucket table (states <= 96 bits)
+    uint64_t hash_slots = 0;           // 2n
     qsi::BasisView view() const { return qsi::BasisView{d_states, d_bstart, n, shift, n_buckets}; }
-    qsi::HashView hview() const { return qsi::HashView{d_hash, hash_mask}; }
+    qsi::HashView hview() const { return qsi::HashView{d_hash, view()}; }
 };
 
 // Launch settings of one class of applies (single vector, batched).  None of them changes results.

@@ -83,11 +83,13 @@ class RequestLoop:
     default to the device solve and ZBasis (both replaceable, e.g. by host-side fakes)."""
 
     def __init__(self, sectors: dict[str, Sector], slots: int = 4, hbm_budget: int = 200 << 30,
-                 solve: Callable | None = None, make_basis: Callable | None = None, batching: bool = True):
+                 solve: Callable | None = None, make_basis: Callable | None = None, batching: bool = True,
+                 min_batch_rows: int | None = None):
         self.sectors = sectors
         self.slots = slots
         self.budget = hbm_budget
         self.batching = batching and solve is None
+        self.min_batch_rows = min_batch_rows  # None: the family's default (small bases run their applies at once)
         self._solve = solve or self._solve_default
         self._make_basis = make_basis or ZBasis
         self._families: dict[str, OperatorFamily] = {}
@@ -181,8 +183,11 @@ class RequestLoop:
                     self._bases[req.sector] = basis
                     if self.batching:
                         cls, n_cls = ring_zeeman_classes(sec.lattice)
-                        self._families[req.sector] = OperatorFamily(
-                            basis, build_ring_zeeman(sec.lattice, [1.0] * 4, [0.0] * 3), cls, n_cls, self.slots)
+                        fam = OperatorFamily(basis, build_ring_zeeman(sec.lattice, [1.0] * 4, [0.0] * 3), cls, n_cls,
+                                             self.slots)
+                        if self.min_batch_rows is not None:
+                            fam.set_min_rows(self.min_batch_rows)
+                        self._families[req.sector] = fam
                     # stays resident and accounted for
                     self._in_use += basis_footprint(sec.dim, self.slots if self.batching else 0)
                 family = self._families.get(req.sector)

@@ -81,7 +81,8 @@ def ftlm(ops, R, M: int = 100, seed: int = 0, precision: str = "mixed", blocks: 
     """Batched FTLM Lanczos recurrences: R[s] Rademacher vectors per sector, M steps.
 
     blocks: R-vector blocks kept per sector, 3 (H q in its own block) or 2 (in-place recurrence, R can double at
-    the same device memory); 0 = three when they fit in free device memory, else two.
+    the same device memory); 0 = two when every sector takes the one-launch FP32 sector apply, else three when
+    they fit in free device memory, else two.
     Returns a list of (alphas (R[s], M), betas (R[s], M)) per sector.
     """
     ops = list(ops)

@@ -190,14 +190,20 @@ def test_kernel_variants_bit_identical(built, name):
         op.apply_batched(X, Y)
         bouts.append(Y)
     # narrow and wide bucket tables (buckets of thousands of states, and bucket numbers in every position of the
-    # table's groups of four)
+    # table's groups of four), with the bisection and with the regional hash, whose regions are the table's buckets
+    # and are rebuilt with it
     bits0 = b.index_info()["bucket_bits"]
     for bits in (8, 12, 31):
         b.set_index(use_hash=True, bucket_bits=bits)
-        op.set_kernel(1, 0)
-        y = np.zeros_like(x)
-        op.evaluate(x, y)
-        outs.append(y)
+        assert b.index_info()["hash"]
+        for use_hash in (0, 1):
+            op.set_kernel(1, use_hash)
+            y = np.zeros_like(x)
+            op.evaluate(x, y)
+            outs.append(y)
+            Y = np.zeros_like(X)
+            op.apply_batched(X, Y)
+            bouts.append(Y)
     b.set_index(use_hash=True, bucket_bits=bits0)
     op.set_kernel(1, 1)
     for y in outs[1:]:

@@ -37,6 +37,7 @@ def test_family_members_batch_bitwise_and_match_their_operators():
     b = q.ZBasis(lohi)
     cls, ncls = ring_zeeman_classes(lat)
     fam = q.OperatorFamily(b, q.build_ring_zeeman(lat, [1.0] * 4, [0.0] * 3), cls, ncls, max_cols=4)
+    fam.set_min_rows(0)  # batch this small basis too
     rng = np.random.default_rng(5)
     params = [(list(rng.uniform(0, 1, 4)), list(rng.uniform(-1, 1, 3))) for _ in range(4)]
     members = [fam.member(ring_zeeman_class_coefficients(g, B)) for g, B in params]
@@ -72,6 +73,30 @@ def test_family_members_batch_bitwise_and_match_their_operators():
     assert st["mean_columns"] > 1.0, st  # concurrent applies ran as batched columns
 
 
+def test_family_small_basis_runs_applies_directly():
+    """Below the family's row threshold (by default 131072) members' applies run at once, one column each, with
+    the results of batched runs."""
+    from qsi_subspace_ed_gb300.hamiltonian import ring_zeeman_class_coefficients, ring_zeeman_classes
+
+    lat = workloads.lattice("pyro_1x2x1")
+    lohi = q.enumerate_basis(lat)
+    b = q.ZBasis(lohi)
+    cls, ncls = ring_zeeman_classes(lat)
+    fam = q.OperatorFamily(b, q.build_ring_zeeman(lat, [1.0] * 4, [0.0] * 3), cls, ncls, max_cols=4)
+    m = fam.member(ring_zeeman_class_coefficients([0.3, 0.5, 0.7, 0.9], [0.1, -0.2, 0.3]))
+    x = np.random.default_rng(2).standard_normal(len(lohi))
+    y_direct = np.zeros_like(x)
+    m.evaluate(x, y_direct)
+    st = fam.stats()
+    assert st["batches"] == st["applies"] == 1
+    fam.set_min_rows(0)
+    y_queued = np.zeros_like(x)
+    m.evaluate(x, y_queued)
+    assert np.array_equal(y_direct, y_queued)
+    with pytest.raises(q.QsiError):
+        fam.set_min_rows(-1)
+
+
 def test_results_identical_alone_and_in_the_mix():
     sectors = _sectors()
     alone = {}
@@ -84,7 +109,7 @@ def test_results_identical_alone_and_in_the_mix():
             alone[r.rid] = r.evals
     finally:
         solo.close()
-    mix = serve.RequestLoop(sectors, slots=4)
+    mix = serve.RequestLoop(sectors, slots=4, min_batch_rows=0)  # batch the small test bases too
     try:
         reqs = [mix.submit(r) for r in _requests()]
         mix.drain(timeout=300)
@@ -105,7 +130,7 @@ def test_batched_results_match_unbatched_solves():
     H(g, B) to 1e-9."""
     sectors = _sectors()
     reqs = _requests(6)
-    loop = serve.RequestLoop(sectors, slots=3)
+    loop = serve.RequestLoop(sectors, slots=3, min_batch_rows=0)
     try:
         for r in reqs:
             loop.submit(r)

@@ -51,9 +51,10 @@ def parse():
     p.add_argument("--ref-step-seconds", type=float, default=2.5,
                    help="target length of one reference-arm step (a sample of whole source rows)")
     p.add_argument("--no-extras", action="store_true", help="skip batched / FTLM / e2e / CPU legs")
-    p.add_argument("--legs", default="e2e,batched,ftlm,lanczos,ftlm_sectors,serve,cpu",
+    p.add_argument("--legs", default="e2e,batched,ftlm,lanczos,ftlm_sectors,serve,materialised,cpu",
                    help="extra legs after the FP64 headline: e2e, batched, ftlm, lanczos (FP64 vs mixed 10-eigenvalue "
-                        "solves), ftlm_sectors (multi-sector FTLM), serve (request loop), cpu (whole oracle apply: "
+                        "solves), ftlm_sectors (multi-sector FTLM), serve (request loop), materialised (the applies, "
+                        "FTLM and, with lanczos, the solves on the materialised operator), cpu (whole oracle apply: "
                         "CPU baseline and parity)")
     p.add_argument("--nev", type=int, default=10)
     p.add_argument("--serve-n", type=int, default=200)
@@ -391,6 +392,111 @@ def ftlm_step_bytes(n: int, R: int, h: float, blocks: int, s: int = 4) -> float:
     return n * (apply_b + 2 * R * s + 4 * R * s + 2 * R * s)
 
 
+def ftlm_rate(q, ops, R, prec, M1, blocks=0):
+    """FTLM vector-steps/s of one sector: per-step time from the difference of an M1 and an M1/3 step run (setup,
+    capture and readout cancel), after a 2-step warm-up run; the rate including setup beside it."""
+    import torch
+
+    M1 = max(3, M1)
+    M0 = max(1, M1 // 3)
+    q.ftlm(ops, [R], M=2, seed=1, precision=prec, blocks=blocks)
+    t = {}
+    for M in (M0, M1):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        q.ftlm(ops, [R], M=M, seed=1, precision=prec, blocks=blocks)
+        t[M] = time.time() - t0
+    per = (t[M1] - t[M0]) / (M1 - M0)
+    return {"R": R, "precision": prec, "ms_per_step": per * 1e3, "vec_steps_per_s": R / per,
+            "vec_steps_per_s_incl_setup": R * M1 / t[M1], "seconds": {str(M0): t[M0], str(M1): t[M1]}}
+
+
+def event_ms(fn, steps, warmup):
+    """Mean milliseconds of fn over `steps` runs timed with CUDA events on the current stream, after `warmup`."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        a.record()
+        fn()
+        b.record()
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / steps
+
+
+def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves):
+    """The operator materialised (qsi_op_materialise: the column of every admitted term stored, as the reference
+    materialises H with toSparseMatrix for diag_DOQSI_ham --algorithm sparse and ftlm_DOQSI_ham): the FP64
+    single-vector apply (bitwise the matrix-free result), the batched FP32 applies, FTLM and optionally the
+    eigen-solves, each as in the matrix-free legs."""
+    import torch
+
+    out = {}
+    torch.cuda.synchronize()
+    t0 = time.time()
+    out["cache_bytes"] = op.materialise(True)
+    out["build_s"] = time.time() - t0
+    y = torch.zeros_like(x)
+    ms = event_ms(lambda: op.evaluate(x, y), args.steps, args.warmup)
+    bpr = 16 + 8 + 8 * h + 8 + 4 * h  # the matrix-free bytes plus the cached column of each hit
+    ach = n * bpr / (ms * 1e-3) / 1e9
+    out["apply_fp64"] = {"value": n / (ms * 1e-3), "unit": "states/s", "ms_per_apply": ms,
+                         "bitwise_equal_to_matrix_free": bool(np.array_equal(y.cpu().numpy(), y_host)),
+                         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                                      "peak_kind": peak_kind, "bytes_per_row": bpr,
+                                      "kernel": "k_apply_tile<double,double,LookupCache>"}}
+    del y
+    for R in [int(v) for v in str(args.R).split(",") if v]:
+        torch.cuda.empty_cache()
+        try:
+            X = torch.randn(n, R, dtype=torch.float32, device=x.device)
+            Y = torch.zeros_like(X)
+        except torch.cuda.OutOfMemoryError as e:
+            out[f"batched_r{R}"] = {"skipped": str(e)[:160]}
+            continue
+        ms = event_ms(lambda: op.apply_batched(X, Y), max(3, args.steps // 3), 1)
+        bpr = 16 + R * 4 * (h + 2) + 4 * h
+        ach = n * bpr / (ms * 1e-3) / 1e9
+        out[f"batched_r{R}"] = {"value": n * R / (ms * 1e-3), "unit": "state-vectors/s", "ms_per_apply": ms,
+                                "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                                             "frac": ach / peak, "peak_kind": peak_kind, "bytes_per_row": bpr}}
+        del X, Y
+    torch.cuda.empty_cache()
+    if "ftlm" in args.legs:
+        R = args.ftlm_R or int(str(args.R).split(",")[0])
+        try:
+            mixed = ftlm_rate(q, [op], R, "mixed", args.ftlm_steps, 2)
+        except q.QsiError as e:
+            mixed = {"R": R, "skipped": str(e)[:160]}
+        torch.cuda.empty_cache()
+        plain = ftlm_rate(q, [op], 1, "f64", args.ftlm_steps)
+        out["ftlm"] = {"mixed": mixed, "plain_fp64": plain}
+        if "vec_steps_per_s" in mixed:
+            out["ftlm"]["speedup_vs_plain_fp64"] = mixed["vec_steps_per_s"] / plain["vec_steps_per_s"]
+    if with_solves:
+        sol = {}
+        for prec, polish in (("f64", 0), ("mixed", 2)):
+            torch.cuda.synchronize()
+            t0 = time.time()
+            ev, _, rep = q.diagonalise(op, nev=args.nev, ncv=args.ncv, tol=1e-10, max_iter=400, seed=1,
+                                       precision=prec, polish_steps=polish, want_vectors=False)
+            sol[prec] = {"seconds": time.time() - t0, "applies": rep.applies, "restarts": rep.restarts,
+                         "evals": [float(v) for v in ev], "max_residual": float(np.max(rep.residual[:args.nev]))}
+        e64, emx = np.array(sol["f64"]["evals"]), np.array(sol["mixed"]["evals"])
+        top = min(emx.max(), e64.max())
+        err = np.array([np.abs(e64 - v).min() for v in emx if v <= top + 1e-8])
+        sol["max_abs_err"] = float(err.max())
+        sol["within_1e-9"] = bool(err.max() <= 1e-9)
+        sol["speedup_mixed_vs_f64"] = sol["f64"]["seconds"] / sol["mixed"]["seconds"]
+        out["lanczos"] = sol
+    op.materialise(False)
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -558,33 +664,19 @@ def run_ours(args):
         # launch per step, the run captured in one CUDA graph, the in-place two-block recurrence) against plain
         # FP64 single-vector Lanczos.
         # Per-step rates come from the difference of an M and an M/3 step run (setup, capture and readout
-        # cancel); the rates including setup are given beside them.
-        M1 = max(3, args.ftlm_steps)
-        M0 = max(1, M1 // 3)
-
-        def ftlm_rate(R, prec, blocks=0):
-            q.ftlm([op], [R], M=2, seed=1, precision=prec, blocks=blocks)  # warm-up (allocations, graph paths)
-            t = {}
-            for M in (M0, M1):
-                torch.cuda.synchronize()
-                t0 = time.time()
-                q.ftlm([op], [R], M=M, seed=1, precision=prec, blocks=blocks)
-                t[M] = time.time() - t0
-            per = (t[M1] - t[M0]) / (M1 - M0)
-            return {"R": R, "precision": prec, "ms_per_step": per * 1e3, "vec_steps_per_s": R / per,
-                    "vec_steps_per_s_incl_setup": R * M1 / t[M1], "seconds": {str(M0): t[M0], str(M1): t[M1]}}
+        # cancel); the rates including setup are given beside them (ftlm_rate).
 
         R_ftlm = args.ftlm_R or int(str(args.R).split(",")[0])
         note = None
         try:
-            mixed = ftlm_rate(R_ftlm, "mixed", 2)  # the batched settings tuned for R = first of --R
+            mixed = ftlm_rate(q, [op], R_ftlm, "mixed", args.ftlm_steps, 2)  # settings tuned for R = first of --R
         except q.QsiError as e:  # device memory taken by others: half the vectors
             if R_ftlm <= 16:
                 raise
             note = f"R={R_ftlm} failed ({str(e)[:120]}); R={R_ftlm // 2} instead"
             R_ftlm //= 2
             torch.cuda.empty_cache()
-            mixed = ftlm_rate(R_ftlm, "mixed", 2)
+            mixed = ftlm_rate(q, [op], R_ftlm, "mixed", args.ftlm_steps, 2)
         mixed["vector_blocks"] = 2
         step_b = ftlm_step_bytes(n, R_ftlm, h, mixed["vector_blocks"])
         fach = step_b / (mixed["ms_per_step"] * 1e-3) / 1e9
@@ -594,7 +686,7 @@ def run_ours(args):
         if note:
             mixed["note"] = note
         torch.cuda.empty_cache()
-        plain = ftlm_rate(1, "f64")
+        plain = ftlm_rate(q, [op], 1, "f64", args.ftlm_steps)
         line["ftlm"] = {"value": mixed["vec_steps_per_s"], "unit": "vec-steps/s", "mixed": mixed, "plain_fp64": plain,
                         "speedup_vs_plain_fp64": mixed["vec_steps_per_s"] / plain["vec_steps_per_s"]}
     if "lanczos" in legs and rank == 0:
@@ -630,6 +722,10 @@ def run_ours(args):
         line["ftlm_sectors"] = ftlm_sectors_leg(args)
     if "serve" in legs and rank == 0:
         line["serve"] = serve_leg(args)
+    if "materialised" in legs and rank == 0:
+        if "x" not in locals():  # the lanczos leg released the headline's vectors
+            x = torch.from_numpy(x_host).to(dev)
+        line["materialised"] = materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, "lanczos" in legs)
     if "cpu" in legs and rank == 0:
         # One whole apply of the reference's push loop (oracle restatement) on all host cores, on the headline's
         # x: the CPU baseline (whole apply, no sample) and the full-size parity check of the GPU results.

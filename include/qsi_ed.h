@@ -186,6 +186,13 @@ qsi_status qsi_basis_search(qsi_basis* b, const uint64_t* states_lohi, int64_t n
 qsi_status qsi_op_create(qsi_basis* b, const qsi_term* terms, int32_t n_terms,
                          qsi_op** out);
 qsi_status qsi_op_destroy(qsi_op* op);
+/* Materialises the operator, as the reference does with LazyOpSum::toSparseMatrix before its sparse solvers
+ * (diag_DOQSI_ham --algorithm sparse, include/matrix_diag_bits.hpp:181-189; ftlm_DOQSI_ham,
+ * src/ftlm_DOQSI_ham.cpp:150-153): enable = 1 stores the column of every admitted term of every row in device
+ * memory (4 bytes per term, in 32-row tiles), so later applies of any kind read columns instead of looking them
+ * up; enable = 0 frees it.  Applies give bitwise the results of the matrix-free apply either way.  *bytes (may
+ * be NULL): the cache's size. */
+qsi_status qsi_op_materialise(qsi_op* op, int32_t enable, int64_t* bytes);
 /* Operator families for serving many parameter points of one sector at once (the request loop that replaces
  * the reference's static phase-diagram plans, driver/ed_phasedia_plan.sh:21-25 with
  * driver/execute_asynchronous.sh:1-38; no counterpart in the operator code): the terms of qsi_op_create with a

@@ -118,6 +118,7 @@ SIGNATURES = {
     "qsi_family_member": [_P, _P, C.POINTER(_P)],
     "qsi_family_stats": [_P, C.POINTER(_I64), C.POINTER(_I64)],
     "qsi_family_set_min_rows": [_P, _I64],
+    "qsi_op_materialise": [_P, _I32, C.POINTER(_I64)],
     "qsi_op_apply": [_P, _P, _P, _I32, _I32, _P],
     "qsi_op_apply_static": [_P, _P, _P, _I32],
     "qsi_op_apply_batched": [_P, _P, _P, _I32, _I32, _I32, _I32, _P],

@@ -100,6 +100,8 @@ def diag_main(argv=None) -> Path:
         evals, evecs = np.array([e0]), vec[:, None]
         print(f"eigval0: E0 = {e0!r} after {its} iterations")
     else:  # compute_spectrum_iterative (matrix_diag_bits.hpp:51-95)
+        if algo in ("dense", "sparse"):  # the reference materialises H first (matrix_diag_bits.hpp:174-189)
+            _materialise_if_it_fits(op)
         evals, evecs, rep = diagonalise(op, nev=a.n_eigvals, ncv=a.ncv, tol=10.0 ** a.atol, max_iter=a.max_iters,
                                         seed=a.rng_seed)
         evecs = evecs[:, : a.n_eigvecs]
@@ -114,6 +116,17 @@ def diag_main(argv=None) -> Path:
     op.close()
     print(f"Writing to\n{out}")
     return out
+
+
+def _materialise_if_it_fits(op) -> None:
+    """Materialises the operator (qsi_op_materialise) unless the device is out of memory for its cache: the
+    matrix-free apply gives the same results, only slower."""
+    from ._lib import QsiError
+
+    try:
+        op.materialise(True)
+    except QsiError as e:
+        print(f"not materialised ({e}); applying matrix-free")
 
 
 def ftlm_parser() -> argparse.ArgumentParser:
@@ -146,6 +159,7 @@ def ftlm_main(argv=None) -> Path:
     H, stem = _hamiltonian(lat, a)
     op = LazyOpSum(ZBasis(basis), H)
     R = 1 << max(0, int(np.ceil(np.log2(max(1, a.n_randvecs)))))  # batched runs take a power of two
+    _materialise_if_it_fits(op)  # as the reference materialises H (src/ftlm_DOQSI_ham.cpp:150-153)
     (al, be), = ftlm([op], [R], M=a.ncv, seed=a.rng_seed, precision=a.precision)
     al, be = al[: a.n_randvecs], be[: a.n_randvecs]
     temps = np.logspace(np.log10(a.T_min), np.log10(a.T_max), a.n_temps)

@@ -379,6 +379,14 @@ class LazyOpSum:
 
     cols = rows
 
+    def materialise(self, enable: bool = True) -> int:
+        """Stores the column of every admitted term (the reference's toSparseMatrix before its sparse solvers);
+        applies then read columns instead of looking them up, with bitwise the same results.  Returns the cache's
+        size in bytes (0 after enable=False)."""
+        nb = C.c_int64()
+        call("qsi_op_materialise", self._h, int(bool(enable)), C.byref(nb))
+        return nb.value
+
     def set_kernel(self, kernel: int = 1, use_hash: bool = True, list_cap: int = 0) -> None:
         """kernel 0: row per thread / warp per row; 1: bit-sliced 32-row tiles (default).  use_hash bit 0: hash
         index lookups; bit 1: FP64 instead of double-float accumulation of FP32 batched applies."""

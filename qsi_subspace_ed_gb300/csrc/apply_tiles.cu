@@ -18,6 +18,8 @@
 #include <vector>
 #include <type_traits>
 
+#include <cub/device/device_scan.cuh>
+
 #include "qsi_device.cuh"
 #include "qsi_handles.h"
 
@@ -218,6 +220,8 @@ __global__ void __launch_bounds__(256, LK::kMinBlocks) k_apply_tile(TileParams P
         tile_spin_words(s, P.nwords, lane, spinw);
         for (int r = 0; r < n_rounds; ++r) adm[r * 32 + lane] = tile_admitted(S, P.n_off, r * 32, lane, vmask, spinw);
         double acc = valid ? (kFam ? fam_diag(P, s.x, s.y, 0) : P.diag[row]) * (double)x[row] : 0.0;
+        const uint64_t cur = lk.cursor(tile, lane);
+        int kk = 0;  // admitted terms of this row looked up so far
         int r = 0;
         uint32_t a = adm[lane];
         while (true) {
@@ -243,7 +247,8 @@ __global__ void __launch_bounds__(256, LK::kMinBlocks) k_apply_tile(TileParams P
                 }
             }
             if (!nh) break;
-            lk.template find_batch<kNB>(tl, th, J, nh);
+            lk.template find_batch<kNB>(tl, th, J, nh, cur, kk);
+            kk += nh;
             XT xv[kNB];
 #pragma unroll
             for (int u = 0; u < kNB; ++u) xv[u] = (u < nh && J[u] >= 0) ? x[J[u]] : (XT)0;
@@ -348,6 +353,8 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                     ++k;
                 }
                 // this row's admitted terms in term order, kNB lookups at a time across the 32-term rounds
+                const uint64_t cur = lk.cursor(tile, lane);
+                int kk = 0;
                 int r = 0;
                 uint32_t a = adm[lane];
                 while (true) {
@@ -371,7 +378,8 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
                             }
                         }
                         if (!nh) break;
-                        lk.template find_batch<kNB>(tl, th, J, nh);
+                        lk.template find_batch<kNB>(tl, th, J, nh, cur, kk);
+                        kk += nh;
 #pragma unroll
                         for (int u = 0; u < kNB; ++u) {
                             if (u >= nh) continue;
@@ -617,11 +625,13 @@ __global__ void __launch_bounds__(256, KM <= kVec4 ? 2 : 3) k_apply_tile_batched
 // Several operators (sectors) in one launch: the grid is partitioned into
 // per-sector block ranges in proportion to each sector's rows x vectors;
 // each block stages its own sector's terms and works through that sector's
-// tiles.  FP32 storage, double-float accumulation; hash lookups when every
-// sector's batched applies use them, else bucket-table lookups.
+// tiles.  FP32 storage, double-float accumulation; the lookup caches when every
+// sector is materialised, else hash lookups when every sector's batched applies
+// use them, else bucket-table lookups.
 struct SectorLaunch {
     TileParams P;
     HashView H;
+    CacheView C;
     const float* x;
     float* y;
     const float2* ycoef;  // accumulating launches: y <- H x + ycoef[c] y per column (nullptr: coefficient 1)
@@ -644,6 +654,7 @@ __global__ void __launch_bounds__(256, KM <= kVec4 ? 2 : 3) k_apply_sectors(cons
     __syncthreads();
     LK lk;
     if constexpr (std::is_same<LK, LookupHash>::value) lk = LookupHash{L.H};
+    else if constexpr (std::is_same<LK, LookupCache>::value) lk = LookupCache{L.C};
     else lk = LookupTable{L.P.B};
     batched_body<float, LK, true, KM>(L.P, lk, L.x, L.y, L.R, accumulate, L.cap, (int64_t)blockIdx.x - L.block_begin,
                                       L.n_blocks, smem_raw, L.ycoef);
@@ -727,6 +738,80 @@ qsi_status build_hash(qsi_basis* b) {
     if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "hash build: %s", cudaGetErrorString(e));
     if (over) return fail(QSI_CUDA_ERROR, "hash build: a state found no slot in its region");
     return QSI_OK;
+}
+
+// ------------------------------------------------------------------ lookup cache (materialised operator)
+// Admitted terms of the tile's widest row: the tile's number of cache lines.
+__global__ void __launch_bounds__(256) k_cache_widths(TileParams P, uint64_t* __restrict__ width) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const TileSmem S = stage_terms(P, smem_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n_rounds = (P.n_off + 31) >> 5;
+    uint32_t* spinw = reinterpret_cast<uint32_t*>(S.tail) + wid * 128;
+    const int64_t ntiles = (P.B.n + 31) >> 5;
+    for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
+        const int64_t row = tile * 32 + lane;
+        const bool valid = row < P.B.n;
+        const state2 s = valid ? P.B.states[row] : make_ulonglong2(0, 0);
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        tile_spin_words(s, P.nwords, lane, spinw);
+        int cnt = 0;
+        for (int r = 0; r < n_rounds; ++r) cnt += __popc(tile_admitted(S, P.n_off, r * 32, lane, vmask, spinw));
+#pragma unroll
+        for (int o = 16; o; o >>= 1) cnt = max(cnt, __shfl_xor_sync(0xffffffffu, cnt, o));
+        if (lane == 0) width[tile] = (uint64_t)cnt;
+        __syncwarp();
+    }
+}
+
+// The column of every admitted term of every row (kEmpty outside the basis), looked up with lk, at the positions
+// LookupCache reads them from.
+template <class LK>
+__global__ void __launch_bounds__(256) k_cache_fill(TileParams P, LK lk, const uint64_t* __restrict__ off,
+                                                    uint32_t* __restrict__ cols) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const TileSmem S = stage_terms(P, smem_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n_rounds = (P.n_off + 31) >> 5;
+    uint32_t* spinw = reinterpret_cast<uint32_t*>(S.tail) + wid * (128 + 32 * n_rounds);
+    uint32_t* adm = spinw + 128;
+    const int64_t ntiles = (P.B.n + 31) >> 5;
+    for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
+        const int64_t row = tile * 32 + lane;
+        const bool valid = row < P.B.n;
+        const state2 s = valid ? P.B.states[row] : make_ulonglong2(0, 0);
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        tile_spin_words(s, P.nwords, lane, spinw);
+        for (int r = 0; r < n_rounds; ++r) adm[r * 32 + lane] = tile_admitted(S, P.n_off, r * 32, lane, vmask, spinw);
+        uint32_t* out = cols + off[tile] * 32 + lane;
+        int kk = 0, r = 0;
+        uint32_t a = adm[lane];
+        while (true) {
+            constexpr int kNB = 4;
+            uint64_t tl[kNB], th[kNB];
+            int64_t J[kNB];
+            int nh = 0;
+#pragma unroll
+            for (int u = 0; u < kNB; ++u) {
+                tl[u] = th[u] = 0;
+                while (!a && r + 1 < n_rounds) a = adm[++r * 32 + lane];
+                if (a) {
+                    const PullTerm& T = S.terms[r * 32 + __ffs(a) - 1];
+                    a &= a - 1;
+                    tl[u] = s.x ^ T.x0;
+                    th[u] = s.y ^ T.x1;
+                    ++nh;
+                }
+            }
+            if (!nh) break;
+            lk.template find_batch<kNB>(tl, th, J, nh);
+#pragma unroll
+            for (int u = 0; u < kNB; ++u)
+                if (u < nh) out[(uint64_t)(kk + u) * 32] = (J[u] < 0) ? kEmpty : (uint32_t)J[u];
+            kk += nh;
+        }
+        __syncwarp();
+    }
 }
 
 // ------------------------------------------------------------------ launchers
@@ -831,6 +916,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
     plan.vec8 = true;
     plan.vec16 = true;
     plan.hash = true;
+    plan.cache = true;
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -842,12 +928,14 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
         qsi_op* op = ops[s];
         if (op->kernel != 1) return fail(QSI_INVALID_ARG, "sector launch needs the tile kernels");
         plan.hash = plan.hash && op->basis->d_hash && op->tune[1].use_hash;
+        plan.cache = plan.cache && op->d_cache_cols;
         const int cap = (std::max(op->tune[1].list_cap, op->n_pull + 1) + 7) & ~7;  // a row: diagonal + terms
         const int n_rounds = (op->n_pull + 31) / 32;
         smem = std::max(smem, term_smem(op) + (size_t)nw * (512 + (size_t)n_rounds * 128 + (size_t)cap * 12));
         L[s].P = TileParams{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
                             op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords, op->tune[1].vec_chunk};
         L[s].H = op->basis->hview();
+        L[s].C = CacheView{op->d_cache_cols, op->d_cache_off};
         L[s].x = X[s];
         L[s].y = Y[s];
         L[s].ycoef = ycoef ? ycoef[s] : nullptr;
@@ -884,7 +972,9 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
 qsi_status launch_sectors(const void* d_records, const SectorPlan& plan, int accumulate, cudaStream_t st) {
     auto go = [&](auto km) {
         constexpr int KM = decltype(km)::value;
-        auto k = plan.hash ? k_apply_sectors<KM, LookupHash> : k_apply_sectors<KM, LookupTable>;
+        auto k = plan.cache ? k_apply_sectors<KM, LookupCache>
+                 : plan.hash ? k_apply_sectors<KM, LookupHash>
+                             : k_apply_sectors<KM, LookupTable>;
         set_smem(k, plan.smem);
         k<<<plan.grid, 256, plan.smem, st>>>((const SectorLaunch*)d_records, plan.n, accumulate);
     };
@@ -960,8 +1050,76 @@ qsi_status launch_family(qsi_op* tmpl, const double* x, double* y, int R, const 
 
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
                               cudaStream_t st) {
+    if (op->d_cache_cols)
+        return launch_tiles_lk(op, LookupCache{CacheView{op->d_cache_cols, op->d_cache_off}}, x, y, R, xdtype, ydtype,
+                               accumulate, st);
     if (op->basis->d_hash && op->tune[R > 1].use_hash) return launch_tiles_lk(op, LookupHash{op->basis->hview()}, x, y, R, xdtype, ydtype, accumulate, st);
     return launch_tiles_lk(op, LookupTable{op->basis->view()}, x, y, R, xdtype, ydtype, accumulate, st);
+}
+
+// Builds (enable) or frees the operator's lookup cache; *bytes: its size.
+qsi_status materialise(qsi_op* op, bool enable, int64_t* bytes) {
+    cudaFree(op->d_cache_cols);
+    cudaFree(op->d_cache_off);
+    op->d_cache_cols = nullptr;
+    op->d_cache_off = nullptr;
+    op->cache_entries = 0;
+    if (enable) {
+        if (op->kernel != 1) return fail(QSI_INVALID_ARG, "qsi_op_materialise: the cache serves the tile kernels (kernel 1)");
+        cudaStream_t st = op->stream;
+        const int64_t ntiles = (op->basis->n + 31) / 32;
+        TileParams P{op->basis->view(), op->d_pull, op->d_lit_off, op->d_lits, op->d_diag_generic, op->diag,
+                     op->d_diag, op->d_diag_ff, op->n_pull, op->n_lits, op->nwords, 0};
+        const int block = 256, nw = block / 32;
+        const int n_rounds = (op->n_pull + 31) / 32;
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
+        // widths, their exclusive scan (tile offsets in cache lines), then the columns
+        uint64_t* width = nullptr;
+        QSI_CUDA(cudaMallocAsync(&width, (size_t)(ntiles + 1) * 8, st));
+        QSI_CUDA(cudaMallocAsync(&op->d_cache_off, (size_t)(ntiles + 1) * 8, st));
+        QSI_CUDA(cudaMemsetAsync(width + ntiles, 0, 8, st));
+        const size_t smem_w = term_smem(op) + (size_t)nw * 512;
+        set_smem(k_cache_widths, smem_w);
+        k_cache_widths<<<grid, block, smem_w, st>>>(P, width);
+        size_t tmp_bytes = 0;
+        QSI_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, width, op->d_cache_off, ntiles + 1, st));
+        void* tmp = nullptr;
+        QSI_CUDA(cudaMallocAsync(&tmp, tmp_bytes, st));
+        QSI_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, width, op->d_cache_off, ntiles + 1, st));
+        uint64_t lines = 0;
+        QSI_CUDA(cudaMemcpyAsync(&lines, op->d_cache_off + ntiles, 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+        cudaFreeAsync(tmp, st);
+        cudaFreeAsync(width, st);
+        const size_t n_entries = (size_t)lines * 32;
+        cudaError_t e = cudaMalloc(&op->d_cache_cols, std::max<size_t>(n_entries, 1) * 4);
+        if (e != cudaSuccess) {
+            cudaFree(op->d_cache_off);
+            op->d_cache_off = nullptr;
+            op->d_cache_cols = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? QSI_OOM : QSI_CUDA_ERROR,
+                        "qsi_op_materialise: %zu bytes for the cache: %s", n_entries * 4, cudaGetErrorString(e));
+        }
+        QSI_CUDA(cudaMemsetAsync(op->d_cache_cols, 0xFF, n_entries * 4, st));  // the lanes below their tile's width
+        const size_t smem_f = term_smem(op) + (size_t)nw * (512 + (size_t)n_rounds * 128);
+        if (op->basis->d_hash) {
+            auto k = k_cache_fill<LookupHash>;
+            set_smem(k, smem_f);
+            k<<<grid, block, smem_f, st>>>(P, LookupHash{op->basis->hview()}, op->d_cache_off, op->d_cache_cols);
+        } else {
+            auto k = k_cache_fill<LookupTable>;
+            set_smem(k, smem_f);
+            k<<<grid, block, smem_f, st>>>(P, LookupTable{op->basis->view()}, op->d_cache_off, op->d_cache_cols);
+        }
+        QSI_CUDA(cudaGetLastError());
+        QSI_CUDA(cudaStreamSynchronize(st));
+        op->cache_entries = n_entries;
+    }
+    if (bytes) *bytes = op->d_cache_cols ? (int64_t)(op->cache_entries * 4 + ((op->basis->n + 31) / 32 + 1) * 8) : 0;
+    return QSI_OK;
 }
 
 }  // namespace qsi

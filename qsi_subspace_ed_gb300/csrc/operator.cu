@@ -604,9 +604,19 @@ extern "C" qsi_status qsi_op_destroy(qsi_op* op) {
     cudaFree(op->d_lits);
     cudaFree(op->d_x);
     cudaFree(op->d_y);
+    cudaFree(op->d_cache_cols);
+    cudaFree(op->d_cache_off);
     if (op->stream) cudaStreamDestroy(op->stream);
     delete op;
     return QSI_OK;
+}
+
+extern "C" qsi_status qsi_op_materialise(qsi_op* op, int32_t enable, int64_t* bytes) {
+    return guarded([&]() -> qsi_status {
+        if (!op || (enable != 0 && enable != 1)) return fail(QSI_INVALID_ARG, "qsi_op_materialise: bad argument");
+        if (op->stream) QSI_CUDA(cudaStreamSynchronize(op->stream));
+        return materialise(op, enable != 0, bytes);
+    });
 }
 
 namespace qsi {

@@ -186,12 +186,16 @@ __device__ __forceinline__ int64_t hash_find(const HashView& Hv, uint64_t lo, ui
 // Lookups of up to NB states at once.  The hash variant issues the first
 // probe of every state before resolving any (independent loads in flight);
 // further probes, needed after a collision, follow one by one.
+// Every lookup class takes the states to look up and, for the materialised operator's cache, where the row's
+// entries start (cursor(tile, lane), once per tile) and the admission ordinal of the batch's first term.
 struct LookupTable {
     BasisView B;
     static constexpr int kNB = 4, kMinBlocks = 3;  // lookups per batch per lane, resident 256-thread blocks
     __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return basis_find(B, lo, hi); }
+    __device__ __forceinline__ uint64_t cursor(int64_t, int) const { return 0; }
     template <int NB>
-    __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n) const {
+    __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n,
+                                               uint64_t = 0, int = 0) const {
 #pragma unroll
         for (int u = 0; u < NB; ++u)
             if (u < n) J[u] = basis_find(B, lo[u], hi[u]);
@@ -202,9 +206,11 @@ struct LookupHash {
     HashView H;
     static constexpr int kNB = 4, kMinBlocks = 3;
     __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return hash_find(H, lo, hi); }
+    __device__ __forceinline__ uint64_t cursor(int64_t, int) const { return 0; }
     // every state's region (one table load each), then every first probe, before resolving any
     template <int NB>
-    __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n) const {
+    __device__ __forceinline__ void find_batch(const uint64_t* lo, const uint64_t* hi, int64_t* J, int n,
+                                               uint64_t = 0, int = 0) const {
         const HashSlot* reg[NB];
         uint32_t cap[NB], off[NB];
         uint4 e[NB];
@@ -240,6 +246,30 @@ struct LookupHash {
             }
             J[u] = r;
         }
+    }
+};
+
+// The materialised operator's lookup cache (qsi_op_materialise): the column of every admitted term of every row,
+// kEmpty for a column outside the basis, in the order the tile kernels visit them.  Tile t's entries start at
+// 32 * off[t]; the row in lane l has its k-th admitted term at 32 * (off[t] + k) + l, so a warp reads one
+// coalesced 128-byte line per admission ordinal.  Results are those of the lookups it replaces, bit for bit.
+struct CacheView {
+    const uint32_t* cols;
+    const uint64_t* off;
+};
+struct LookupCache {
+    CacheView C;
+    static constexpr int kNB = 8, kMinBlocks = 3;
+    __device__ __forceinline__ uint64_t cursor(int64_t tile, int lane) const { return C.off[tile] * 32 + lane; }
+    template <int NB>
+    __device__ __forceinline__ void find_batch(const uint64_t*, const uint64_t*, int64_t* J, int n, uint64_t cur,
+                                               int k0) const {
+#pragma unroll
+        for (int u = 0; u < NB; ++u)
+            if (u < n) {
+                const uint32_t c = __ldg(C.cols + cur + (uint64_t)(k0 + u) * 32);
+                J[u] = (c == kEmpty) ? -1 : (int64_t)c;
+            }
     }
 };
 

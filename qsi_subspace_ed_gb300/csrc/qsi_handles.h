@@ -52,6 +52,9 @@ struct qsi_op {
     qsi_tuning tune[2];             // [0] single-vector applies, [1] batched applies (R > 1)
     double* d_diag = nullptr;       // per-row diagonal (tile kernels)
     float2* d_diag_ff = nullptr;    // the same as double-float pairs (FP32 batched kernel)
+    uint32_t* d_cache_cols = nullptr;  // lookup cache of the materialised operator (qsi_op_materialise), or null
+    uint64_t* d_cache_off = nullptr;   // its tile offsets in 32-entry lines
+    size_t cache_entries = 0;
     cudaStream_t stream = nullptr;
     int device = 0;        // the device current at qsi_op_create (owner of every buffer and of the stream)
     void* d_x = nullptr;   // staging for host-pointer applies
@@ -74,6 +77,8 @@ qsi_status family_apply(qsi_op* op, const double* x, double* y, int accumulate, 
 // Called by qsi_op_destroy for a family member.
 void family_release_member(qsi_op* op);
 qsi_status build_hash(qsi_basis* b);
+// Builds (enable) or frees an operator's lookup cache (qsi_op_materialise); *bytes: its size in device memory.
+qsi_status materialise(qsi_op* op, bool enable, int64_t* bytes);
 // Bucket table of a basis at its current width (b->bits, b->shift, b->n_buckets), allocated with padding for the
 // 16-byte reads of bucket_bounds.
 qsi_status build_buckets(qsi_basis* b);
@@ -90,6 +95,7 @@ struct SectorPlan {
     bool vec8 = true;  // ... of 8 vectors per lane, and every sector's batched applies are set to them
     bool vec16 = true; // ... of 16 vectors per lane, likewise
     bool hash = true;  // every sector's batched applies look columns up through the hash index
+    bool cache = true; // every sector is materialised (qsi_op_materialise): columns come from the lookup caches
 };
 qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float* const* Y, const int* R,
                         SectorPlan& plan, const double* weights = nullptr, const float2* const* ycoef = nullptr);

@@ -135,6 +135,14 @@ def test_ftlm_sector_launch_lookup_and_tuning_independent():
     for op in ops:
         op.set_kernel(1, 1)
         op.set_tuning(0, 0)
+    # materialised sectors (the lookup caches in the same one-launch apply): bitwise the same recurrences
+    for op in ops:
+        assert op.materialise(True) > 0
+    other = q.ftlm(ops, [64, 64], M=20, seed=4, precision="mixed")
+    for (a, b), (c, d) in zip(ref, other):
+        assert np.array_equal(a, c) and np.array_equal(b, d)
+    for op in ops:
+        op.materialise(False)
 
 
 def test_tridiag_ritz_matches_numpy():

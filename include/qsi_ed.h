@@ -311,8 +311,7 @@ typedef struct qsi_lanczos_cfg {
                              FP64 rounds (the 2nd on [X, HX - X theta]) refine the pairs */
     int32_t want_vectors; /* write eigenvectors */
     int32_t block;        /* QSI_F32 only: 16 = block Lanczos on FP32 blocks of 16 vectors through the
-                             batched apply (nev <= 13), 1 = single-vector, 0 = block for bases of at
-                             least 65536 states when nev <= 13, else single-vector */
+                             batched apply (nev <= 13); 0 or 1 = single-vector Lanczos on FP32 vectors */
     int32_t reserved;
 } qsi_lanczos_cfg;
 
@@ -372,10 +371,8 @@ qsi_status qsi_ftlm_run(qsi_op** ops, int32_t n_sectors, const int32_t* R,
 /* qsi_ftlm_run with the number of R-vector blocks kept per sector: 3 (H q in
  * its own block), 2 (in-place recurrence: H q accumulated into the previous
  * vector block, so R can double at the same device-memory footprint), or 0 =
- * what qsi_ftlm_run does: two when every sector takes the one-launch FP32
- * sector apply (whose two-block step moves fewer bytes), else three when they
- * fit in free device memory, else two.  Both layouts give the same
- * recurrences up to rounding. */
+ * three when they fit in free device memory, else two (what qsi_ftlm_run
+ * does).  Both layouts give the same recurrences up to rounding. */
 qsi_status qsi_ftlm_run_blocks(qsi_op** ops, int32_t n_sectors, const int32_t* R,
                                int32_t M, uint64_t seed, int32_t precision,
                                int32_t blocks, double* alphas, double* betas);

@@ -267,6 +267,83 @@ __global__ void __launch_bounds__(256, LK::kMinBlocks) k_apply_tile(TileParams P
     }
 }
 
+// Family mode with a few columns (FP64 [row][R], 2 <= R <= RC): the single-vector tile kernel with each lane
+// summing all R columns of its row, the R values of a hit gathered from one place.  Each column's sum is the one
+// k_apply_tile forms for that column alone (same terms in the same order, same coefficients and tests), so a
+// member's result does not depend on the batch it ran in.
+template <class LK, int RC>
+__global__ void __launch_bounds__(256, 2) k_apply_tile_cols(TileParams P, LK lk, const double* __restrict__ x,
+                                                            double* __restrict__ y, int accumulate) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const TileSmem S = stage_terms(P, smem_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n_rounds = (P.n_off + 31) >> 5;
+    const int R = P.fR;
+    uint32_t* spinw = reinterpret_cast<uint32_t*>(S.tail) + wid * (128 + 32 * n_rounds);
+    uint32_t* adm = spinw + 128;
+    const int64_t ntiles = (P.B.n + 31) >> 5;
+    for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
+        const int64_t row = tile * 32 + lane;
+        const bool valid = row < P.B.n;
+        const state2 s = valid ? P.B.states[row] : make_ulonglong2(0, 0);
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+        tile_spin_words(s, P.nwords, lane, spinw);
+        for (int r = 0; r < n_rounds; ++r) adm[r * 32 + lane] = tile_admitted(S, P.n_off, r * 32, lane, vmask, spinw);
+        double acc[RC];
+#pragma unroll
+        for (int c = 0; c < RC; ++c) acc[c] = (valid && c < R) ? fam_diag(P, s.x, s.y, c) * x[row * R + c] : 0.0;
+        const uint64_t cur = lk.cursor(tile, lane);
+        int kk = 0, r = 0;
+        uint32_t a = adm[lane];
+        while (true) {
+            constexpr int kNB = 4;
+            int tt[kNB];
+            uint64_t tl[kNB], th[kNB];
+            int64_t J[kNB];
+            int nh = 0;
+#pragma unroll
+            for (int u = 0; u < kNB; ++u) {
+                tt[u] = 0;
+                tl[u] = th[u] = 0;
+                while (!a && r + 1 < n_rounds) a = adm[++r * 32 + lane];
+                if (a) {
+                    tt[u] = r * 32 + __ffs(a) - 1;
+                    a &= a - 1;
+                    const PullTerm& T = S.terms[tt[u]];
+                    tl[u] = s.x ^ T.x0;
+                    th[u] = s.y ^ T.x1;
+                    ++nh;
+                }
+            }
+            if (!nh) break;
+            lk.template find_batch<kNB>(tl, th, J, nh, cur, kk);
+            kk += nh;
+#pragma unroll
+            for (int u = 0; u < kNB; ++u) {
+                if (u >= nh || J[u] < 0) continue;
+                const double cs = term_coeff(S.terms[tt[u]], s);
+                const double* xj = x + J[u] * R;
+                double xv[RC];
+#pragma unroll
+                for (int c = 0; c < RC; ++c) xv[c] = (c < R) ? xj[c] : 0.0;
+#pragma unroll
+                for (int c = 0; c < RC; ++c)
+                    if (c < R && above_tol(xv[c])) acc[c] += fam_coef(P, cs, c) * xv[c];
+            }
+        }
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < RC; ++c) {
+                if (c >= R) break;
+                double v = acc[c];
+                if (accumulate) v += y[row * R + c];
+                y[row * R + c] = v;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // KM values selecting 16-byte FP32 gathers of 4 (kVec4) or 8 (kVec8) vectors per lane (see batched_body), and
 // the bases, vector counts and pointers each takes.  Their hit lists mark the diagonal slot with the top bit of
 // the row index.
@@ -1018,6 +1095,15 @@ static qsi_status launch_family_lk(qsi_op* tmpl, LK lk, const double* x, double*
         const int grid = (int)std::max<int64_t>(
             1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * (T.grid_bps > 0 ? T.grid_bps : 8)));
         auto k = k_apply_tile<double, double, LK, true>;
+        set_smem(k, smem);
+        k<<<grid, block, smem, st>>>(P, lk, x, y, accumulate);
+    } else if (R <= 8) {  // a few columns: every lane sums all columns of its row
+        const size_t smem = term_smem(tmpl) + (size_t)nw * (512 + (size_t)(tmpl->n_pull + 31) / 32 * 128);
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
+        auto k = (R <= 2) ? k_apply_tile_cols<LK, 2> : (R <= 4) ? k_apply_tile_cols<LK, 4> : k_apply_tile_cols<LK, 8>;
         set_smem(k, smem);
         k<<<grid, block, smem, st>>>(P, lk, x, y, accumulate);
     } else {

@@ -60,8 +60,13 @@ struct qsi_family {
     double* X = nullptr;
     double* Y = nullptr;
     size_t cols_alloc = 0;
-    double* fcoef = nullptr;         // [n_cls][max_cols]
-    const double** xptr = nullptr;   // device arrays of the members' vector pointers
+    // one device block and its page-locked host image, copied in one transfer per batch:
+    // [n_cls][32] class coefficients, 32 x pointers, 32 y pointers, 32 accumulate flags
+    unsigned char* dpack = nullptr;
+    unsigned char* hpack = nullptr;
+    size_t pack_bytes = 0;
+    double* fcoef = nullptr;         // views into dpack
+    const double** xptr = nullptr;
     double** yptr = nullptr;
     int* accs = nullptr;
 };
@@ -114,20 +119,18 @@ qsi_status run_batch(qsi_family* f, const std::vector<qsi_family::Req*>& batch) 
         QSI_CUDA(cudaMalloc(&f->Y, (size_t)n * R * sizeof(double)));
         f->cols_alloc = (size_t)R;
     }
-    std::vector<double> coef((size_t)f->n_cls * R);
-    std::vector<const double*> xs(R);
-    std::vector<double*> ys(R);
-    std::vector<int> accs(R);
+    // the batch's coefficients ([class][R]), pointers and flags into the pinned image, then one copy
+    double* coef = reinterpret_cast<double*>(f->hpack);
+    const double** xs = reinterpret_cast<const double**>(f->hpack + ((unsigned char*)f->xptr - f->dpack));
+    double** ys = reinterpret_cast<double**>(f->hpack + ((unsigned char*)f->yptr - f->dpack));
+    int* accs = reinterpret_cast<int*>(f->hpack + ((unsigned char*)f->accs - f->dpack));
     for (int c = 0; c < R; ++c) {
         for (int k = 0; k < f->n_cls; ++k) coef[(size_t)k * R + c] = batch[c]->op->fcoef[k];
         xs[c] = batch[c]->x;
         ys[c] = batch[c]->y;
         accs[c] = batch[c]->accumulate;
     }
-    QSI_CUDA(cudaMemcpyAsync(f->fcoef, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, st));
-    QSI_CUDA(cudaMemcpyAsync(f->xptr, xs.data(), (size_t)R * sizeof(double*), cudaMemcpyHostToDevice, st));
-    QSI_CUDA(cudaMemcpyAsync(f->yptr, ys.data(), (size_t)R * sizeof(double*), cudaMemcpyHostToDevice, st));
-    QSI_CUDA(cudaMemcpyAsync(f->accs, accs.data(), (size_t)R * sizeof(int), cudaMemcpyHostToDevice, st));
+    QSI_CUDA(cudaMemcpyAsync(f->dpack, f->hpack, f->pack_bytes, cudaMemcpyHostToDevice, st));
     k_gather_columns<<<grid_for(n * R, 256), 256, 0, st>>>(f->xptr, R, n, f->X);
     QSI_CUDA(cudaGetLastError());
     qsi_status s = launch_family(T, f->X, f->Y, R, f->fcoef, 0, st);
@@ -248,10 +251,16 @@ extern "C" qsi_status qsi_family_create(qsi_basis* b, const qsi_term* terms, int
             delete f;
             return fail(QSI_INVALID_ARG, "qsi_family_create: diagonal terms other than single-site z");
         }
-        cudaError_t e = cudaMalloc(&f->fcoef, (size_t)n_classes * 32 * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&f->xptr, 32 * sizeof(double*));
-        if (e == cudaSuccess) e = cudaMalloc(&f->yptr, 32 * sizeof(double*));
-        if (e == cudaSuccess) e = cudaMalloc(&f->accs, 32 * sizeof(int));
+        const size_t coef_b = (size_t)n_classes * 32 * sizeof(double), ptr_b = 32 * sizeof(double*);
+        f->pack_bytes = coef_b + 2 * ptr_b + 32 * sizeof(int);
+        cudaError_t e = cudaMalloc(&f->dpack, f->pack_bytes);
+        if (e == cudaSuccess) e = cudaMallocHost(&f->hpack, f->pack_bytes);
+        if (e == cudaSuccess) {
+            f->fcoef = reinterpret_cast<double*>(f->dpack);
+            f->xptr = reinterpret_cast<const double**>(f->dpack + coef_b);
+            f->yptr = reinterpret_cast<double**>(f->dpack + coef_b + ptr_b);
+            f->accs = reinterpret_cast<int*>(f->dpack + coef_b + 2 * ptr_b);
+        }
         if (e != cudaSuccess) {
             qsi_family_destroy(f);
             return fail(QSI_OOM, "qsi_family_create: %s", cudaGetErrorString(e));
@@ -273,10 +282,8 @@ extern "C" qsi_status qsi_family_destroy(qsi_family* f) {
     if (f->tmpl) qsi_op_destroy(f->tmpl);
     cudaFree(f->X);
     cudaFree(f->Y);
-    cudaFree(f->fcoef);
-    cudaFree(f->xptr);
-    cudaFree(f->yptr);
-    cudaFree(f->accs);
+    cudaFree(f->dpack);
+    if (f->hpack) cudaFreeHost(f->hpack);
     delete f;
     return QSI_OK;
 }

@@ -6,8 +6,9 @@
 // reduced in a fixed order (per-block partial sums, then one block), so a solve
 // is deterministic for a given seed.  With precision QSI_F32 the stored Krylov
 // vectors are FP32 and the operator gathers FP32, while the working vector w,
-// every coefficient and the projected eigenproblem stay FP64; the Ritz pairs
-// are then polished by FP64 Rayleigh-Ritz steps with FP64 applies.
+// every coefficient and the projected eigenproblem stay FP64 (sums over FP32
+// vectors run in double-float on the FP32 pipe, about 2^-46 relative); the
+// Ritz pairs are then polished by FP64 Rayleigh-Ritz steps with FP64 applies.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -43,6 +44,60 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
     if (threadIdx.x == 0)
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) r += sh[k];
     return r;  // valid in thread 0
+}
+
+// Double-float accumulator (two FP32 words, about 2^-46 relative): a += x * (ch + cl), x an FP32 value, with an
+// error-free product and sum (TwoProd by fma, Knuth's TwoSum), all on the FP32 pipe.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ void df_fma(DF& a, float ch, float cl, float x) {
+    const float p = ch * x;
+    const float e = fmaf(ch, x, -p) + cl * x;
+    const float s = a.hi + p;
+    const float bb = s - a.hi;
+    const float err = (a.hi - (s - bb)) + (p - bb);
+    a.hi = s;
+    a.lo += err + e;
+}
+__device__ __forceinline__ double df_value(const DF& a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ void df_split(double v, float& h, float& l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+// FP32 Krylov vectors: the dots V_i . w of eight vectors per pass over the rows (w, FP64, split into a float pair
+// once per row and pass), accumulated in double-float: GB300's FP64 pipe runs at 1/64 of the FP32 rate, and the
+// FP64 form of these loops is bound by it.  |w|^2 stays an FP64 sum (one FMA per row).
+constexpr int kDotGroup = 8;
+__global__ void __launch_bounds__(kRedBlock) k_multidot_f32(const float* __restrict__ V, int64_t ld_v, int k,
+                                                            const double* __restrict__ w, int64_t n,
+                                                            double* __restrict__ partial) {
+    __shared__ double sh[32];
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+    for (int g0 = 0; g0 < k; g0 += kDotGroup) {
+        DF acc[kDotGroup];
+#pragma unroll
+        for (int u = 0; u < kDotGroup; ++u) acc[u] = DF{0.f, 0.f};
+        for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+            float wh, wl;
+            df_split(w[r], wh, wl);
+#pragma unroll
+            for (int u = 0; u < kDotGroup; ++u)
+                if (g0 + u < k) df_fma(acc[u], wh, wl, V[(int64_t)(g0 + u) * ld_v + r]);
+        }
+#pragma unroll
+        for (int u = 0; u < kDotGroup; ++u) {
+            if (g0 + u >= k) break;
+            const double s = block_sum(df_value(acc[u]), sh);
+            if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * (k + 1) + g0 + u] = s;
+        }
+    }
+    double acc = 0.0;
+    for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) acc += w[r] * w[r];
+    const double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * (k + 1) + k] = s;
 }
 
 // partial[b*(k+1) + i] = sum over this block's rows of V_i . w  (i < k), and
@@ -99,6 +154,29 @@ __global__ void __launch_bounds__(kRedBlock) k_multi_axpy(const VT* __restrict__
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
+// FP32 Krylov vectors: w -= sum_i h_i V_i with the sum formed in double-float (h_i as float pairs) and one FP64
+// subtraction per row; partial[b] = this block's sum of the new w^2.
+__global__ void __launch_bounds__(kRedBlock) k_multi_axpy_f32(const float* __restrict__ V, int64_t ld_v, int k,
+                                                              const double* __restrict__ h, double* __restrict__ w,
+                                                              int64_t n, double* __restrict__ partial) {
+    __shared__ double sh[32];
+    __shared__ float hh[256], hl[256];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) df_split(h[i], hh[i], hl[i]);
+    __syncthreads();
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+    double acc = 0.0;
+    for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+        DF s{0.f, 0.f};
+        for (int i = 0; i < k; ++i) df_fma(s, hh[i], hl[i], V[(int64_t)i * ld_v + r]);
+        const double v = w[r] - df_value(s);
+        w[r] = v;
+        acc += v * v;
+    }
+    const double t = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
 // out = w * (1/beta), converted to the storage type.
 template <typename VT>
 __global__ void k_scale_store(const double* __restrict__ w, const double* __restrict__ beta, VT* __restrict__ out,
@@ -137,11 +215,27 @@ __global__ void k_to_f64(const VT* __restrict__ v, double* __restrict__ w, int64
         w[r] = (double)v[r];
 }
 
-// V[:, 0..k) <- V[:, 0..m) * Y[0..m, 0..k) in place, row chunk by row chunk.
+// V[:, 0..k) <- V[:, 0..m) * Y[0..m, 0..k) in place, row chunk by row chunk.  FP32 vectors: each sum in
+// double-float with Y as float pairs (FP32 pipe); FP64 vectors: FP64.
 template <typename VT>
 __global__ void __launch_bounds__(128) k_rotate(VT* __restrict__ V, int64_t ld_v, int m, int k,
                                                 const double* __restrict__ Y, int64_t n) {
     extern __shared__ double ys[];  // m*k
+    if constexpr (sizeof(VT) == 4) {
+        float2* y2 = reinterpret_cast<float2*>(ys);
+        for (int i = threadIdx.x; i < m * k; i += blockDim.x) df_split(Y[i], y2[i].x, y2[i].y);
+        __syncthreads();
+        for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+            float row[160];
+            for (int j = 0; j < m; ++j) row[j] = (float)V[(int64_t)j * ld_v + r];
+            for (int i = 0; i < k; ++i) {
+                DF acc{0.f, 0.f};
+                for (int j = 0; j < m; ++j) df_fma(acc, y2[j * k + i].x, y2[j * k + i].y, row[j]);
+                V[(int64_t)i * ld_v + r] = (VT)(acc.hi + acc.lo);
+            }
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < m * k; i += blockDim.x) ys[i] = Y[i];
     __syncthreads();
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
@@ -359,7 +453,8 @@ struct Vecs {
     // h[0..k) = V_i . w and h[k] = |w|^2, copied to host
     template <typename VT>
     qsi_status dots(const VT* V, int64_t ldv, int k, const double* w, std::vector<double>& h) {
-        k_multidot<VT><<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, w, n, partial);
+        if constexpr (sizeof(VT) == 4) k_multidot_f32<<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, w, n, partial);
+        else k_multidot<VT><<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, w, n, partial);
         k_reduce_partials<<<1, 256, 0, st>>>(partial, kRedGrid, k + 1, red);
         h.resize(k + 1);
         QSI_CUDA(cudaMemcpyAsync(h.data(), red, (size_t)(k + 1) * 8, cudaMemcpyDeviceToHost, st));
@@ -370,7 +465,8 @@ struct Vecs {
     template <typename VT>
     qsi_status axpy(const VT* V, int64_t ldv, int k, const std::vector<double>& h, double* w, double& nrm2) {
         QSI_CUDA(cudaMemcpyAsync(red + 1, h.data(), (size_t)k * 8, cudaMemcpyHostToDevice, st));
-        k_multi_axpy<VT><<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, red + 1, w, n, partial);
+        if constexpr (sizeof(VT) == 4) k_multi_axpy_f32<<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, red + 1, w, n, partial);
+        else k_multi_axpy<VT><<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, red + 1, w, n, partial);
         k_reduce_partials<<<1, 256, 0, st>>>(partial, kRedGrid, 1, red);
         QSI_CUDA(cudaMemcpyAsync(&nrm2, red, 8, cudaMemcpyDeviceToHost, st));
         QSI_CUDA(cudaStreamSynchronize(st));
@@ -1264,9 +1360,11 @@ extern "C" qsi_status qsi_lanczos_solve(qsi_op* op, const qsi_lanczos_cfg* cfg, 
         if (!op || !cfg || !evals) return fail(QSI_INVALID_ARG, "qsi_lanczos_solve: null argument");
         if (report) std::memset(report, 0, sizeof(*report));
         if (cfg->precision == QSI_F32) {
-            // FP32 Krylov blocks through the batched apply (btrlan) when asked (block == 16), or by default for
-            // bases large enough that the apply dominates and nev fits two kept blocks
-            const bool block = cfg->block == kBlk || (cfg->block == 0 && op->basis->n >= (1 << 16) && cfg->nev <= 13);
+            // FP32 Krylov blocks through the batched apply (btrlan) when asked (block == 16); by default the
+            // single-vector solver with FP32 Krylov vectors (on the 96-spin sector the block solver needs seven
+            // times the vector applies of single-vector Lanczos for the same ten eigenpairs, more than the
+            // batched apply saves per vector)
+            const bool block = cfg->block == kBlk;
             if (block) return btrlan(op, *cfg, evals, evecs, report);
             if (cfg->block != 0 && cfg->block != 1) return fail(QSI_INVALID_ARG, "qsi_lanczos_solve: block must be 0, 1 or 16");
             return trlan<float>(op, *cfg, evals, evecs, report);
@@ -2029,9 +2127,9 @@ struct FtlmSector {
 //   P <- H C - beta_prev P;  alpha = <C, P>;  P <- P - alpha C;  beta = |P|;  P /= beta;  swap(P, C).
 // The one-launch sector apply takes -beta_prev per column as its accumulate coefficient (double-float), and its
 // column work is two passes (k_col_dots3: <C, P>, |P|^2 and |C|^2 in one read; k_ftlm_update_scaled:
-// P <- (P - alpha C) / beta), so a step moves 6 blocks beyond the apply's gathers against 9 for three blocks: the
-// one-launch form always takes two blocks unless three are asked for.  The per-sector launches instead have the
-// column pass also scale C by -beta for the next step, and take three blocks when they fit.
+// P <- (P - alpha C) / beta), so a step moves 6 blocks beyond the apply's gathers against 9 for three blocks,
+// though the accumulating apply is slower on small sectors: three blocks are taken when they fit.  The
+// per-sector launches instead have the column pass also scale C by -beta for the next step.
 template <typename VT>
 static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint64_t seed, double* alphas,
                            double* betas, int blocks) {
@@ -2046,10 +2144,10 @@ static qsi_status ftlm_run(qsi_op** ops, int ns, const int32_t* Rs, int M, uint6
         block_bytes += (size_t)ops[s]->basis->n * R * sizeof(VT);
         one_launch = one_launch && ops[s]->kernel == 1 && ops[s]->ff_accumulate;
     }
-    if (blocks == 0) {  // one launch: two blocks; else three blocks when they fit with 4 GiB to spare, else two
+    if (blocks == 0) {  // three blocks when they fit with 4 GiB to spare, else two
         size_t free_b = 0, total_b = 0;
         QSI_CUDA(cudaMemGetInfo(&free_b, &total_b));
-        blocks = (!one_launch && 3 * block_bytes + ((size_t)4 << 30) <= free_b) ? 3 : 2;
+        blocks = (3 * block_bytes + ((size_t)4 << 30) <= free_b) ? 3 : 2;
     }
     if (blocks != 2 && blocks != 3) return fail(QSI_INVALID_ARG, "ftlm: blocks must be 0, 2 or 3");
     const bool two = (blocks == 2);

@@ -32,8 +32,7 @@ def diagonalise(op: LazyOpSum, nev: int = 1, ncv: int = 15, tol: float = 1e-10, 
 
     ncv is clamped to the dimension and nev to ncv-1 (matrix_diag_bits.hpp:64-66).
     precision 'mixed' stores Krylov vectors in FP32 and polishes with FP64 Rayleigh-Ritz; block (mixed only):
-    16 = block Lanczos on FP32 blocks of 16 vectors through the batched apply, 1 = single-vector (FP64
-    coefficients), 0 = block for large bases when nev <= 13.
+    16 = block Lanczos on FP32 blocks of 16 vectors through the batched apply, 0 or 1 = single-vector.
     Returns (evals, evecs (dim x nev) or None, SolveReport).
     """
     n = op.rows()
@@ -81,8 +80,7 @@ def ftlm(ops, R, M: int = 100, seed: int = 0, precision: str = "mixed", blocks: 
     """Batched FTLM Lanczos recurrences: R[s] Rademacher vectors per sector, M steps.
 
     blocks: R-vector blocks kept per sector, 3 (H q in its own block) or 2 (in-place recurrence, R can double at
-    the same device memory); 0 = two when every sector takes the one-launch FP32 sector apply, else three when
-    they fit in free device memory, else two.
+    the same device memory); 0 = three when they fit in free device memory, else two.
     Returns a list of (alphas (R[s], M), betas (R[s], M)) per sector.
     """
     ops = list(ops)

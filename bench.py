@@ -440,7 +440,9 @@ def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves)
     out["cache_bytes"] = op.materialise(True)
     out["build_s"] = time.time() - t0
     y = torch.zeros_like(x)
+    torch.cuda.nvtx.range_push("timed_materialised")  # lets ncu capture these launches
     ms = event_ms(lambda: op.evaluate(x, y), args.steps, args.warmup)
+    torch.cuda.nvtx.range_pop()
     bpr = 16 + 8 + 8 * h + 8 + 4 * h  # the matrix-free bytes plus the cached column of each hit
     ach = n * bpr / (ms * 1e-3) / 1e9
     out["apply_fp64"] = {"value": n / (ms * 1e-3), "unit": "states/s", "ms_per_apply": ms,
@@ -457,7 +459,9 @@ def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves)
         except torch.cuda.OutOfMemoryError as e:
             out[f"batched_r{R}"] = {"skipped": str(e)[:160]}
             continue
+        torch.cuda.nvtx.range_push(f"timed_materialised_r{R}")
         ms = event_ms(lambda: op.apply_batched(X, Y), max(3, args.steps // 3), 1)
+        torch.cuda.nvtx.range_pop()
         bpr = 16 + R * 4 * (h + 2) + 4 * h
         ach = n * bpr / (ms * 1e-3) / 1e9
         out[f"batched_r{R}"] = {"value": n * R / (ms * 1e-3), "unit": "state-vectors/s", "ms_per_apply": ms,

@@ -432,6 +432,7 @@ def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves)
     materialises H with toSparseMatrix for diag_DOQSI_ham --algorithm sparse and ftlm_DOQSI_ham): the FP64
     single-vector apply (bitwise the matrix-free result), the batched FP32 applies, FTLM and optionally the
     eigen-solves, each as in the matrix-free legs."""
+    import numpy as np
     import torch
 
     out = {}

@@ -77,19 +77,26 @@ __global__ void __launch_bounds__(kRedBlock) k_multidot_f32(const float* __restr
     const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
     const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
     for (int g0 = 0; g0 < k; g0 += kDotGroup) {
+        // the group's vectors (the last repeated past k, its sums unused): every load unconditional, so a
+        // row's kDotGroup + 1 loads are in flight together
+        const int nv = min(kDotGroup, k - g0);
+        const float* vp[kDotGroup];
+#pragma unroll
+        for (int u = 0; u < kDotGroup; ++u) vp[u] = V + (int64_t)(g0 + min(u, nv - 1)) * ld_v;
         DF acc[kDotGroup];
 #pragma unroll
         for (int u = 0; u < kDotGroup; ++u) acc[u] = DF{0.f, 0.f};
         for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+            const double wd = __ldg(w + r);
+            float v[kDotGroup];
+#pragma unroll
+            for (int u = 0; u < kDotGroup; ++u) v[u] = __ldg(vp[u] + r);
             float wh, wl;
-            df_split(w[r], wh, wl);
+            df_split(wd, wh, wl);
 #pragma unroll
-            for (int u = 0; u < kDotGroup; ++u)
-                if (g0 + u < k) df_fma(acc[u], wh, wl, V[(int64_t)(g0 + u) * ld_v + r]);
+            for (int u = 0; u < kDotGroup; ++u) df_fma(acc[u], wh, wl, v[u]);
         }
-#pragma unroll
-        for (int u = 0; u < kDotGroup; ++u) {
-            if (g0 + u >= k) break;
+        for (int u = 0; u < nv; ++u) {
             const double s = block_sum(df_value(acc[u]), sh);
             if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * (k + 1) + g0 + u] = s;
         }
@@ -154,22 +161,34 @@ __global__ void __launch_bounds__(kRedBlock) k_multi_axpy(const VT* __restrict__
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-// FP32 Krylov vectors: w -= sum_i h_i V_i with the sum formed in double-float (h_i as float pairs) and one FP64
-// subtraction per row; partial[b] = this block's sum of the new w^2.
+// FP32 Krylov vectors: w -= sum_i h_i V_i with the sum formed in double-float (h_i as float pairs; four
+// interleaved partial sums combined in a fixed order, so four loads per row are in flight and the dependent chain
+// is a quarter as long) and one FP64 subtraction per row; partial[b] = this block's sum of the new w^2.
 __global__ void __launch_bounds__(kRedBlock) k_multi_axpy_f32(const float* __restrict__ V, int64_t ld_v, int k,
                                                               const double* __restrict__ h, double* __restrict__ w,
                                                               int64_t n, double* __restrict__ partial) {
     __shared__ double sh[32];
     __shared__ float hh[256], hl[256];
-    for (int i = threadIdx.x; i < k; i += blockDim.x) df_split(h[i], hh[i], hl[i]);
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        hh[i] = hl[i] = 0.f;
+        if (i < k) df_split(h[i], hh[i], hl[i]);
+    }
     __syncthreads();
     const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
     const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+    const int k4 = (k + 3) & ~3;
     double acc = 0.0;
     for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
-        DF s{0.f, 0.f};
-        for (int i = 0; i < k; ++i) df_fma(s, hh[i], hl[i], V[(int64_t)i * ld_v + r]);
-        const double v = w[r] - df_value(s);
+        DF s[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        for (int i = 0; i < k4; i += 4) {
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = __ldg(V + (int64_t)min(i + u, k - 1) * ld_v + r);  // h = 0 past k
+#pragma unroll
+            for (int u = 0; u < 4; ++u) df_fma(s[u], hh[i + u], hl[i + u], v[u]);
+        }
+        const double t = (df_value(s[0]) + df_value(s[1])) + (df_value(s[2]) + df_value(s[3]));
+        const double v = w[r] - t;
         w[r] = v;
         acc += v * v;
     }

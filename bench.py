@@ -404,7 +404,11 @@ def ftlm_rate(q, ops, R, prec, M1, blocks=0):
     for M in (M0, M1):
         torch.cuda.synchronize()
         t0 = time.time()
+        if M == M1:
+            torch.cuda.nvtx.range_push(f"timed_ftlm_{prec}")  # lets ncu list one run's launches
         q.ftlm(ops, [R], M=M, seed=1, precision=prec, blocks=blocks)
+        if M == M1:
+            torch.cuda.nvtx.range_pop()
         t[M] = time.time() - t0
     per = (t[M1] - t[M0]) / (M1 - M0)
     return {"R": R, "precision": prec, "ms_per_step": per * 1e3, "vec_steps_per_s": R / per,

@@ -196,7 +196,108 @@ __global__ void __launch_bounds__(kRedBlock) k_multi_axpy_f32(const float* __res
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
 }
 
-// out = w * (1/beta), converted to the storage type.
+// The working vector of the FP32 solve as a double-float pair array: split once per Lanczos step, then the
+// reorthogonalisation (dots, updates, norms) and the store of the next Krylov vector run on the FP32 pipe with no
+// FP64 operation per row.
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) {  // (a - b) in double-float, renormalised
+    const float s = a.x - b.x;
+    const float bb = s - a.x;
+    const float e = ((a.x - (s - bb)) + (-b.x - bb)) + (a.y - b.y);
+    const float hi = s + e;
+    return make_float2(hi, e - (hi - s));
+}
+__global__ void k_split_f64(const double* __restrict__ w, float2* __restrict__ wf, int64_t n) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        float h, l;
+        df_split(w[r], h, l);
+        wf[r] = make_float2(h, l);
+    }
+}
+// partial[b*(k+1) + i] = V_i . w (i < k) and partial[b*(k+1) + k] = |w|^2 over this block's rows, w a pair array.
+__global__ void __launch_bounds__(kRedBlock) k_multidot_df(const float* __restrict__ V, int64_t ld_v, int k,
+                                                           const float2* __restrict__ wf, int64_t n,
+                                                           double* __restrict__ partial) {
+    __shared__ double sh[32];
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+    for (int g0 = 0; g0 < k; g0 += kDotGroup) {
+        const int nv = min(kDotGroup, k - g0);
+        const float* vp[kDotGroup];
+#pragma unroll
+        for (int u = 0; u < kDotGroup; ++u) vp[u] = V + (int64_t)(g0 + min(u, nv - 1)) * ld_v;
+        DF acc[kDotGroup];
+#pragma unroll
+        for (int u = 0; u < kDotGroup; ++u) acc[u] = DF{0.f, 0.f};
+        for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+            const float2 wv = __ldg(wf + r);
+            float v[kDotGroup];
+#pragma unroll
+            for (int u = 0; u < kDotGroup; ++u) v[u] = __ldg(vp[u] + r);
+#pragma unroll
+            for (int u = 0; u < kDotGroup; ++u) df_fma(acc[u], wv.x, wv.y, v[u]);
+        }
+        for (int u = 0; u < nv; ++u) {
+            const double t = block_sum(df_value(acc[u]), sh);
+            if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * (k + 1) + g0 + u] = t;
+        }
+    }
+    DF nrm{0.f, 0.f};
+    for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+        const float2 wv = __ldg(wf + r);
+        df_fma(nrm, wv.x, 2.f * wv.y, wv.x);  // hi^2 + 2 hi lo
+    }
+    const double t = block_sum(df_value(nrm), sh);
+    if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * (k + 1) + k] = t;
+}
+// w -= sum_i h_i V_i on the pair array (the sum as in k_multi_axpy_f32, the subtraction in double-float);
+// partial[b] = this block's |w|^2.
+__global__ void __launch_bounds__(kRedBlock) k_multi_axpy_df(const float* __restrict__ V, int64_t ld_v, int k,
+                                                             const double* __restrict__ h, float2* __restrict__ wf,
+                                                             int64_t n, double* __restrict__ partial) {
+    __shared__ double sh[32];
+    __shared__ float hh[256], hl[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        hh[i] = hl[i] = 0.f;
+        if (i < k) df_split(h[i], hh[i], hl[i]);
+    }
+    __syncthreads();
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+    const int k4 = (k + 3) & ~3;
+    DF nrm{0.f, 0.f};
+    for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
+        DF s[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        for (int i = 0; i < k4; i += 4) {
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = __ldg(V + (int64_t)min(i + u, k - 1) * ld_v + r);  // h = 0 past k
+#pragma unroll
+            for (int u = 0; u < 4; ++u) df_fma(s[u], hh[i + u], hl[i + u], v[u]);
+        }
+        float2 t = df_sub(make_float2(s[0].hi, s[0].lo), make_float2(-s[1].hi, -s[1].lo));
+        t = df_sub(t, make_float2(-s[2].hi, -s[2].lo));
+        t = df_sub(t, make_float2(-s[3].hi, -s[3].lo));
+        const float2 wv = df_sub(wf[r], t);
+        wf[r] = wv;
+        df_fma(nrm, wv.x, 2.f * wv.y, wv.x);
+    }
+    const double t = block_sum(df_value(nrm), sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+// out = w / |w| rounded to FP32 (beta_sq: the squared norm on the device).
+__global__ void k_scale_store_df(const float2* __restrict__ wf, const double* __restrict__ beta_sq,
+                                 float* __restrict__ out, int64_t n) {
+    const double inv = 1.0 / sqrt(*beta_sq);
+    float ih, il;
+    df_split(inv, ih, il);
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const float2 wv = wf[r];
+        const float p = wv.x * ih;
+        out[r] = p + (fmaf(wv.x, ih, -p) + (wv.x * il + wv.y * ih));
+    }
+}
+
+// out = w * (1/beta), converted to the storage type.// out = w * (1/beta), converted to the storage type.
 template <typename VT>
 __global__ void k_scale_store(const double* __restrict__ w, const double* __restrict__ beta, VT* __restrict__ out,
                               int64_t n) {
@@ -480,6 +581,24 @@ struct Vecs {
         QSI_CUDA(cudaStreamSynchronize(st));
         return QSI_OK;
     }
+    // FP32 Krylov vectors with the working vector as a pair array: h[0..k) = V_i . w, h[k] = |w|^2
+    qsi_status dots_df(const float* V, int64_t ldv, int k, const float2* wf, std::vector<double>& h) {
+        k_multidot_df<<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, wf, n, partial);
+        k_reduce_partials<<<1, 256, 0, st>>>(partial, kRedGrid, k + 1, red);
+        h.resize(k + 1);
+        QSI_CUDA(cudaMemcpyAsync(h.data(), red, (size_t)(k + 1) * 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+        return QSI_OK;
+    }
+    // ... w -= V h; returns |w|^2 (device copy left in red[0])
+    qsi_status axpy_df(const float* V, int64_t ldv, int k, const std::vector<double>& h, float2* wf, double& nrm2) {
+        QSI_CUDA(cudaMemcpyAsync(red + 1, h.data(), (size_t)k * 8, cudaMemcpyHostToDevice, st));
+        k_multi_axpy_df<<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, red + 1, wf, n, partial);
+        k_reduce_partials<<<1, 256, 0, st>>>(partial, kRedGrid, 1, red);
+        QSI_CUDA(cudaMemcpyAsync(&nrm2, red, 8, cudaMemcpyDeviceToHost, st));
+        QSI_CUDA(cudaStreamSynchronize(st));
+        return QSI_OK;
+    }
     // w -= V h ; returns |w|^2 (device copy left in red[0])
     template <typename VT>
     qsi_status axpy(const VT* V, int64_t ldv, int k, const std::vector<double>& h, double* w, double& nrm2) {
@@ -714,6 +833,18 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     QSI_CUDA(V.alloc((size_t)(m + 1) * n, st));
     QSI_CUDA(w.alloc((size_t)n, st));
     QSI_CUDA(dY.alloc((size_t)m * m, st));
+    constexpr bool kDF = sizeof(VT) == 4;  // FP32 vectors: reorthogonalise w as a double-float pair array
+    DevBuf<float2> wf;
+    if (kDF) QSI_CUDA(wf.alloc((size_t)n, st));
+    // the reorthogonalisation's dots and updates, on w (FP64) or on its pair array (FP32 vectors)
+    auto rdots = [&](int k, std::vector<double>& hv) -> qsi_status {
+        if constexpr (kDF) return vx.dots_df(reinterpret_cast<const float*>(V.p), n, k, wf.p, hv);
+        else return vx.dots<VT>(V.p, n, k, w.p, hv);
+    };
+    auto raxpy = [&](int k, const std::vector<double>& hv, double& nrm2) -> qsi_status {
+        if constexpr (kDF) return vx.axpy_df(reinterpret_cast<const float*>(V.p), n, k, hv, wf.p, nrm2);
+        else return vx.axpy<VT>(V.p, n, k, hv, w.p, nrm2);
+    };
     auto vec = [&](int j) { return V.p + (size_t)j * n; };
     // start vector N(0,1), normalised (stored)
     k_randn<<<grid_for(n, 256), 256, 0, st>>>(w.p, n, cfg.seed, 0);
@@ -735,22 +866,23 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
             if (s) return s;
             ++applies;
             clk.mark("apply");
+            if (kDF) k_split_f64<<<grid_for(n, 256), 256, 0, st>>>(w.p, wf.p, n);
             // full reorthogonalisation: classical Gram-Schmidt against v_0..v_j, repeated once
             // when the norm drops by more than 1/sqrt(2) (DGKS criterion)
-            s = vx.dots<VT>(V.p, n, j + 1, w.p, h);
+            s = rdots(j + 1, h);
             if (s) return s;
             double before = h[j + 1];
             double a = h[j];
             std::vector<double> hh(h.begin(), h.begin() + j + 1);
             double nrm2 = 0;
-            s = vx.axpy<VT>(V.p, n, j + 1, hh, w.p, nrm2);
+            s = raxpy(j + 1, hh, nrm2);
             if (s) return s;
             if (nrm2 < 0.5 * before) {
-                s = vx.dots<VT>(V.p, n, j + 1, w.p, h);
+                s = rdots(j + 1, h);
                 if (s) return s;
                 a += h[j];
                 hh.assign(h.begin(), h.begin() + j + 1);
-                s = vx.axpy<VT>(V.p, n, j + 1, hh, w.p, nrm2);
+                s = raxpy(j + 1, hh, nrm2);
                 if (s) return s;
             }
             alpha[j] = a;
@@ -759,17 +891,21 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
                 // invariant subspace: continue from a fresh random direction orthogonal to V
                 b = 0.0;
                 k_randn<<<grid_for(n, 256), 256, 0, st>>>(w.p, n, cfg.seed + 7919 * (uint64_t)(j + 1 + restarts * m), 0);
+                if (kDF) k_split_f64<<<grid_for(n, 256), 256, 0, st>>>(w.p, wf.p, n);
                 for (int pass = 0; pass < 2; ++pass) {
-                    s = vx.dots<VT>(V.p, n, j + 1, w.p, h);
+                    s = rdots(j + 1, h);
                     if (s) return s;
                     hh.assign(h.begin(), h.begin() + j + 1);
-                    s = vx.axpy<VT>(V.p, n, j + 1, hh, w.p, nrm2);
+                    s = raxpy(j + 1, hh, nrm2);
                     if (s) return s;
                 }
             }
             beta[j] = b;
             QSI_CUDA(cudaMemcpyAsync(vx.red, &nrm2, 8, cudaMemcpyHostToDevice, st));
-            k_scale_store<VT><<<grid_for(n, 256), 256, 0, st>>>(w.p, vx.red, vec(j + 1), n);
+            if constexpr (kDF)
+                k_scale_store_df<<<grid_for(n, 256), 256, 0, st>>>(wf.p, vx.red, reinterpret_cast<float*>(vec(j + 1)), n);
+            else
+                k_scale_store<VT><<<grid_for(n, 256), 256, 0, st>>>(w.p, vx.red, vec(j + 1), n);
             clk.mark("orthogonalise");
         }
         // projected matrix: arrowhead (kept Ritz values + couplings) then tridiagonal

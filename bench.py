@@ -275,6 +275,21 @@ def ftlm_sectors_leg(args):
         errs[nm] = {"max_abs_dC": float(np.abs(th32["C"] - th64["C"]).max()),
                     "max_C": float(np.abs(th64["C"]).max()), "e_ref_diff": abs(th32["e_ref"] - th64["e_ref"])}
     out["mixed_vs_f64"] = errs
+    # the same runs on the materialised sectors, as the reference's ftlm_DOQSI_ham materialises H first
+    mat = {"cache_bytes": sum(op.materialise(True) for op in ops)}
+    for prec in ("mixed", "f64"):
+        q.ftlm(ops, [R] * len(ops), M=3, seed=1, precision=prec)
+        torch_sync()
+        t0 = time.time()
+        rm = q.ftlm(ops, [R] * len(ops), M=M, seed=1, precision=prec)
+        dt = time.time() - t0
+        mat[prec] = {"seconds": dt, "vec_steps_per_s": len(ops) * R * M / dt,
+                     "bitwise_equal_to_matrix_free": all(np.array_equal(a[0], c[0]) and np.array_equal(a[1], c[1])
+                                                         for a, c in zip(rm, res[prec]))}
+    mat["speedup_mixed_vs_f64"] = mat["f64"]["seconds"] / mat["mixed"]["seconds"]
+    for op in ops:
+        op.materialise(False)
+    out["materialised"] = mat
     return out
 
 

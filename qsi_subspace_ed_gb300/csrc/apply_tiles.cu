@@ -818,6 +818,90 @@ qsi_status build_hash(qsi_basis* b) {
 }
 
 // ------------------------------------------------------------------ lookup cache (materialised operator)
+// Single-vector apply of a materialised operator: a sliced-ELL product over the cache alone (no states, no
+// admission test): lane l of tile t sums row 32 t + l as the diagonal, then its entries in cache order (the
+// admission order of the tile kernels) with coefficient +-cs of the entry's term and the entry's sign, the same
+// sums in the same order as k_apply_tile, so the result is bitwise the matrix-free one.
+template <typename XT, typename YT, typename TT>
+__global__ void __launch_bounds__(256) k_apply_cached(const PullTerm* __restrict__ terms, int n_off,
+                                                      const double* __restrict__ diag, CacheView C,
+                                                      const TT* __restrict__ tids, int64_t n, const XT* __restrict__ x,
+                                                      YT* __restrict__ y, int accumulate) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* cs = reinterpret_cast<double*>(smem_raw);
+    for (int k = threadIdx.x; k < n_off; k += blockDim.x) cs[k] = terms[k].cs;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int64_t ntiles = (n + 31) >> 5;
+    for (int64_t tile = (int64_t)blockIdx.x * nw + wid; tile < ntiles; tile += (int64_t)gridDim.x * nw) {
+        const int64_t row = tile * 32 + lane;
+        const bool valid = row < n;
+        const uint64_t o0 = C.off[tile];
+        const int width = (int)(C.off[tile + 1] - o0);
+        double acc = valid ? diag[row] * (double)x[row] : 0.0;
+        const uint32_t* cp = C.cols + o0 * 32 + lane;
+        const TT* tp = tids + o0 * 32 + lane;
+        constexpr int kU = 8;  // entries in flight per lane
+        for (int k0 = 0; k0 < width; k0 += kU) {
+            uint32_t c[kU];
+            TT t[kU];
+            XT xv[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const bool in = k0 + u < width;
+                c[u] = in ? __ldg(cp + (uint64_t)(k0 + u) * 32) : kEmpty;
+                t[u] = in ? __ldg(tp + (uint64_t)(k0 + u) * 32) : (TT)0;
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) xv[u] = (c[u] != kEmpty) ? x[c[u] & ~kCacheNeg] : (XT)0;
+#pragma unroll
+            for (int u = 0; u < kU; ++u)
+                if (c[u] != kEmpty && above_tol(xv[u])) {
+                    const double v = cs[t[u]];
+                    acc += ((c[u] & kCacheNeg) ? -v : v) * (double)xv[u];
+                }
+        }
+        if (valid) {
+            if (accumulate) acc += (double)y[row];
+            y[row] = (YT)acc;
+        }
+    }
+}
+
+static qsi_status launch_cached(qsi_op* op, const void* x, void* y, int xdtype, int ydtype, int accumulate,
+                                cudaStream_t st) {
+    const int64_t n = op->basis->n;
+    const int block = 256, nw = block / 32;
+    const int64_t ntiles = (n + 31) / 32;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int bps = op->tune[0].grid_bps > 0 ? op->tune[0].grid_bps : 8;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * bps));
+    const size_t smem = (size_t)std::max(op->n_pull, 1) * 8;
+    const CacheView C{op->d_cache_cols, op->d_cache_off};
+    auto go = [&](auto xt, auto yt, auto tt) {
+        using XT = decltype(xt);
+        using YT = decltype(yt);
+        using TT = decltype(tt);
+        auto k = k_apply_cached<XT, YT, TT>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, block, smem, st>>>(op->d_pull, op->n_pull, op->d_diag, C, (const TT*)op->d_cache_tid, n,
+                                     (const XT*)x, (YT*)y, accumulate);
+    };
+    auto by_tid = [&](auto xt, auto yt) {
+        if (op->cache_tid_bytes == 1) go(xt, yt, uint8_t{});
+        else go(xt, yt, uint16_t{});
+    };
+    if (xdtype == QSI_F64) by_tid(double{}, double{});
+    else if (ydtype == QSI_F64) by_tid(float{}, double{});
+    else by_tid(float{}, float{});
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(QSI_CUDA_ERROR, "cached apply launch: %s", cudaGetErrorString(e));
+    return QSI_OK;
+}
+
+
 // Admitted terms of the tile's widest row: the tile's number of cache lines.
 __global__ void __launch_bounds__(256) k_cache_widths(TileParams P, uint64_t* __restrict__ width) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -843,9 +927,9 @@ __global__ void __launch_bounds__(256) k_cache_widths(TileParams P, uint64_t* __
 
 // The column of every admitted term of every row (kEmpty outside the basis), looked up with lk, at the positions
 // LookupCache reads them from.
-template <class LK>
+template <class LK, typename TT>
 __global__ void __launch_bounds__(256) k_cache_fill(TileParams P, LK lk, const uint64_t* __restrict__ off,
-                                                    uint32_t* __restrict__ cols) {
+                                                    uint32_t* __restrict__ cols, TT* __restrict__ tids) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TileSmem S = stage_terms(P, smem_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -861,19 +945,23 @@ __global__ void __launch_bounds__(256) k_cache_fill(TileParams P, LK lk, const u
         tile_spin_words(s, P.nwords, lane, spinw);
         for (int r = 0; r < n_rounds; ++r) adm[r * 32 + lane] = tile_admitted(S, P.n_off, r * 32, lane, vmask, spinw);
         uint32_t* out = cols + off[tile] * 32 + lane;
+        TT* tout = tids + off[tile] * 32 + lane;
         int kk = 0, r = 0;
         uint32_t a = adm[lane];
         while (true) {
             constexpr int kNB = 4;
+            int tt[kNB];
             uint64_t tl[kNB], th[kNB];
             int64_t J[kNB];
             int nh = 0;
 #pragma unroll
             for (int u = 0; u < kNB; ++u) {
+                tt[u] = 0;
                 tl[u] = th[u] = 0;
                 while (!a && r + 1 < n_rounds) a = adm[++r * 32 + lane];
                 if (a) {
-                    const PullTerm& T = S.terms[r * 32 + __ffs(a) - 1];
+                    tt[u] = r * 32 + __ffs(a) - 1;
+                    const PullTerm& T = S.terms[tt[u]];
                     a &= a - 1;
                     tl[u] = s.x ^ T.x0;
                     th[u] = s.y ^ T.x1;
@@ -884,7 +972,13 @@ __global__ void __launch_bounds__(256) k_cache_fill(TileParams P, LK lk, const u
             lk.template find_batch<kNB>(tl, th, J, nh);
 #pragma unroll
             for (int u = 0; u < kNB; ++u)
-                if (u < nh) out[(uint64_t)(kk + u) * 32] = (J[u] < 0) ? kEmpty : (uint32_t)J[u];
+                if (u < nh) {
+                    // the column, with the sign of the term's matrix element on this row in the top bit
+                    const PullTerm& T = S.terms[tt[u]];
+                    const bool neg = T.has_z && ((__popcll(~s.x & T.z0) + __popcll(~s.y & T.z1)) & 1);
+                    out[(uint64_t)(kk + u) * 32] = (J[u] < 0) ? kEmpty : ((uint32_t)J[u] | (neg ? kCacheNeg : 0u));
+                    tout[(uint64_t)(kk + u) * 32] = (TT)tt[u];
+                }
             kk += nh;
         }
         __syncwarp();
@@ -1136,9 +1230,11 @@ qsi_status launch_family(qsi_op* tmpl, const double* x, double* y, int R, const 
 
 qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdtype, int ydtype, int accumulate,
                               cudaStream_t st) {
-    if (op->d_cache_cols)
+    if (op->d_cache_cols) {
+        if (R == 1) return launch_cached(op, x, y, xdtype, ydtype, accumulate, st);
         return launch_tiles_lk(op, LookupCache{CacheView{op->d_cache_cols, op->d_cache_off}}, x, y, R, xdtype, ydtype,
                                accumulate, st);
+    }
     if (op->basis->d_hash && op->tune[R > 1].use_hash) return launch_tiles_lk(op, LookupHash{op->basis->hview()}, x, y, R, xdtype, ydtype, accumulate, st);
     return launch_tiles_lk(op, LookupTable{op->basis->view()}, x, y, R, xdtype, ydtype, accumulate, st);
 }
@@ -1147,8 +1243,10 @@ qsi_status launch_apply_tiles(qsi_op* op, const void* x, void* y, int R, int xdt
 qsi_status materialise(qsi_op* op, bool enable, int64_t* bytes) {
     cudaFree(op->d_cache_cols);
     cudaFree(op->d_cache_off);
+    cudaFree(op->d_cache_tid);
     op->d_cache_cols = nullptr;
     op->d_cache_off = nullptr;
+    op->d_cache_tid = nullptr;
     op->cache_entries = 0;
     if (enable) {
         if (op->kernel != 1) return fail(QSI_INVALID_ARG, "qsi_op_materialise: the cache serves the tile kernels (kernel 1)");
@@ -1181,30 +1279,42 @@ qsi_status materialise(qsi_op* op, bool enable, int64_t* bytes) {
         cudaFreeAsync(tmp, st);
         cudaFreeAsync(width, st);
         const size_t n_entries = (size_t)lines * 32;
+        op->cache_tid_bytes = op->n_pull <= 256 ? 1 : 2;
         cudaError_t e = cudaMalloc(&op->d_cache_cols, std::max<size_t>(n_entries, 1) * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&op->d_cache_tid, std::max<size_t>(n_entries, 1) * op->cache_tid_bytes);
         if (e != cudaSuccess) {
             cudaFree(op->d_cache_off);
+            cudaFree(op->d_cache_cols);
             op->d_cache_off = nullptr;
             op->d_cache_cols = nullptr;
+            op->d_cache_tid = nullptr;
             return fail(e == cudaErrorMemoryAllocation ? QSI_OOM : QSI_CUDA_ERROR,
-                        "qsi_op_materialise: %zu bytes for the cache: %s", n_entries * 4, cudaGetErrorString(e));
+                        "qsi_op_materialise: %zu bytes for the cache: %s", n_entries * (4 + op->cache_tid_bytes),
+                        cudaGetErrorString(e));
         }
         QSI_CUDA(cudaMemsetAsync(op->d_cache_cols, 0xFF, n_entries * 4, st));  // the lanes below their tile's width
+        QSI_CUDA(cudaMemsetAsync(op->d_cache_tid, 0, n_entries * op->cache_tid_bytes, st));
         const size_t smem_f = term_smem(op) + (size_t)nw * (512 + (size_t)n_rounds * 128);
+        auto fill = [&](auto lk, auto* tids) {
+            auto k = k_cache_fill<decltype(lk), std::remove_pointer_t<decltype(tids)>>;
+            set_smem(k, smem_f);
+            k<<<grid, block, smem_f, st>>>(P, lk, op->d_cache_off, op->d_cache_cols, tids);
+        };
         if (op->basis->d_hash) {
-            auto k = k_cache_fill<LookupHash>;
-            set_smem(k, smem_f);
-            k<<<grid, block, smem_f, st>>>(P, LookupHash{op->basis->hview()}, op->d_cache_off, op->d_cache_cols);
+            if (op->cache_tid_bytes == 1) fill(LookupHash{op->basis->hview()}, (uint8_t*)op->d_cache_tid);
+            else fill(LookupHash{op->basis->hview()}, (uint16_t*)op->d_cache_tid);
         } else {
-            auto k = k_cache_fill<LookupTable>;
-            set_smem(k, smem_f);
-            k<<<grid, block, smem_f, st>>>(P, LookupTable{op->basis->view()}, op->d_cache_off, op->d_cache_cols);
+            if (op->cache_tid_bytes == 1) fill(LookupTable{op->basis->view()}, (uint8_t*)op->d_cache_tid);
+            else fill(LookupTable{op->basis->view()}, (uint16_t*)op->d_cache_tid);
         }
         QSI_CUDA(cudaGetLastError());
         QSI_CUDA(cudaStreamSynchronize(st));
         op->cache_entries = n_entries;
     }
-    if (bytes) *bytes = op->d_cache_cols ? (int64_t)(op->cache_entries * 4 + ((op->basis->n + 31) / 32 + 1) * 8) : 0;
+    if (bytes)
+        *bytes = op->d_cache_cols ? (int64_t)(op->cache_entries * (4 + op->cache_tid_bytes) +
+                                              ((op->basis->n + 31) / 32 + 1) * 8)
+                                  : 0;
     return QSI_OK;
 }
 

@@ -606,6 +606,7 @@ extern "C" qsi_status qsi_op_destroy(qsi_op* op) {
     cudaFree(op->d_y);
     cudaFree(op->d_cache_cols);
     cudaFree(op->d_cache_off);
+    cudaFree(op->d_cache_tid);
     if (op->stream) cudaStreamDestroy(op->stream);
     delete op;
     return QSI_OK;

@@ -250,9 +250,12 @@ struct LookupHash {
 };
 
 // The materialised operator's lookup cache (qsi_op_materialise): the column of every admitted term of every row,
-// kEmpty for a column outside the basis, in the order the tile kernels visit them.  Tile t's entries start at
+// kEmpty for a column outside the basis, in the order the tile kernels visit them (with the term's index and the
+// sign of its matrix element on the row beside it, for the single-vector kernel that reads only the cache).  Tile t's entries start at
 // 32 * off[t]; the row in lane l has its k-th admitted term at 32 * (off[t] + k) + l, so a warp reads one
 // coalesced 128-byte line per admission ordinal.  Results are those of the lookups it replaces, bit for bit.
+// Bit 31 of a cached column holds the sign of the term's matrix element on that row (columns are below 2^31).
+constexpr uint32_t kCacheNeg = 0x80000000u;
 struct CacheView {
     const uint32_t* cols;
     const uint64_t* off;
@@ -268,7 +271,7 @@ struct LookupCache {
         for (int u = 0; u < NB; ++u)
             if (u < n) {
                 const uint32_t c = __ldg(C.cols + cur + (uint64_t)(k0 + u) * 32);
-                J[u] = (c == kEmpty) ? -1 : (int64_t)c;
+                J[u] = (c == kEmpty) ? -1 : (int64_t)(c & ~kCacheNeg);
             }
     }
 };

@@ -54,6 +54,8 @@ struct qsi_op {
     float2* d_diag_ff = nullptr;    // the same as double-float pairs (FP32 batched kernel)
     uint32_t* d_cache_cols = nullptr;  // lookup cache of the materialised operator (qsi_op_materialise), or null
     uint64_t* d_cache_off = nullptr;   // its tile offsets in 32-entry lines
+    void* d_cache_tid = nullptr;       // the term index of every entry (uint8, or uint16 beyond 256 terms)
+    int cache_tid_bytes = 1;
     size_t cache_entries = 0;
     cudaStream_t stream = nullptr;
     int device = 0;        // the device current at qsi_op_create (owner of every buffer and of the stream)

@@ -446,7 +446,7 @@ def event_ms(fn, steps, warmup):
     return sum(a.elapsed_time(b) for a, b in ev) / steps
 
 
-def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves):
+def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves, workload):
     """The operator materialised (qsi_op_materialise: the column of every admitted term stored, as the reference
     materialises H with toSparseMatrix for diag_DOQSI_ham --algorithm sparse and ftlm_DOQSI_ham): the FP64
     single-vector apply (bitwise the matrix-free result), the batched FP32 applies, FTLM and optionally the
@@ -463,13 +463,14 @@ def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves)
     torch.cuda.nvtx.range_push("timed_materialised")  # lets ncu capture these launches
     ms = event_ms(lambda: op.evaluate(x, y), args.steps, args.warmup)
     torch.cuda.nvtx.range_pop()
-    bpr = 16 + 8 + 8 * h + 8 + 4 * h  # the matrix-free bytes plus the cached column of each hit
+    bpr = 16 + 8 + 8 * h + 8 + 5 * h  # the matrix-free bytes plus each hit's cached column and term index
     ach = n * bpr / (ms * 1e-3) / 1e9
     out["apply_fp64"] = {"value": n / (ms * 1e-3), "unit": "states/s", "ms_per_apply": ms,
                          "bitwise_equal_to_matrix_free": bool(np.array_equal(y.cpu().numpy(), y_host)),
                          "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                                       "peak_kind": peak_kind, "bytes_per_row": bpr,
-                                      "kernel": "k_apply_tile<double,double,LookupCache>"}}
+                                      "kernel": "k_apply_cached<double,double,uint8>",
+                                      "traffic": measured_traffic(workload, "k_apply_cached<double,double,uint8>", n)}}
     del y
     for R in [int(v) for v in str(args.R).split(",") if v]:
         torch.cuda.empty_cache()
@@ -484,9 +485,11 @@ def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves)
         torch.cuda.nvtx.range_pop()
         bpr = 16 + R * 4 * (h + 2) + 4 * h
         ach = n * bpr / (ms * 1e-3) / 1e9
+        kn = f"k_apply_tile_batched<float,LookupCache,FF,16-byte gathers x{op.tuning(1)['vec_width'] or 4}> R={R}"
         out[f"batched_r{R}"] = {"value": n * R / (ms * 1e-3), "unit": "state-vectors/s", "ms_per_apply": ms,
                                 "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                                             "frac": ach / peak, "peak_kind": peak_kind, "bytes_per_row": bpr}}
+                                             "frac": ach / peak, "peak_kind": peak_kind, "bytes_per_row": bpr,
+                                             "kernel": kn, "traffic": measured_traffic(workload, kn, n)}}
         del X, Y
     torch.cuda.empty_cache()
     if "ftlm" in args.legs:
@@ -749,7 +752,8 @@ def run_ours(args):
     if "materialised" in legs and rank == 0:
         if "x" not in locals():  # the lanczos leg released the headline's vectors
             x = torch.from_numpy(x_host).to(dev)
-        line["materialised"] = materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, "lanczos" in legs)
+        line["materialised"] = materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, "lanczos" in legs,
+                                                w.name)
     if "cpu" in legs and rank == 0:
         # One whole apply of the reference's push loop (oracle restatement) on all host cores, on the headline's
         # x: the CPU baseline (whole apply, no sample) and the full-size parity check of the GPU results.

@@ -307,8 +307,9 @@ typedef struct qsi_lanczos_cfg {
     double tol;           /* relative residual tolerance (10^--atol) */
     uint64_t seed;        /* start vector seed (N(0,1)) */
     int32_t polish_steps; /* FP64 Rayleigh-Ritz polish rounds after convergence; with QSI_F32 and
-                             >= 2 rounds the FP32 Krylov phase stops at max(tol, 1e-7) and the
-                             FP64 rounds (the 2nd on [X, HX - X theta]) refine the pairs */
+                             >= 2 rounds the FP32 Krylov phase stops at max(tol, 1e-7), ten times
+                             looser per round beyond two (at most 1e-4), and the FP64 rounds (the
+                             2nd and later on [X, HX - X theta]) refine the pairs */
     int32_t want_vectors; /* write eigenvectors */
     int32_t block;        /* QSI_F32 only: 16 = block Lanczos on FP32 blocks of 16 vectors through the
                              batched apply (nev <= 13); 0 or 1 = single-vector Lanczos on FP32 vectors */

@@ -809,6 +809,11 @@ static qsi_status finish_solve(qsi_op* op, const qsi_lanczos_cfg& cfg, Vecs& vx,
 }
 
 
+// Relative residual at which an FP32 Krylov phase hands its pairs to `rounds` FP64 polish rounds: 1e-7 (what FP32
+// vectors resolve) for two rounds, ten times looser for each further round (at most 1e-4), which trades FP32
+// restarts for FP64 residual-augmented Rayleigh-Ritz rounds.
+static double fp32_stop(int rounds) { return std::min(1e-4, 1e-7 * std::pow(10.0, std::max(0, rounds - 2))); }
+
 // Thick-restart Lanczos (Wu & Simon) for the nev smallest eigenpairs.
 template <typename VT>
 static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, double* evecs, qsi_report* rep) {
@@ -823,7 +828,7 @@ static qsi_status trlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, d
     // Rayleigh-Ritz): the Krylov phase stops at a residual FP32 vectors resolve (1e-7 relative) and the FP64
     // rounds take the pairs the rest of the way; otherwise it runs to tol itself.
     const double tol_req = cfg.tol > 0 ? cfg.tol : 1e-10;
-    const double tol = (sizeof(VT) == 4 && cfg.polish_steps >= 2) ? std::max(tol_req, 1e-7) : tol_req;
+    const double tol = (sizeof(VT) == 4 && cfg.polish_steps >= 2) ? std::max(tol_req, fp32_stop(cfg.polish_steps)) : tol_req;
     const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
     Vecs vx;
     qsi_status s = vx.init(n, st);
@@ -1232,7 +1237,7 @@ static qsi_status btrlan(qsi_op* op, const qsi_lanczos_cfg& cfg, double* evals, 
     if (kb + 2 > nblk || nev > keep || (int64_t)(nblk + 1) * kBlk > n)
         return fail(QSI_INVALID_ARG, "block lanczos: nev %d needs more Krylov blocks than fit (dim %lld)", nev, (long long)n);
     const int m = nblk * kBlk;
-    const double tol = std::max(cfg.tol > 0 ? cfg.tol : 1e-10, cfg.polish_steps >= 2 ? 1e-7 : 0.0);
+    const double tol = std::max(cfg.tol > 0 ? cfg.tol : 1e-10, cfg.polish_steps >= 2 ? fp32_stop(cfg.polish_steps) : 0.0);
     const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
     // nblk + 1 Krylov blocks, W and one spare block (the Cholesky QR output; also half of the restart scratch)
     std::vector<DevBuf<float>> store(nblk + 3);

@@ -505,7 +505,7 @@ def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves,
             out["ftlm"]["speedup_vs_plain_fp64"] = mixed["vec_steps_per_s"] / plain["vec_steps_per_s"]
     if with_solves:
         sol = {}
-        for prec, polish in (("f64", 0), ("mixed", 2)):
+        for prec, polish in (("f64", 0), ("mixed", 3)):
             torch.cuda.synchronize()
             t0 = time.time()
             ev, _, rep = q.diagonalise(op, nev=args.nev, ncv=args.ncv, tol=1e-10, max_iter=400, seed=1,
@@ -724,7 +724,7 @@ def run_ours(args):
         torch.cuda.empty_cache()
         out = {"nev": args.nev, "ncv": args.ncv, "tol": 1e-10}
         res = {}
-        for prec, polish in (("f64", 0), ("mixed", 2)):
+        for prec, polish in (("f64", 0), ("mixed", 3)):
             torch.cuda.synchronize()
             t0 = time.time()
             ev, _, rep = q.diagonalise(op, nev=args.nev, ncv=args.ncv, tol=1e-10, max_iter=400, seed=1,

@@ -857,8 +857,11 @@ __global__ void __launch_bounds__(256) k_apply_cached(const PullTerm* __restrict
 #pragma unroll
             for (int u = 0; u < kU; ++u)
                 if (c[u] != kEmpty && above_tol(xv[u])) {
-                    const double v = cs[t[u]];
-                    acc += ((c[u] & kCacheNeg) ? -v : v) * (double)xv[u];
+                    // -cs for a negative entry as a flip of the sign bit (integer work, exactly the negation), so
+                    // the FP64 pipe, GB300's bottleneck here, sees one multiply-add per hit
+                    const double v = __longlong_as_double(__double_as_longlong(cs[t[u]]) ^
+                                                          ((unsigned long long)(c[u] & kCacheNeg) << 32));
+                    acc += v * (double)xv[u];
                 }
         }
         if (valid) {

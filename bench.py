@@ -64,7 +64,7 @@ def parse():
     p.add_argument("--serve-rate", type=float, default=40.0)
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--serve-96", action="store_true",
-                   help="serve leg: the config-5 mix with the 96-spin sector (32-spin Q=0, 64-spin Q=0, 96-spin "
+                   help="serve leg: the request mix with the 96-spin sector (32-spin Q=0, 64-spin Q=0, 96-spin "
                         "12.12.12.12; weights 0.5/0.35/0.15) instead of the 64-spin 8.8.8.8 sector")
     p.add_argument("--ncv", type=int, default=24)
     return p.parse_args()
@@ -303,7 +303,7 @@ def torch_sync():
 
 
 def serve_leg(args):
-    """Request loop (config 5 scaled to the bench's time): Poisson phase-diagram points over three resident sectors,
+    """Request loop (the phase-diagram request mix, scaled to the bench's time): Poisson points over three resident sectors,
     served with `slots` concurrent solves and same-sector continuous batching (operator families: concurrent
     requests' applies run as columns of one batched apply), against the same requests solved one after another
     without batching (plain FP64 GPU solves)."""
@@ -318,7 +318,7 @@ def serve_leg(args):
                    "pyro_1x2x3.s12.12.12.12": serve.Sector("pyro_1x2x3.s12.12.12.12", l96,
                                                             q.enumerate_basis_gpu(l96, workloads.equal_sector(l96)))}
         weights = {"pyro_1x2x1.Q0": 0.5, "pyro_1x2x2.Q0": 0.35, "pyro_1x2x3.s12.12.12.12": 0.15}
-        note = "the config-5 mix with the 96-spin sector; admission by HBM footprint lets about two of its solves run at once"
+        note = "the request mix with the 96-spin sector; admission by HBM footprint lets two or three of its solves run at once"
     else:
         sectors = {"pyro_1x2x1.Q0": serve.Sector("pyro_1x2x1.Q0", l32, q.enumerate_basis(l32)),
                    "pyro_1x2x2.s8.8.8.8": serve.Sector("pyro_1x2x2.s8.8.8.8", l64,
@@ -730,7 +730,7 @@ def run_ours(args):
         line["ftlm"] = {"value": mixed["vec_steps_per_s"], "unit": "vec-steps/s", "mixed": mixed, "plain_fp64": plain,
                         "speedup_vs_plain_fp64": mixed["vec_steps_per_s"] / plain["vec_steps_per_s"]}
     if "lanczos" in legs and rank == 0:
-        # 96-spin eigen-solves (the workloads of configs 2 and 3): the nev lowest eigenpairs in plain FP64 and in
+        # 96-spin eigen-solves (the FP64 and mixed-precision solves of the sector): the nev lowest eigenpairs in plain FP64 and in
         # mixed precision (FP32 Krylov vectors and gathers, FP64 recurrences, FP64 Rayleigh-Ritz polish), and the
         # errors of the mixed eigenvalues against the FP64 ones
         del x, y

@@ -730,7 +730,7 @@ def run_ours(args):
         line["ftlm"] = {"value": mixed["vec_steps_per_s"], "unit": "vec-steps/s", "mixed": mixed, "plain_fp64": plain,
                         "speedup_vs_plain_fp64": mixed["vec_steps_per_s"] / plain["vec_steps_per_s"]}
     if "lanczos" in legs and rank == 0:
-        # 96-spin eigen-solves (the FP64 and mixed-precision solves of the sector): the nev lowest eigenpairs in plain FP64 and in
+        # 96-spin eigen-solves: the nev lowest eigenpairs in plain FP64 and in
         # mixed precision (FP32 Krylov vectors and gathers, FP64 recurrences, FP64 Rayleigh-Ritz polish), and the
         # errors of the mixed eigenvalues against the FP64 ones
         del x, y

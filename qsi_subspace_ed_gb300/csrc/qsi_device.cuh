@@ -204,7 +204,9 @@ struct LookupTable {
 
 struct LookupHash {
     HashView H;
-    static constexpr int kNB = 4, kMinBlocks = 3;
+    // 4 resident blocks (64 registers, a 64-byte spill): 66.9 ms against 74-75 ms at 3 (80 registers) on the
+    // 96-spin sector, whose single-vector apply is bound by the latency of its dependent lookups
+    static constexpr int kNB = 4, kMinBlocks = 4;
     __device__ __forceinline__ int64_t find(uint64_t lo, uint64_t hi) const { return hash_find(H, lo, hi); }
     __device__ __forceinline__ uint64_t cursor(int64_t, int) const { return 0; }
     // every state's region (one table load each), then every first probe, before resolving any

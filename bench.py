@@ -485,8 +485,7 @@ def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves,
                                       "kernel": "k_apply_cached<double,double,uint8>",
                                       "traffic": measured_traffic(workload, "k_apply_cached<double,double,uint8>", n)}}
     del y
-    Rs = [int(v) for v in str(args.R).split(",") if v]
-    for R in Rs[1:] + Rs[:1]:  # the first of --R (FTLM's R) last, so its tuned settings stay for the FTLM run
+    for R in [int(v) for v in str(args.R).split(",") if v]:
         torch.cuda.empty_cache()
         try:
             X = torch.randn(n, R, dtype=torch.float32, device=x.device)
@@ -494,8 +493,6 @@ def materialised_leg(args, q, op, n, h, x, y_host, peak, peak_kind, with_solves,
         except torch.cuda.OutOfMemoryError as e:
             out[f"batched_r{R}"] = {"skipped": str(e)[:160]}
             continue
-        if not args.no_tune:  # the cached batched kernels' own launch settings (lists, lanes, blocks per SM)
-            out.setdefault("tuning", {})[f"r{R}"] = op.autotune(R=R, dtype="f32", X=X, Y=Y).splitlines()[-1]
         torch.cuda.nvtx.range_push(f"timed_materialised_r{R}")
         ms = event_ms(lambda: op.apply_batched(X, Y), max(3, args.steps // 3), 1)
         torch.cuda.nvtx.range_pop()

@@ -692,15 +692,8 @@ __device__ __forceinline__ void batched_body(const TileParams& P, const LK& lk, 
     }
 }
 
-// Resident 256-thread blocks per SM of the batched kernels: 2 for 16-byte gathers (they hold a row's gathers in
-// flight in registers), 3 otherwise, and 3 for 8 vectors per lane with the lookup cache, which then needs no spill.
-template <class LK, int KM>
-constexpr int batched_min_blocks() {
-    return (KM == kVec8 && std::is_same<LK, LookupCache>::value) ? 3 : (KM <= kVec4 ? 2 : 3);
-}
-
 template <typename XT, class LK, bool kFF, int KM, bool kFam = false>
-__global__ void __launch_bounds__(256, batched_min_blocks<LK, KM>()) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
+__global__ void __launch_bounds__(256, KM <= kVec4 ? 2 : 3) k_apply_tile_batched(TileParams P, LK lk, const XT* __restrict__ x,
                                                             XT* __restrict__ y, int R, int accumulate, int cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     batched_body<XT, LK, kFF, KM, kFam>(P, lk, x, y, R, accumulate, cap, blockIdx.x, gridDim.x, smem_raw);
@@ -726,7 +719,7 @@ struct SectorLaunch {
 };
 
 template <int KM, class LK>
-__global__ void __launch_bounds__(256, batched_min_blocks<LK, KM>()) k_apply_sectors(const SectorLaunch* __restrict__ secs, int n_secs,
+__global__ void __launch_bounds__(256, KM <= kVec4 ? 2 : 3) k_apply_sectors(const SectorLaunch* __restrict__ secs, int n_secs,
                                                           int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SectorLaunch L;
@@ -1131,8 +1124,7 @@ qsi_status plan_sectors(qsi_op* const* ops, int n, const float* const* X, float*
     if (smem > 227 * 1024) return fail(QSI_INVALID_ARG, "sector launch: %zu bytes of shared memory needed", smem);
     // one wave of the kernel's resident blocks per SM, or the first sector's tuned blocks per SM
     const int bps = ops[0]->tune[1].grid_bps;
-    const int resident = plan.vec4 ? ((plan.cache && plan.vec8 && !plan.vec16) ? 3 : 2) : 3;  // batched_min_blocks
-    const int total = sms * (bps > 0 ? bps : resident);
+    const int total = sms * (bps > 0 ? bps : plan.vec4 ? 2 : 3);
     int begin = 0;
     for (int s = 0; s < n; ++s) {
         const int64_t tiles = (ops[s]->basis->n + 31) / 32;

@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(256, LK::kMinBlocks) k_apply_tile(TileParams P
 // k_apply_tile forms for that column alone (same terms in the same order, same coefficients and tests), so a
 // member's result does not depend on the batch it ran in.
 template <class LK, int RC>
-__global__ void __launch_bounds__(256, RC <= 4 ? 3 : 2) k_apply_tile_cols(TileParams P, LK lk, const double* __restrict__ x,
+__global__ void __launch_bounds__(256, RC <= 4 ? 4 : 2) k_apply_tile_cols(TileParams P, LK lk, const double* __restrict__ x,
                                                             double* __restrict__ y, int accumulate) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TileSmem S = stage_terms(P, smem_raw);

@@ -401,6 +401,15 @@ def test_states_up_to_128_bits():
         op.apply_batched(X, Y)
         ref0 = O.apply_port(lohi, specs, X[:, 5].astype(np.float64), threads=1)
         np.testing.assert_allclose(Y[:, 5], ref0, rtol=0, atol=4e-6 * np.abs(ref0).max())
+    # materialised without a hash index (the cache filled through the bucket table): bitwise the same applies
+    assert op.materialise(True) > 0
+    y3 = np.zeros_like(x)
+    op.evaluate(x, y3)
+    assert np.array_equal(y3, y)
+    Y3 = np.zeros_like(X)
+    op.apply_batched(X, Y3)
+    assert np.array_equal(Y3, Y)
+    op.materialise(False)
 
 
 def test_degenerate_sizes():

@@ -1264,26 +1264,41 @@ qsi_status materialise(qsi_op* op, bool enable, int64_t* bytes) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((ntiles + nw - 1) / nw, (int64_t)sms * 8));
         // widths, their exclusive scan (tile offsets in cache lines), then the columns
+        // the scratch arrays are freed, and a failure leaves no partial cache behind, on every path out
         uint64_t* width = nullptr;
-        QSI_CUDA(cudaMallocAsync(&width, (size_t)(ntiles + 1) * 8, st));
-        QSI_CUDA(cudaMallocAsync(&op->d_cache_off, (size_t)(ntiles + 1) * 8, st));
-        QSI_CUDA(cudaMemsetAsync(width + ntiles, 0, 8, st));
+        void* tmp = nullptr;
+        auto scratch_free = [&]() {
+            cudaFreeAsync(tmp, st);
+            cudaFreeAsync(width, st);
+            tmp = nullptr;
+            width = nullptr;
+        };
+        auto fail_partial = [&](cudaError_t e, const char* what) {
+            scratch_free();
+            cudaFree(op->d_cache_off);
+            op->d_cache_off = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? QSI_OOM : QSI_CUDA_ERROR, "qsi_op_materialise: %s: %s", what,
+                        cudaGetErrorString(e));
+        };
+        cudaError_t e = cudaMallocAsync(&width, (size_t)(ntiles + 1) * 8, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&op->d_cache_off, (size_t)(ntiles + 1) * 8, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(width + ntiles, 0, 8, st);
+        if (e != cudaSuccess) return fail_partial(e, "tile offsets");
         const size_t smem_w = term_smem(op) + (size_t)nw * 512;
         set_smem(k_cache_widths, smem_w);
         k_cache_widths<<<grid, block, smem_w, st>>>(P, width);
         size_t tmp_bytes = 0;
-        QSI_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, width, op->d_cache_off, ntiles + 1, st));
-        void* tmp = nullptr;
-        QSI_CUDA(cudaMallocAsync(&tmp, tmp_bytes, st));
-        QSI_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, width, op->d_cache_off, ntiles + 1, st));
+        e = cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, width, op->d_cache_off, ntiles + 1, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&tmp, tmp_bytes, st);
+        if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, width, op->d_cache_off, ntiles + 1, st);
         uint64_t lines = 0;
-        QSI_CUDA(cudaMemcpyAsync(&lines, op->d_cache_off + ntiles, 8, cudaMemcpyDeviceToHost, st));
-        QSI_CUDA(cudaStreamSynchronize(st));
-        cudaFreeAsync(tmp, st);
-        cudaFreeAsync(width, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&lines, op->d_cache_off + ntiles, 8, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail_partial(e, "tile widths");
+        scratch_free();
         const size_t n_entries = (size_t)lines * 32;
         op->cache_tid_bytes = op->n_pull <= 256 ? 1 : 2;
-        cudaError_t e = cudaMalloc(&op->d_cache_cols, std::max<size_t>(n_entries, 1) * 4);
+        e = cudaMalloc(&op->d_cache_cols, std::max<size_t>(n_entries, 1) * 4);
         if (e == cudaSuccess) e = cudaMalloc(&op->d_cache_tid, std::max<size_t>(n_entries, 1) * op->cache_tid_bytes);
         if (e != cudaSuccess) {
             cudaFree(op->d_cache_off);
@@ -1295,8 +1310,18 @@ qsi_status materialise(qsi_op* op, bool enable, int64_t* bytes) {
                         "qsi_op_materialise: %zu bytes for the cache: %s", n_entries * (4 + op->cache_tid_bytes),
                         cudaGetErrorString(e));
         }
-        QSI_CUDA(cudaMemsetAsync(op->d_cache_cols, 0xFF, n_entries * 4, st));  // the lanes below their tile's width
-        QSI_CUDA(cudaMemsetAsync(op->d_cache_tid, 0, n_entries * op->cache_tid_bytes, st));
+        auto drop_cache = [&](cudaError_t err) {  // a cache that was not filled completely is never used
+            cudaFree(op->d_cache_cols);
+            cudaFree(op->d_cache_tid);
+            cudaFree(op->d_cache_off);
+            op->d_cache_cols = nullptr;
+            op->d_cache_tid = nullptr;
+            op->d_cache_off = nullptr;
+            return fail(QSI_CUDA_ERROR, "qsi_op_materialise: %s", cudaGetErrorString(err));
+        };
+        e = cudaMemsetAsync(op->d_cache_cols, 0xFF, n_entries * 4, st);  // the lanes below their tile's width
+        if (e == cudaSuccess) e = cudaMemsetAsync(op->d_cache_tid, 0, n_entries * op->cache_tid_bytes, st);
+        if (e != cudaSuccess) return drop_cache(e);
         const size_t smem_f = term_smem(op) + (size_t)nw * (512 + (size_t)n_rounds * 128);
         auto fill = [&](auto lk, auto* tids) {
             auto k = k_cache_fill<decltype(lk), std::remove_pointer_t<decltype(tids)>>;
@@ -1310,8 +1335,9 @@ qsi_status materialise(qsi_op* op, bool enable, int64_t* bytes) {
             if (op->cache_tid_bytes == 1) fill(LookupTable{op->basis->view()}, (uint8_t*)op->d_cache_tid);
             else fill(LookupTable{op->basis->view()}, (uint16_t*)op->d_cache_tid);
         }
-        QSI_CUDA(cudaGetLastError());
-        QSI_CUDA(cudaStreamSynchronize(st));
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return drop_cache(e);
         op->cache_entries = n_entries;
     }
     if (bytes)

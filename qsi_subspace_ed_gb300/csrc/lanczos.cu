@@ -161,41 +161,6 @@ __global__ void __launch_bounds__(kRedBlock) k_multi_axpy(const VT* __restrict__
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-// FP32 Krylov vectors: w -= sum_i h_i V_i with the sum formed in double-float (h_i as float pairs; four
-// interleaved partial sums combined in a fixed order, so four loads per row are in flight and the dependent chain
-// is a quarter as long) and one FP64 subtraction per row; partial[b] = this block's sum of the new w^2.
-__global__ void __launch_bounds__(kRedBlock) k_multi_axpy_f32(const float* __restrict__ V, int64_t ld_v, int k,
-                                                              const double* __restrict__ h, double* __restrict__ w,
-                                                              int64_t n, double* __restrict__ partial) {
-    __shared__ double sh[32];
-    __shared__ float hh[256], hl[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-        hh[i] = hl[i] = 0.f;
-        if (i < k) df_split(h[i], hh[i], hl[i]);
-    }
-    __syncthreads();
-    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-    const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
-    const int k4 = (k + 3) & ~3;
-    double acc = 0.0;
-    for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) {
-        DF s[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-        for (int i = 0; i < k4; i += 4) {
-            float v[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = __ldg(V + (int64_t)min(i + u, k - 1) * ld_v + r);  // h = 0 past k
-#pragma unroll
-            for (int u = 0; u < 4; ++u) df_fma(s[u], hh[i + u], hl[i + u], v[u]);
-        }
-        const double t = (df_value(s[0]) + df_value(s[1])) + (df_value(s[2]) + df_value(s[3]));
-        const double v = w[r] - t;
-        w[r] = v;
-        acc += v * v;
-    }
-    const double t = block_sum(acc, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = t;
-}
-
 // The working vector of the FP32 solve as a double-float pair array: split once per Lanczos step, then the
 // reorthogonalisation (dots, updates, norms) and the store of the next Krylov vector run on the FP32 pipe with no
 // FP64 operation per row.
@@ -249,8 +214,9 @@ __global__ void __launch_bounds__(kRedBlock) k_multidot_df(const float* __restri
     const double t = block_sum(df_value(nrm), sh);
     if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * (k + 1) + k] = t;
 }
-// w -= sum_i h_i V_i on the pair array (the sum as in k_multi_axpy_f32, the subtraction in double-float);
-// partial[b] = this block's |w|^2.
+// w -= sum_i h_i V_i on the pair array: the sum in double-float with h_i as float pairs (four interleaved partial
+// sums combined in a fixed order, so four loads per row are in flight and the dependent chain is a quarter as
+// long), the subtraction in double-float; partial[b] = this block's |w|^2.
 __global__ void __launch_bounds__(kRedBlock) k_multi_axpy_df(const float* __restrict__ V, int64_t ld_v, int k,
                                                              const double* __restrict__ h, float2* __restrict__ wf,
                                                              int64_t n, double* __restrict__ partial) {
@@ -603,8 +569,7 @@ struct Vecs {
     template <typename VT>
     qsi_status axpy(const VT* V, int64_t ldv, int k, const std::vector<double>& h, double* w, double& nrm2) {
         QSI_CUDA(cudaMemcpyAsync(red + 1, h.data(), (size_t)k * 8, cudaMemcpyHostToDevice, st));
-        if constexpr (sizeof(VT) == 4) k_multi_axpy_f32<<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, red + 1, w, n, partial);
-        else k_multi_axpy<VT><<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, red + 1, w, n, partial);
+        k_multi_axpy<VT><<<kRedGrid, kRedBlock, 0, st>>>(V, ldv, k, red + 1, w, n, partial);
         k_reduce_partials<<<1, 256, 0, st>>>(partial, kRedGrid, 1, red);
         QSI_CUDA(cudaMemcpyAsync(&nrm2, red, 8, cudaMemcpyDeviceToHost, st));
         QSI_CUDA(cudaStreamSynchronize(st));

@@ -264,3 +264,16 @@ def test_device_path_fails_loudly_without_a_gpu():
     basis = workloads.q0_32spin().basis_lohi
     with pytest.raises(q.QsiError, match="QSI_CUDA_ERROR"):
         q.ZBasis(basis)
+
+
+def test_new_entry_points_reject_null_handles():
+    """qsi_op_materialise and qsi_family_set_min_rows return QSI_INVALID_ARG for a null handle (no GPU needed)."""
+    import ctypes as C
+
+    from qsi_subspace_ed_gb300 import _lib
+
+    lib = q.load()
+    nb = C.c_int64()
+    assert lib.qsi_op_materialise(None, 1, C.byref(nb)) == _lib.QSI_INVALID_ARG
+    assert lib.qsi_op_materialise(None, 0, None) == _lib.QSI_INVALID_ARG
+    assert lib.qsi_family_set_min_rows(None, 0) == _lib.QSI_INVALID_ARG
